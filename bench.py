@@ -1,0 +1,318 @@
+"""Benchmark: cell-updates/s of the KKS step on one GB300.
+
+Workload (the single-grid configuration): 2D 4096 x 4096 grid, dx = 5 nm,
+16 enriched stripes and 64 particles at seeded positions, zero-flux
+boundaries, 5-point Laplacian, explicit Euler at the stability-limited dt,
+Philox nucleation every 100 steps (seed 42, the reference's physical
+nucleation parameters).  One benchmark step = 100 time steps + the
+nucleation call of that interval.  The headline `value` is the FP32
+precision form with fields resident in HBM; `fp64` is the plain FP64 fused
+step on the same workload; `e2e` goes through the C ABI with host buffers
+(upload of the four FP64 fields, 100 steps, read-out) every step.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun each rank runs an independent replica on its own GPU
+(replicas only: the grids do not exchange data), so scaling is weak.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "phasefield-precipitate-aging_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+METRIC = "cell-updates/s FP32 vs plain FP64 on one GB300 at stated error; p50/p99 latency"
+N_SIDE = 4096
+STEPS_PER_BENCH_STEP = 100
+NUC = dict(sigma=(0.13, 0.13), unit_a=0.352e-9)
+WORKLOAD = (f"single 2D grid {N_SIDE}x{N_SIDE}, dx=5nm, 16 enriched stripes + 64 particles "
+            f"(seeded), zero-flux, 5-point Laplacian, KKS-stable dt, Philox nucleation every "
+            f"{STEPS_PER_BENCH_STEP} steps (seed 42); one bench step = {STEPS_PER_BENCH_STEP} "
+            f"time steps + 1 nucleation call")
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm = [float(r[1]) for r in self.rows if len(r) > 8 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 8 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows if len(r) > 8
+                          for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def measured_peak_hbm():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(kernel):
+    """dram read+write bytes per launch from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}.txt")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+def cpu_baseline(fields, params, steps, fast=True):
+    """The CPU oracle (the reference's step semantics, reference host flags,
+    OpenMP on every host core) on the same workload."""
+    import oracle as O
+    O.build(fast=True)
+    lib = O.Oracle(os.path.join(ROOT, "oracle", "liboracle_fast.so" if fast else "liboracle.so"))
+    prm = O.OrcParams.from_dict(params)
+    t0 = time.perf_counter()
+    lib.run2d(fields, prm, steps)
+    return time.perf_counter() - t0
+
+
+def run_reference(args, ws, rank):
+    """--impl reference: the CPU path timed on this host's cores."""
+    if rank != 0:
+        return
+    from pfa_gb300 import ic, lib as pl
+    fields = ic.config2(n=N_SIDE)
+    import oracle as O
+    params = O.model_params().as_dict()
+    per = 2  # time steps per bench step of this arm (a bounded sample)
+    for _ in range(args.warmup):
+        cpu_baseline(fields, params, per)
+    t = 0.0
+    for _ in range(args.steps):
+        t += cpu_baseline(fields, params, per)
+    cells = N_SIDE * N_SIDE
+    value = cells * per * args.steps / t
+    cores = os.cpu_count()
+    line = {"metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD, "sample": f"{per} time steps of the full grid per step"},
+            "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": cores,
+                             "kind": "port",
+                             "sample": f"{per} FP64 time steps of the {N_SIDE}^2 grid per step"},
+            "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp32k"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    args = ap.parse_args()
+    ws, rank, local = dist_env()
+    if args.warmup < 3:
+        args.warmup = 3
+
+    if args.impl == "reference":
+        if ws > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+        run_reference(args, ws, rank)
+        return
+
+    import torch
+    from pfa_gb300 import build, ic, lib as pl
+    build.build()
+    L = pl.load()
+    pl.check(L.pfa_set_device(local), "pfa_set_device")
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    fields = ic.config2(seed=2 + rank, n=N_SIDE)
+    params = pl.model_params()
+    cells = N_SIDE * N_SIDE
+    nuc_kw = dict(seed=42, geometry=pl.NUC_REFERENCE_GEOMETRY, interval=STEPS_PER_BENCH_STEP,
+                  sigma=NUC["sigma"], unit_a=NUC["unit_a"], d=(params["dx"],) * 3,
+                  dt_nuc=STEPS_PER_BENCH_STEP * params["dt"])
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---- device-resident FP32 precision form (headline value) ----
+    g = pl.Grid2D(fields, params, precision=args.precision)
+    g.set_nucleation(**nuc_kw)
+    g.run(args.warmup * STEPS_PER_BENCH_STEP)
+    g.sync()
+    barrier()
+    with ClockSampler(local) as clk:
+        ms = g.run_timed(args.steps * STEPS_PER_BENCH_STEP)
+    barrier()
+    t = max_over_ranks(ms / 1e3)
+    value = ws * cells * STEPS_PER_BENCH_STEP * args.steps / t
+
+    # kernel-only time of the step kernel (no nucleation): average launch
+    g2 = pl.Grid2D(fields, params, precision=args.precision)
+    g2.run(200)
+    kms = g2.run_timed(400) / 400
+    g2.close()
+    bytes_per_cell = 48 if args.precision == "fp32" else 64
+    peak, peak_kind = measured_peak_hbm()
+    achieved = bytes_per_cell * cells / (kms / 1e3) / 1e9
+    kname = "step2d_f32_4096" if args.precision == "fp32" else "step2d_f32k_4096"
+    traffic = profiled_traffic(kname)
+
+    # ---- plain FP64 fused step on the same workload ----
+    g64 = pl.Grid2D(fields, params, precision="fp64")
+    g64.set_nucleation(**nuc_kw)
+    g64.run(STEPS_PER_BENCH_STEP)
+    ms64 = g64.run_timed(STEPS_PER_BENCH_STEP)
+    fp64_value = cells * STEPS_PER_BENCH_STEP / (ms64 / 1e3)
+
+    # ---- stated error: FP32 form vs FP64 after the same 400 steps ----
+    ga = pl.Grid2D(fields, params, precision=args.precision)
+    gb = pl.Grid2D(fields, params, precision="fp64")
+    ga.run(400)
+    gb.run(400)
+    fa, fb = ga.read(), gb.read()
+    err = [float(np.max(np.abs(a[1:-1, 1:-1] - b[1:-1, 1:-1]))) for a, b in zip(fa, fb)]
+    ga.close()
+    gb.close()
+    g64.close()
+
+    # ---- e2e through the C ABI with host buffers ----
+    host_in = []
+    host_out = []
+    for a in fields:
+        h = torch.empty(a.shape, dtype=torch.float64, pin_memory=True).numpy()
+        h[...] = a
+        host_in.append(h)
+        host_out.append(torch.empty(a.shape, dtype=torch.float64, pin_memory=True).numpy())
+    ge = pl.Grid2D(fields, params, precision=args.precision)
+    ge.set_nucleation(**nuc_kw)
+    for _ in range(1):
+        ge.upload(host_in)
+        ge.run(STEPS_PER_BENCH_STEP)
+        ge.read(host_out)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ge.upload(host_in)
+        ge.run(STEPS_PER_BENCH_STEP)
+        ge.read(host_out)
+    barrier()
+    te = max_over_ranks(time.perf_counter() - t0)
+    ge.close()
+    e2e_value = ws * cells * STEPS_PER_BENCH_STEP * args.steps / te
+    io_bytes = 4 * fields[0].size * 8
+
+    line = None
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu:
+            sample_steps = 3
+            tc = cpu_baseline(fields, pl.model_params(), sample_steps)
+            cpu = {"value": cells * sample_steps / tc, "unit": "cell-updates/s",
+                   "cores": os.cpu_count(), "kind": "port",
+                   "sample": f"{sample_steps} FP64 time steps of the {N_SIDE}^2 grid, "
+                             f"OpenMP, reference host flags"}
+        line = {
+            "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "nx": N_SIDE, "ny": N_SIDE,
+                       "precision": args.precision, "dt": params["dt"],
+                       "l2": "inputs larger than L2 (FP32 state 6 x 67 MB)",
+                       "parallelism": f"replicas x{ws}"},
+            "fp64": {"value": fp64_value, "unit": "cell-updates/s",
+                     "ms_per_step": ms64, "speedup_fp32_over_fp64": value / ws / fp64_value},
+            "max_field_error": {"vs": "fp64 GPU step (pinned to the reference at 1e-12)",
+                                "steps": 400, "x_Cr": err[0], "x_Nb": err[1],
+                                "phi_delta": err[2], "phi_laves": err[3]},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "kernel": "k_step2d_f32", "bytes_per_cell": bytes_per_cell,
+                         "kernel_ms": kms, "peak_kind": peak_kind},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": io_bytes,
+                    "d2h_bytes_per_step": io_bytes},
+            "gpu_launches": args.steps * (STEPS_PER_BENCH_STEP + 2),
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line))
+    g.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

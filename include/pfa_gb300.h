@@ -1,0 +1,130 @@
+/*
+ * pfa_gb300.h -- extern "C" interface of libpfa_gb300.so.
+ *
+ * Plain pointers and sizes only.  This is the surface a non-C++ caller
+ * (ctypes, cgo, JNI, ...) binds.  Each function below mirrors one
+ * reference entry point of usnistgov/phasefield-precipitate-aging with host
+ * arrays passed flat instead of through HostData (the C++ drop-in with the
+ * reference's own signatures is pfa_reference_abi.h), or adds a capability
+ * the reference's loop needs from its caller (multi-step runs, 3D grids,
+ * batches of grids).
+ *
+ * Layout of every 2D field: row-major (ny x nx) doubles with a one-cell ghost
+ * ring, nx = Nx + 2, ny = Ny + 2 (src/main.cpp:229-233).  3D fields are
+ * (nz x ny x nx) with the same ring.  Field order: x_Cr, x_Nb, phi_delta,
+ * phi_laves.
+ *
+ * Every function returns 0 on success or a PFA_E* code, which also becomes
+ * the sticky error word (pfa_last_error).  Nothing here falls back to the
+ * CPU: without a usable GPU the calls fail with PFA_ECUDA.
+ */
+#ifndef PFA_GB300_H
+#define PFA_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+struct CudaData; /* layout in pfa_reference_abi.h (src/type.h:58-107) */
+
+enum {
+	PFA_OK = 0,
+	PFA_EINVAL = 1,   /* bad argument or unsupported configuration */
+	PFA_ECUDA = 2,    /* a CUDA runtime call failed */
+	PFA_ESTATE = 3,   /* CudaData not initialised by this library */
+	PFA_EOVERFLOW = 4,/* an event buffer overflowed */
+	PFA_ENOMEM = 5    /* device allocation failed */
+};
+
+enum { PFA_MODE_FUSED = 0, PFA_MODE_COMPAT = 1 };
+enum { PFA_FP64 = 0, PFA_FP32 = 1, PFA_FP32_KPHI = 2 };
+enum { PFA_NUC_REFERENCE_GEOMETRY = 0, PFA_NUC_FIXED_GEOMETRY = 1 };
+
+/* ---- errors (replaces checkCuda's assert, src/discretization.cu:23-30) ---- */
+int pfa_last_error(void);
+const char* pfa_error_string(int code);
+const char* pfa_last_error_message(void);
+void pfa_clear_error(void);
+
+/* ---- device selection (cudaSetDevice for this library's runtime) ---- */
+int pfa_set_device(int device);
+int pfa_device_count(void);
+
+/* ---- configuration of one CudaData (library-side table) ---- */
+int pfa_set_mode(struct CudaData* dev, int mode);
+int pfa_set_precision(struct CudaData* dev, int precision);
+int pfa_set_nucleation(struct CudaData* dev, uint64_t seed, int geometry);
+
+/* ---- mirrors of the reference entry points ---- */
+/* init_cuda, src/data.cuh:21-25 / src/data.cu:10-92; mask is nm*nm doubles */
+int pfa_init_cuda(struct CudaData* dev, int nx, int ny, int nm, const double* mask,
+                  const double* kappa, const double* omega, const double* Lmob,
+                  const double* D_Cr, const double* D_Nb, const double* conc_Cr,
+                  const double* conc_Nb, const double* phi_del, const double* phi_lav);
+/* free_cuda, src/data.cuh:30 / src/data.cu:94-154 */
+int pfa_free_cuda(struct CudaData* dev);
+/* read_out_result, src/data.cuh:35 / src/data.cu:156-172 */
+int pfa_read_out_result(struct CudaData* dev, double* conc_Cr, double* conc_Nb,
+                        double* phi_del, double* phi_lav, int nx, int ny);
+/* the host-to-device half of init_cuda (src/data.cu:83-91) on a live CudaData */
+int pfa_upload_fields(struct CudaData* dev, const double* conc_Cr, const double* conc_Nb,
+                      const double* phi_del, const double* phi_lav, int nx, int ny);
+/* src/discretization.cuh:39-111 */
+int pfa_device_boundaries(struct CudaData* dev, int nx, int ny, int nm, int bx, int by);
+int pfa_device_fictitious(struct CudaData* dev, int nx, int ny, int nm, int bx, int by);
+int pfa_fictitious_boundaries(struct CudaData* dev, int nx, int ny, int nm, int bx, int by);
+int pfa_device_laplacian(struct CudaData* dev, int nx, int ny, int nm, int bx, int by,
+                         double dx, double dy);
+int pfa_device_laplacian_boundaries(struct CudaData* dev, int nx, int ny, int nm, int bx, int by);
+int pfa_device_evolution(struct CudaData* dev, int nx, int ny, int nm, int bx, int by,
+                         double alpha, double dt);
+int pfa_device_init_prng(struct CudaData* dev, int nx, int ny, int nm, int bx, int by);
+int pfa_device_nucleation(struct CudaData* dev, int nx, int ny, int nm, int bx, int by,
+                          double sigma_del, double sigma_lav, double unit_a, double ifce_width,
+                          double dx, double dy, double dz, double dt);
+/* device_dataviz, src/discretization.cuh:116 / src/discretization.cu:1231-1263 */
+int pfa_device_dataviz(struct CudaData* dev, double* conc_Cr, double* conc_Nb, double* conc_Ni,
+                       double* phi_del, double* phi_lav, double* phi, int nx, int ny);
+/* the caller-side pointer swap of src/main.cpp:318-321 */
+int pfa_swap(struct CudaData* dev);
+
+/* ---- the update loop of src/main.cpp:285-321 ---- */
+/* nsteps x (device_evolution + swap); nucleation after every step whose
+ * index k satisfies k % nuc_interval == 0 when nuc_interval > 0
+ * (src/main.cpp:307-316), with the nucleation arguments last given to
+ * pfa_set_nucleation_args.  Replayed from a captured CUDA graph. */
+int pfa_run(struct CudaData* dev, int nsteps, double alpha, double dt);
+int pfa_set_nucleation_args(struct CudaData* dev, int nuc_interval, double sigma_del,
+                            double sigma_lav, double unit_a, double dx, double dy, double dz,
+                            double dt_nuc);
+/* pfa_run bracketed by CUDA events on the library's stream; ms = elapsed */
+int pfa_run_timed(struct CudaData* dev, int nsteps, double alpha, double dt, float* ms);
+int pfa_sync(struct CudaData* dev);
+void* pfa_stream(struct CudaData* dev);
+/* number of nucleation events of the last nucleation call, and the events
+ * (cell index, phase) in canonical order; returns the count */
+int pfa_last_nucleation_events(struct CudaData* dev, int64_t* cells, int32_t* phases, int cap);
+
+/* ---- on-device FP64 field summary (src/alloy625.cpp:811-863) ---- */
+/* out[5] = mean x_Cr, mean x_Nb, f_gamma, f_delta, f_laves over the interior */
+int pfa_summarize(struct CudaData* dev, double* out);
+
+/* ---- model helpers ---- */
+/* out[13]: D_Cr[2], D_Nb[2], kappa[2], omega[2], Lmob[2], alpha, dt, rho(D J).
+ * dt_rule 0 = the reference's dt (src/main.cpp:260-268, with meshres);
+ * dt_rule 1 = half the KKS-aware explicit stability limit. */
+int pfa_model_params(double dx, double ifce_width, double xcr0, double xnb0, double meshres,
+                     int dim, int dt_rule, double* out);
+/* the FP32 fast-path coefficients (44 floats), for tests */
+int pfa_model_fast_coef(float* out, int n);
+/* Philox4x32-10 on the device for n counters (4 words each) under one
+ * 64-bit key, for the generator's known-answer test */
+int pfa_philox_block(const uint32_t* ctr, uint64_t key, uint32_t* out, int n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,124 @@
+/*
+ * ref_shim.cpp -- links the oracle's step semantics to the reference's own
+ * compiled energy functions (thermo/parabola625.c, thermo/nucleation.c of
+ * usnistgov/phasefield-precipitate-aging, compiled from where they lie by
+ * oracle/Makefile into oracle/_ref/).
+ *
+ * TEST INFRASTRUCTURE ONLY.  Used in the build container to make the golden
+ * vectors under tests/golden (tests/golden/make_golden.py); it pins the
+ * oracle's restated energy tables against the reference's code.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#include "parabola625.h"
+#include "nucleation.h"
+#include "pfa_oracle.h"
+
+extern "C" {
+
+double ref_p(double x) { return p(x); }
+double ref_pprime(double x) { return pPrime(x); }
+
+double ref_fict(int phase, int comp, double a, double b, double c, double d, double e)
+{
+	switch (phase * 2 + comp) {
+	case 0: return fict_gam_Cr(a, b, c, d, e);
+	case 1: return fict_gam_Nb(a, b, c, d, e);
+	case 2: return fict_del_Cr(a, b, c, d, e);
+	case 3: return fict_del_Nb(a, b, c, d, e);
+	case 4: return fict_lav_Cr(a, b, c, d, e);
+	default: return fict_lav_Nb(a, b, c, d, e);
+	}
+}
+
+double ref_g(int phase, double a, double b)
+{
+	return phase == 0 ? g_gam(a, b) : (phase == 1 ? g_del(a, b) : g_lav(a, b));
+}
+
+double ref_dg(int phase, int comp, double a, double b)
+{
+	switch (phase * 2 + comp) {
+	case 0: return dg_gam_dxCr(a, b);
+	case 1: return dg_gam_dxNb(a, b);
+	case 2: return dg_del_dxCr(a, b);
+	case 3: return dg_del_dxNb(a, b);
+	case 4: return dg_lav_dxCr(a, b);
+	default: return dg_lav_dxNb(a, b);
+	}
+}
+
+double ref_D(int row, int col, double a, double b)
+{
+	switch (row * 2 + col) {
+	case 0: return D_CrCr(a, b);
+	case 1: return D_CrNb(a, b);
+	case 2: return D_NbCr(a, b);
+	default: return D_NbNb(a, b);
+	}
+}
+
+double ref_xe(int phase, int comp)
+{
+	switch (phase * 2 + comp) {
+	case 0: return xe_gam_Cr();
+	case 1: return xe_gam_Nb();
+	case 2: return xe_del_Cr();
+	case 3: return xe_del_Nb();
+	case 4: return xe_lav_Cr();
+	default: return xe_lav_Nb();
+	}
+}
+
+double ref_kT(void) { return kT(); }
+double ref_RT(void) { return RT(); }
+double ref_Vm(void) { return Vm(); }
+
+void ref_nucleation_probability_sphere(double xCr, double xNb, double dG, double dcc, double dnn,
+                                       double sigma, double Vatom, double n_gam, double dV,
+                                       double dt, double* Rstar, double* P)
+{
+	nucleation_probability_sphere(xCr, xNb, dG, dcc, dnn, sigma, Vatom, n_gam, dV, dt, Rstar, P);
+}
+
+/* Philox is the project's own (no counterpart in the reference). */
+void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+double orc_u53(uint32_t hi, uint32_t lo);
+
+} /* extern "C" */
+
+static void nuc_prob_ref(double xCr, double xNb, double dG, double dcc, double dnn, double sigma,
+                         double Vatom, double n_gam, double dV, double dt, double* R, double* P)
+{
+	nucleation_probability_sphere(xCr, xNb, dG, dcc, dnn, sigma, Vatom, n_gam, dV, dt, R, P);
+}
+
+extern "C" {
+#define SFN(name) ref_##name
+#define E_P(x) p(x)
+#define E_PPRIME(x) pPrime(x)
+#define E_FICT_GAM_CR fict_gam_Cr
+#define E_FICT_GAM_NB fict_gam_Nb
+#define E_FICT_DEL_CR fict_del_Cr
+#define E_FICT_DEL_NB fict_del_Nb
+#define E_FICT_LAV_CR fict_lav_Cr
+#define E_FICT_LAV_NB fict_lav_Nb
+#define E_G_GAM g_gam
+#define E_G_DEL g_del
+#define E_G_LAV g_lav
+#define E_DG_GAM_CR dg_gam_dxCr
+#define E_DG_GAM_NB dg_gam_dxNb
+#define E_D_CRCR D_CrCr
+#define E_D_NBNB D_NbNb
+#define E_NUC_PROB nuc_prob_ref
+#define E_XE_GAM_CR xe_gam_Cr()
+#define E_XE_GAM_NB xe_gam_Nb()
+#define E_XE_DEL_CR xe_del_Cr()
+#define E_XE_DEL_NB xe_del_Nb()
+#define E_XE_LAV_CR xe_lav_Cr()
+#define E_XE_LAV_NB xe_lav_Nb()
+#define ORC_RESTRICT __restrict__
+#include "step_impl.h"
+}

@@ -1,0 +1,419 @@
+/*
+ * step_impl.h -- the oracle's step, nucleation and summary semantics.
+ *
+ * TEST INFRASTRUCTURE ONLY (see pfa_oracle.h).
+ *
+ * This file is included twice: by pfa_oracle.c with the oracle's own
+ * restated energies, and by ref_shim.cpp with the reference's compiled
+ * thermo/parabola625.c functions.  The includer defines:
+ *   SFN(name)            -- symbol prefix for the exported functions
+ *   E_P(x), E_PPRIME(x)  -- interpolator p and p'
+ *   E_FICT_GAM_CR(...), E_FICT_GAM_NB, E_FICT_DEL_CR, E_FICT_DEL_NB,
+ *   E_FICT_LAV_CR, E_FICT_LAV_NB  -- (XCR, XNB, pDel, pGam, pLav)
+ *   E_G_GAM, E_G_DEL, E_G_LAV, E_DG_GAM_CR, E_DG_GAM_NB  -- (XCR, XNB)
+ *   E_D_CRCR, E_D_NBNB   -- composition-dependent diffusivities
+ *   E_NUC_PROB(...)      -- nucleation_probability_sphere
+ *   E_XE_GAM_CR ... E_XE_LAV_NB -- equilibrium compositions (no parentheses)
+ * Compiles as C99 and as C++.
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#ifndef ORC_RESTRICT
+#define ORC_RESTRICT
+#endif
+
+/* Zero-flux fill of the one-cell halo ring: halo <- adjacent interior.
+ * Follows boundary_kernel for nm = 3 (src/discretization.cu:360-394).  The
+ * reference fills the four sides concurrently, so its corners are racy; here
+ * the side columns are filled first and the rows second, which leaves each
+ * corner equal to its diagonal interior neighbour. */
+static void SFN(bc2d)(double* f, int nx, int ny)
+{
+	for (int y = 0; y < ny; y++) {
+		f[(size_t)y * nx + 0] = f[(size_t)y * nx + 1];
+		f[(size_t)y * nx + nx - 1] = f[(size_t)y * nx + nx - 2];
+	}
+	for (int x = 0; x < nx; x++) {
+		f[x] = f[(size_t)nx + x];
+		f[(size_t)(ny - 1) * nx + x] = f[(size_t)(ny - 2) * nx + x];
+	}
+}
+
+/* 3D analogue (no reference: the reference is 2D only): x faces, then y
+ * faces, then z faces, each copying the adjacent interior plane. */
+static void SFN(bc3d)(double* f, int nx, int ny, int nz)
+{
+	const size_t sxy = (size_t)nx * ny;
+	for (int z = 0; z < nz; z++)
+		for (int y = 0; y < ny; y++) {
+			double* row = f + z * sxy + (size_t)y * nx;
+			row[0] = row[1];
+			row[nx - 1] = row[nx - 2];
+		}
+	for (int z = 0; z < nz; z++)
+		for (int x = 0; x < nx; x++) {
+			double* pl = f + z * sxy;
+			pl[x] = pl[(size_t)nx + x];
+			pl[(size_t)(ny - 1) * nx + x] = pl[(size_t)(ny - 2) * nx + x];
+		}
+	memcpy(f, f + sxy, sxy * sizeof(double));
+	memcpy(f + (size_t)(nz - 1) * sxy, f + (size_t)(nz - 2) * sxy, sxy * sizeof(double));
+}
+
+/* Fictitious gamma compositions at every cell, src/discretization.cu:50-74. */
+static void SFN(fict_gam_all)(double* const* f, double* ORC_RESTRICT gcr,
+                              double* ORC_RESTRICT gnb, size_t n)
+{
+	const double* cr = f[0];
+	const double* nb = f[1];
+	const double* pd = f[2];
+	const double* pl = f[3];
+	long long i;
+	#pragma omp parallel for schedule(static)
+	for (i = 0; i < (long long)n; i++) {
+		const double xCr = cr[i];
+		const double xNb = nb[i];
+		const double pDel = E_P(pd[i]);
+		const double pLav = E_P(pl[i]);
+		const double pGam = 1.0 - pDel - pLav;
+		gcr[i] = E_FICT_GAM_CR(xCr, xNb, pDel, pGam, pLav);
+		gnb[i] = E_FICT_GAM_NB(xCr, xNb, pDel, pGam, pLav);
+	}
+}
+
+/* Cahn-Hilliard and Allen-Cahn update at one cell, given the four Laplacians.
+ * composition_kernel src/discretization.cu:843-865, delta_kernel :888-914,
+ * laves_kernel :916-942, allen_cahn_kernel :944-980. */
+static void SFN(update_cell)(const orc_params* prm,
+                             double xCr, double xNb, double phD, double phL,
+                             double lapCr, double lapNb, double lapD, double lapL,
+                             double* oCr, double* oNb, double* oD, double* oL)
+{
+	const double dt = prm->dt;
+	*oCr = xCr + dt * (prm->D_Cr[0] * lapCr + prm->D_Cr[1] * lapNb);
+	*oNb = xNb + dt * (prm->D_Nb[0] * lapCr + prm->D_Nb[1] * lapNb);
+
+	const double pDel = E_P(phD);
+	const double pLav = E_P(phL);
+	const double pGam = 1.0 - pDel - pLav;
+	const double gam_Cr = E_FICT_GAM_CR(xCr, xNb, pDel, pGam, pLav);
+	const double gam_Nb = E_FICT_GAM_NB(xCr, xNb, pDel, pGam, pLav);
+	const double gam_nrg = E_G_GAM(gam_Cr, gam_Nb);
+	const double dgGdxCr = E_DG_GAM_CR(gam_Cr, gam_Nb);
+	const double dgGdxNb = E_DG_GAM_NB(gam_Cr, gam_Nb);
+
+	{
+		const double del_Cr = E_FICT_DEL_CR(xCr, xNb, pDel, pGam, pLav);
+		const double del_Nb = E_FICT_DEL_NB(xCr, xNb, pDel, pGam, pLav);
+		const double del_nrg = E_G_DEL(del_Cr, del_Nb);
+		const double gp = gam_nrg - del_nrg - dgGdxCr * (gam_Cr - del_Cr) - dgGdxNb * (gam_Nb - del_Nb);
+		const double dF = -E_PPRIME(phD) * gp
+		                  + 2.0 * prm->omega[0] * phD * (phD - 1.0) * (2.0 * phD - 1.0)
+		                  + 2.0 * prm->alpha * phD * phL * phL
+		                  - prm->kappa[0] * lapD;
+		*oD = phD - dt * prm->Lmob[0] * dF;
+	}
+	{
+		const double lav_Cr = E_FICT_LAV_CR(xCr, xNb, pDel, pGam, pLav);
+		const double lav_Nb = E_FICT_LAV_NB(xCr, xNb, pDel, pGam, pLav);
+		const double lav_nrg = E_G_LAV(lav_Cr, lav_Nb);
+		const double gp = gam_nrg - lav_nrg - dgGdxCr * (gam_Cr - lav_Cr) - dgGdxNb * (gam_Nb - lav_Nb);
+		const double dF = -E_PPRIME(phL) * gp
+		                  + 2.0 * prm->omega[1] * phL * (phL - 1.0) * (2.0 * phL - 1.0)
+		                  + 2.0 * prm->alpha * phL * phD * phD
+		                  - prm->kappa[1] * lapL;
+		*oL = phL - dt * prm->Lmob[1] * dF;
+	}
+}
+
+/* One explicit Euler step, reference sequence src/main.cpp:289-305:
+ * boundaries on the old fields, fictitious gamma compositions, their
+ * boundaries, 5-point mask convolution (src/discretization.cu:550-603 with the
+ * mask of src/mesh.cpp:187-196), Laplacian boundaries, then CH + AC at every
+ * cell.  The Laplacians live in new_f until the update overwrites them, as in
+ * the reference. */
+void SFN(step2d)(double* old_f[4], double* new_f[4], int nx, int ny,
+                 const orc_params* prm, double* work)
+{
+	const size_t n = (size_t)nx * ny;
+	double* gcr = work;
+	double* gnb = work + n;
+	for (int k = 0; k < 4; k++)
+		SFN(bc2d)(old_f[k], nx, ny);
+	SFN(fict_gam_all)(old_f, gcr, gnb, n);
+	SFN(bc2d)(gcr, nx, ny);
+	SFN(bc2d)(gnb, nx, ny);
+
+	const double dx = prm->dx, dy = prm->dy;
+	const double m_n = 1. / (dy * dy);
+	const double m_w = 1. / (dx * dx);
+	const double m_c = -2. * (dx * dx + dy * dy) / (dx * dx * dy * dy);
+	const double m_e = 1. / (dx * dx);
+	const double m_s = 1. / (dy * dy);
+	const double* src[4] = {gcr, gnb, old_f[2], old_f[3]};
+	int y;
+	#pragma omp parallel for schedule(static)
+	for (y = 1; y < ny - 1; y++) {
+		for (int k = 0; k < 4; k++) {
+			const double* s = src[k];
+			double* d = new_f[k];
+			for (int x = 1; x < nx - 1; x++) {
+				const size_t i = (size_t)y * nx + x;
+				double v = 0.;
+				v += m_n * s[i - nx];
+				v += m_w * s[i - 1];
+				v += m_c * s[i];
+				v += m_e * s[i + 1];
+				v += m_s * s[i + nx];
+				d[i] = v;
+			}
+		}
+	}
+	for (int k = 0; k < 4; k++)
+		SFN(bc2d)(new_f[k], nx, ny);
+
+	long long i;
+	#pragma omp parallel for schedule(static)
+	for (i = 0; i < (long long)n; i++) {
+		SFN(update_cell)(prm, old_f[0][i], old_f[1][i], old_f[2][i], old_f[3][i],
+		                 new_f[0][i], new_f[1][i], new_f[2][i], new_f[3][i],
+		                 &new_f[0][i], &new_f[1][i], &new_f[2][i], &new_f[3][i]);
+	}
+}
+
+/* nsteps steps with the caller-side pointer swap of src/main.cpp:318-321;
+ * on return a[] holds the latest fields (pointers are swapped in place). */
+void SFN(run2d)(double* a[4], double* b[4], int nx, int ny, const orc_params* prm,
+                double* work, int nsteps)
+{
+	for (int s = 0; s < nsteps; s++) {
+		SFN(step2d)(a, b, nx, ny, prm, work);
+		for (int k = 0; k < 4; k++) {
+			double* t = a[k];
+			a[k] = b[k];
+			b[k] = t;
+		}
+	}
+}
+
+/* 3D step: the same sequence with a 7-point Laplacian and six-face zero-flux
+ * fill.  The reference has no 3D path (src/main.cpp:418-421); this extends
+ * its 2D equations unchanged. */
+void SFN(step3d)(double* old_f[4], double* new_f[4], int nx, int ny, int nz,
+                 const orc_params* prm, double* work)
+{
+	const size_t sxy = (size_t)nx * ny;
+	const size_t n = sxy * nz;
+	double* gcr = work;
+	double* gnb = work + n;
+	for (int k = 0; k < 4; k++)
+		SFN(bc3d)(old_f[k], nx, ny, nz);
+	SFN(fict_gam_all)(old_f, gcr, gnb, n);
+	SFN(bc3d)(gcr, nx, ny, nz);
+	SFN(bc3d)(gnb, nx, ny, nz);
+
+	const double dx = prm->dx, dy = prm->dy, dz = prm->dz;
+	const double mx = 1. / (dx * dx), my = 1. / (dy * dy), mz = 1. / (dz * dz);
+	const double mc = -2. * (mx + my + mz);
+	const double* src[4] = {gcr, gnb, old_f[2], old_f[3]};
+	int z;
+	#pragma omp parallel for schedule(static)
+	for (z = 1; z < nz - 1; z++) {
+		for (int k = 0; k < 4; k++) {
+			const double* s = src[k];
+			double* d = new_f[k];
+			for (int y = 1; y < ny - 1; y++)
+				for (int x = 1; x < nx - 1; x++) {
+					const size_t i = z * sxy + (size_t)y * nx + x;
+					double v = 0.;
+					v += mz * s[i - sxy];
+					v += my * s[i - nx];
+					v += mx * s[i - 1];
+					v += mc * s[i];
+					v += mx * s[i + 1];
+					v += my * s[i + nx];
+					v += mz * s[i + sxy];
+					d[i] = v;
+				}
+		}
+	}
+	for (int k = 0; k < 4; k++)
+		SFN(bc3d)(new_f[k], nx, ny, nz);
+
+	long long i;
+	#pragma omp parallel for schedule(static)
+	for (i = 0; i < (long long)n; i++) {
+		SFN(update_cell)(prm, old_f[0][i], old_f[1][i], old_f[2][i], old_f[3][i],
+		                 new_f[0][i], new_f[1][i], new_f[2][i], new_f[3][i],
+		                 &new_f[0][i], &new_f[1][i], &new_f[2][i], &new_f[3][i]);
+	}
+}
+
+/* Paint one nucleus: embed_OPC_kernel, src/discretization.cu:1046-1077. */
+static void SFN(embed)(double* cr, double* nb, double* phi, int nx, int ny,
+                       int x, int y, double xCr, double xNb,
+                       double par_Cr, double par_Nb, double R_precip)
+{
+	const double R_dep_Cr = R_precip * sqrt((par_Cr - xCr) / (xCr - E_XE_GAM_CR));
+	const double R_dep_Nb = R_precip * sqrt((par_Nb - xNb) / (xNb - E_XE_GAM_NB));
+	const long long ntot = (long long)nx * ny;
+	for (int i = (int)(-R_precip); i < R_precip; i++) {
+		for (int j = (int)(-R_precip); j < R_precip; j++) {
+			const long long idn = (long long)nx * (y + j) + (x + i);
+			const double r = sqrt((double)(i * i + j * j));
+			if (idn >= 0 && idn < ntot) {
+				if (r <= R_precip) {
+					cr[idn] = par_Cr;
+					nb[idn] = par_Nb;
+					phi[idn] = 1.;
+				} else {
+					if (r <= R_dep_Cr)
+						cr[idn] = E_XE_GAM_CR;
+					if (r <= R_dep_Nb)
+						nb[idn] = E_XE_GAM_NB;
+				}
+			}
+		}
+	}
+}
+
+/* Decide one cell: the per-thread body of nucleation_kernel
+ * (src/discretization.cu:1079-1177) evaluated on an unmodified snapshot.
+ * Returns a bitmask: bit 0 = delta event, bit 1 = laves event; writes the
+ * radii in cells. */
+static int SFN(nuc_decide)(double* const* f, int nx, int ny, int x, int y,
+                           const orc_nuc_params* np, uint64_t seed, uint64_t call,
+                           double* rd, double* rl)
+{
+	const double dV = np->dx * np->dy * np->dz;
+	const double Vatom = 0.25 * np->unit_a * np->unit_a * np->unit_a;
+	const double n_gam = dV / Vatom;
+	const double R = 1.75e-9 / np->dx;
+	const long long ntot = (long long)nx * ny;
+	double phi_pre = 0.;
+	for (int i = (int)(-R); i < R; i++)
+		for (int j = (int)(-R); j < R; j++) {
+			const long long idn = (long long)nx * (y + j) + (x + i);
+			if (idn >= 0 && idn < ntot && i * i + j * j < R * R)
+				phi_pre = fmax(phi_pre, E_P(f[2][idn]) + E_P(f[3][idn]));
+		}
+	if (!(phi_pre < 1e-10))
+		return 0;
+	const long long idx = (long long)nx * y + x;
+	const double xCr = f[0][idx];
+	const double xNb = f[1][idx];
+	uint32_t ctr[4] = {(uint32_t)idx, (uint32_t)((uint64_t)idx >> 32),
+	                   (uint32_t)call, (uint32_t)(call >> 32)};
+	uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+	uint32_t w[4];
+	orc_philox4x32_10(ctr, key, w);
+	const double u[2] = {orc_u53(w[0], w[1]), orc_u53(w[2], w[3])};
+	const double dG = E_G_GAM(xCr, xNb);
+	const double dCrCr = E_D_CRCR(xCr, xNb);
+	const double dNbNb = E_D_NBNB(xCr, xNb);
+	int mask = 0;
+	for (int ph = 0; ph < 2; ph++) {
+		double Rstar = 0., P = 0.;
+		E_NUC_PROB(xCr, xNb, dG, dCrCr, dNbNb, np->sigma[ph], Vatom, n_gam, dV, np->dt, &Rstar, &P);
+		if (Rstar > 0.) {
+			const double rp = Rstar / np->dx;
+			if (P - u[ph] > 0) {
+				mask |= 1 << ph;
+				if (ph == 0)
+					*rd = rp;
+				else
+					*rl = rp;
+			}
+		}
+	}
+	return mask;
+}
+
+/* Two-phase nucleation: every interior cell decides on the same snapshot,
+ * then events are painted in ascending cell order, delta before laves. */
+int SFN(nucleation2d)(double* f[4], int nx, int ny, const orc_nuc_params* np,
+                      uint64_t seed, uint64_t call, orc_nuc_event* events, int max_events)
+{
+	const size_t n = (size_t)nx * ny;
+	unsigned char* mask = (unsigned char*)calloc(n, 1);
+	double* rad = (double*)calloc(2 * n, sizeof(double));
+	int y;
+	#pragma omp parallel for schedule(dynamic, 4)
+	for (y = 1; y < ny - 1; y++)
+		for (int x = 1; x < nx - 1; x++) {
+			const size_t i = (size_t)y * nx + x;
+			mask[i] = (unsigned char)SFN(nuc_decide)(f, nx, ny, x, y, np, seed, call,
+			                                           &rad[2 * i], &rad[2 * i + 1]);
+		}
+	int count = 0;
+	for (size_t i = 0; i < n; i++) {
+		if (!mask[i])
+			continue;
+		const int x = (int)(i % nx), yy = (int)(i / nx);
+		const double xCr = f[0][i], xNb = f[1][i];
+		for (int ph = 0; ph < 2; ph++) {
+			if (!(mask[i] & (1 << ph)))
+				continue;
+			const double rp = rad[2 * i + ph];
+			if (count < max_events && events) {
+				events[count].cell = (int64_t)i;
+				events[count].phase = ph;
+				events[count].pad = 0;
+				events[count].xcr = xCr;
+				events[count].xnb = xNb;
+				events[count].r_precip = rp;
+			}
+			count++;
+			if (ph == 0)
+				SFN(embed)(f[0], f[1], f[2], nx, ny, x, yy, xCr, xNb, E_XE_DEL_CR, E_XE_DEL_NB, rp);
+			else
+				SFN(embed)(f[0], f[1], f[3], nx, ny, x, yy, xCr, xNb, E_XE_LAV_CR, E_XE_LAV_NB, rp);
+		}
+	}
+	free(mask);
+	free(rad);
+	return count;
+}
+
+/* Field summary over the interior nodes: mean x_Cr, x_Nb and phase fractions
+ * (gamma, delta, laves), src/alloy625.cpp:811-863.  Compensated sums. */
+static void SFN(summarize_range)(const double* const* f, size_t nx, size_t ny, size_t nz,
+                                 int is3d, double out[5])
+{
+	double s[5] = {0, 0, 0, 0, 0}, c[5] = {0, 0, 0, 0, 0};
+	const size_t z0 = is3d ? 1 : 0, z1 = is3d ? nz - 1 : 1;
+	for (size_t z = z0; z < z1; z++)
+		for (size_t y = 1; y < ny - 1; y++)
+			for (size_t x = 1; x < nx - 1; x++) {
+				const size_t i = (z * ny + y) * nx + x;
+				double v[5];
+				v[0] = f[0][i];
+				v[1] = f[1][i];
+				v[3] = E_P(f[2][i]);
+				v[4] = E_P(f[3][i]);
+				v[2] = 1.0;
+				v[2] -= v[3];
+				v[2] -= v[4];
+				for (int k = 0; k < 5; k++) {
+					const double yk = v[k] - c[k];
+					const double t = s[k] + yk;
+					c[k] = (t - s[k]) - yk;
+					s[k] = t;
+				}
+			}
+	const double ntot = (double)(nx - 2) * (double)(ny - 2) * (is3d ? (double)(nz - 2) : 1.0);
+	for (int k = 0; k < 5; k++)
+		out[k] = s[k] / ntot;
+}
+
+void SFN(summarize2d)(const double* f[4], int nx, int ny, double out[5])
+{
+	SFN(summarize_range)(f, nx, ny, 1, 0, out);
+}
+
+void SFN(summarize3d)(const double* f[4], int nx, int ny, int nz, double out[5])
+{
+	SFN(summarize_range)(f, nx, ny, nz, 1, out);
+}

@@ -1,0 +1,47 @@
+// pfa_internal.h -- shared declarations of libpfa_gb300 (not installed).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace pfa {
+
+// Per-grid model constants (double on the host; the FP32 kernels round them).
+struct ModelConst {
+  double D[2][2];    // D[0] = [D_CrCr, D_CrNb], D[1] = [D_NbCr, D_NbNb]
+  double kappa[2];   // gradient coefficients (delta, laves)
+  double omega[2];   // well heights
+  double L[2];       // Allen-Cahn mobilities
+  double alpha;      // three-phase penalty
+  double dt;         // time step
+  double mask[5];    // 5-point mask: north, west, centre, east, south (2D)
+  double idx2[3];    // 1/dx^2, 1/dy^2, 1/dz^2
+};
+
+// Coefficients of the FP32 fast path, derived on the host in double.
+//  * gamma solve in the reference's three-variable form (all denominator
+//    terms are non-negative on the simplex, so it does not cancel):
+//      den   = d . [pD^2, pD pG, pD pL, pG^2, pG pL, pL^2]
+//      num_k = XCR (l_k . [pD pG pL]) + XNB (m_k . [pD pG pL]) + q_k . monomials
+//    with the scale folded into l, m, q;  x^gamma_k = num_k / den.
+//  * grand-potential difference of phase i as a quadratic in
+//      u = x^gamma - xe_gamma:  c0 + u1 (c1 + c11 u1 + c12 u2) + u2 (c2 + c22 u2)
+struct FastCoef {
+  float den[6];        // d
+  float num[2][12];    // per comp: l0 l1 l2 m0 m1 m2 q0..q5
+  float dP[2][6];      // per phase (delta, laves): c0 c1 c2 c11 c12 c22
+  float xe_gam[2];
+};
+
+void model_fast_coef(FastCoef* out);
+
+// Host model helpers (pfa_model.cpp)
+double model_D(int row, int col, double xcr, double xnb);
+double model_kks_diffusivity(const double Dcr[2], const double Dnb[2]);
+
+// Sticky error word of the library (last failure); see pfa_gb300.h.
+void set_error(int code, const char* where);
+
+}  // namespace pfa

@@ -1,0 +1,67 @@
+// pfa_kernels.h -- kernel argument blocks and launchers of libpfa_gb300.
+#pragma once
+
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "pfa_internal.h"
+
+namespace pfa {
+
+// Arguments of one fused 2D step (passed by value to the kernel).
+struct Step2DArgs {
+  const void* in[4];    // x_Cr, x_Nb, phi_del, phi_lav (double or float)
+  void* out[4];
+  const float* cin[4];  // FP32 form: Kahan compensation in (x_Cr, x_Nb[, phi_del, phi_lav])
+  float* cout[4];
+  int Nx, Ny, pitch;    // interior size and row pitch (elements)
+  int write_halo;       // also write the mirrored ghost ring
+  int nine;             // 3x3 mask has non-zero corners
+  int kahan_phi;        // FP32 form: compensate the phase fields too
+  ModelConst m;
+  double mask9[9];      // full 3x3 mask, row-major (rows y-1..y+1)
+  FastCoef k;
+  float dtD[2][2];      // dt * D
+  float dtL[2];         // dt * L
+  float om2[2];         // 2 omega
+  float alpha2;         // 2 alpha
+  float kap[2];         // kappa
+};
+
+// Layout conversion between FP64 reference fields and FP32 form fields.
+struct ConvArgs {
+  double* f64[4];
+  float* f32[4];
+  float* c32[4];
+  int Nx, Ny, pitch64, pitch32;
+};
+
+// Arguments of the reference's per-stage kernels (compat mode).
+struct StageArgs {
+  double* f[4];         // fields the stage reads (old) or fills
+  double* o[4];         // fields the stage writes (new / Laplacians)
+  double* gam[2];       // fictitious gamma compositions
+  double* del[2];       // fictitious delta compositions
+  double* lav[2];       // fictitious laves compositions
+  int nx, ny;           // full array extent including the ghost ring
+  ModelConst m;
+  double mask9[9];
+};
+
+cudaError_t launch_step2d_f64(const Step2DArgs& a, cudaStream_t s);
+cudaError_t launch_step2d_f32(const Step2DArgs& a, cudaStream_t s);
+cudaError_t launch_import_f32(const ConvArgs& a, cudaStream_t s);
+cudaError_t launch_export_f32(const ConvArgs& a, cudaStream_t s);
+
+// compat-mode stages (pfa_stages.cu)
+cudaError_t launch_bc(double* f, int nx, int ny, cudaStream_t s);
+cudaError_t launch_fictitious(const StageArgs& a, cudaStream_t s);
+cudaError_t launch_convolution(const double* in, double* out, int nx, int ny,
+                               const double* mask9, cudaStream_t s);
+cudaError_t launch_evolution(const StageArgs& a, cudaStream_t s);
+cudaError_t launch_dataviz(const double* cr, const double* nb, const double* pd,
+                           const double* pl, double* ni, double* phi, int nx, int ny,
+                           cudaStream_t s);
+
+}  // namespace pfa

@@ -1,0 +1,334 @@
+// pfa_nucleation.cu -- stochastic nucleation of libpfa_gb300 (sm_103a).
+//
+// The reference's nucleation_kernel (src/discretization.cu:1079-1177) lets
+// every thread scan its neighbourhood, draw from a clock-seeded curand XORWOW
+// state and paint nuclei into its neighbours' cells while other threads
+// read them.  Here the same per-cell physics runs in two deterministic
+// phases:
+//   1. k_nuc_decide: every interior cell decides on the unmodified fields
+//      (neighbourhood scan, driving force g_gam, diffusivities, classical
+//      nucleation probability thermo/nucleation.c:30-69) with Philox4x32-10
+//      draws keyed by (seed, call counter, cell).  Events are compacted with a
+//      warp ballot and one atomic per warp.
+//   2. k_nuc_apply: one CTA sorts the events by cell and paints them in that
+//      order, delta before laves (embed_OPC_kernel, :1046-1077).
+// The FP64 probability is evaluated only where an FP32 bound cannot exclude
+// an event: if dt dV (J_Cr + J_Nb) < 1e-17 the FP64 P_nuc is 0 or 2^-53 and
+// no draw u >= 2^-53 can fall below it, so skipping such cells changes no
+// decision.
+#include <cstdint>
+
+#include "pfa_device.cuh"
+#include "pfa_nucleation.h"
+
+namespace pfa {
+
+using namespace dev;
+
+// ---- Philox4x32-10 (Salmon, Moraes, Dror, Shaw: "Parallel random numbers:
+// as easy as 1, 2, 3", SC'11): 10 rounds of two 32x32->64 multiplies with
+// Weyl-sequence key bumps. ----
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
+  constexpr uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
+  constexpr uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+  for (int r = 0; r < 10; r++) {
+    if (r > 0) {
+      k.x += W0;
+      k.y += W1;
+    }
+    const uint32_t hi0 = __umulhi(M0, c.x), lo0 = M0 * c.x;
+    const uint32_t hi1 = __umulhi(M1, c.z), lo1 = M1 * c.z;
+    c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+  }
+  return c;
+}
+
+// 53 random bits -> uniform double in (0, 1]
+__device__ __forceinline__ double u53(uint32_t hi, uint32_t lo) {
+  const unsigned long long k = ((((unsigned long long)hi) << 32) | lo) >> 11;
+  return double(k + 1ull) * (1.0 / 9007199254740992.0);
+}
+
+namespace {
+
+template <class T>
+__device__ __forceinline__ double ld(const void* p, size_t i) {
+  return double(static_cast<const T*>(p)[i]);
+}
+
+// Storage index of the reference linear index idn (row width nx = Nx + 2).
+__device__ __forceinline__ size_t sidx(long long idn, int nxr, int pitch) {
+  return size_t(idn / nxr) * pitch + size_t(idn % nxr);
+}
+
+// composition-dependent diffusivities D_CrCr, D_NbNb (thermo/parabola625.c:1860-1894)
+__device__ void diffusivities(double X, double Y, double& dcc, double& dnn) {
+  const double xni = -X - Y + 1;
+  const double mNb = kMobPreNb * exp(-34.982563536715503 * Y * xni + 14.437947842988088 * Y);
+  const double mCr = kMobPreCr * exp(-7.1543718172640256 * X * xni + 3.3541967644499233 * X);
+  const double mNi = kMobPreNi * exp(-8.5221193705645018 * X * xni + 4.0036674816806448 * X -
+                                     442.62877981749585 * Y * xni - 0.82164267100913768 * Y);
+  const double s0 = -kHCrCr * X - kHCrNb * Y;  // column Cr
+  const double s1 = -kHCrNb * X - kHNbNb * Y;  // column Nb
+  dcc = -mNb * X * Y * (s0 + kHCrNbAddA) + mCr * X * (1 - X) * (s0 + kHCrCrAdd) - mNi * X * s0 * xni;
+  dnn = -mCr * X * Y * (s1 + kHCrNbAddB) + mNb * Y * (1 - Y) * (s1 + kHNbNbAdd) - mNi * Y * s1 * xni;
+}
+
+// nucleation_probability_sphere, thermo/nucleation.c:30-69 (src/nucleation.cu:30-70)
+__device__ void probability_sphere(double xCr, double xNb, double dG, double dcc, double dnn,
+                                   double sigma, double Vatom, double n_gam, double dV, double dt,
+                                   double& Rstar, double& P) {
+  const double sigma_cubed = sigma * sigma * sigma;
+  const double Zeldov = (Vatom * dG * dG) / (8. * kPi * sqrt(kKT * sigma_cubed));
+  const double Gstar = (16. * kPi * sigma_cubed) / (3. * dG * dG);
+  constexpr double a2 = kLatticeConst * kLatticeConst;
+  const double a4 = a2 * a2;
+  const double BstarCr = (3. * Gstar * dcc * xCr) / (sigma * a4);
+  const double BstarNb = (3. * Gstar * dnn * xNb) / (sigma * a4);
+  const double k1Cr = BstarCr * Zeldov * n_gam;
+  const double k1Nb = BstarNb * Zeldov * n_gam;
+  const double k2 = Gstar / kKT;
+  const double dc_Cr = -xCr + kXe[0][0];
+  const double dc_Nb = xNb - kXe[0][1];
+  const double JCr = k1Cr * exp(-k2 / dc_Cr);
+  const double JNb = k1Nb * exp(-k2 / dc_Nb);
+  const double P0 = exp(-dt * dV * (JCr + JNb));
+  P = 1. - P0;
+  Rstar = (2. * sigma) / dG;
+}
+
+// True when no event is possible for either phase (see file comment).
+__device__ bool surely_no_event(float X, float Y, const NucArgs& a) {
+  const float dcCr = float(kXe[0][0]) - X, dcNb = Y - float(kXe[0][1]);
+  if (!(dcCr > 0.0f && dcNb > 0.0f && X > 0.0f && Y > 0.0f && X + Y < 1.0f)) return false;
+  // g_gam in FP32
+  const float u = X - float(kXe[0][0]), v = Y - float(kXe[0][1]);
+  const float dG = float(kG[0][0]) * u * u + (float(kG[0][1]) * X - float(kG[0][2])) * v +
+                   float(kG[0][3]) * v * v;
+  if (!(dG > 0.0f)) return false;
+  // |D| bound: the three mobility terms of D are each bounded by
+  // pre * exp(e) * (|s| + add) (times compositions <= 1)
+  const float xni = 1.0f - X - Y;
+  const float eNb = -34.982563536715503f * Y * xni + 14.437947842988088f * Y;
+  const float eCr = -7.1543718172640256f * X * xni + 3.3541967644499233f * X;
+  const float eNi = -8.5221193705645018f * X * xni + 4.0036674816806448f * X -
+                    442.62877981749585f * Y * xni - 0.82164267100913768f * Y;
+  const float emax = fmaxf(eNb, fmaxf(eCr, eNi));
+  const float lnDmax = logf(3.0f * 1.5e-20f * 2.5e6f) + emax;  // 3 terms, pre <= 1.5e-20, |s|+add <= 2.5e6
+  float lnz = -INFINITY;
+#pragma unroll
+  for (int ph = 0; ph < 2; ph++) {
+    const float sigma = float(a.sigma[ph]);
+    const float s3 = sigma * sigma * sigma;
+    // ln(k1) <= ln(3 G* Dmax x / (sigma a^4) * Zeldov * n_gam), x <= 1
+    const float Gstar = (16.0f * float(kPi) * s3) / (3.0f * dG * dG);
+    const float Z = float(a.Vatom) * dG * dG / (8.0f * float(kPi) * sqrtf(float(kKT) * s3));
+    const float a4 = float(kLatticeConst * kLatticeConst * kLatticeConst * kLatticeConst);
+    const float lnk1 = logf(3.0f * Gstar / (sigma * a4)) + lnDmax + logf(Z) + float(a.ln_ngam);
+    const float k2 = Gstar / float(kKT);
+    // max(J_Cr, J_Nb) <= k1_max exp(-min(k2 / dc_Cr, k2 / dc_Nb))
+    const float lnJ = lnk1 - fminf(k2 / dcCr, k2 / dcNb);
+    lnz = fmaxf(lnz, lnJ + 0.6931472f);  // J_Cr + J_Nb <= 2 max
+  }
+  lnz += float(a.ln_dtdV);
+  return isfinite(lnz) ? (lnz < -39.1439f - 12.0f) : false;  // ln(1e-17) - 12
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_nuc_decide(NucArgs a) {
+  const int gx = blockIdx.x * 32 + (threadIdx.x & 31);
+  const int gy = blockIdx.y * 8 + (threadIdx.x >> 5);
+  const int nxr = a.Nx + 2, nyr = a.Ny + 2;
+  bool ev = false;
+  NucEvent e;
+  if (gx < a.Nx && gy < a.Ny) {
+    const int x = gx + 1, y = gy + 1;
+    const long long idx = (long long)nxr * y + x;
+    const long long ntot = (long long)nxr * nyr;
+    const double R = a.R_scan;
+    double phi_pre = 0.0;
+    for (int i = int(-R); i < R; i++)
+      for (int j = int(-R); j < R; j++) {
+        const long long idn = (long long)nxr * (y + j) + (x + i);
+        if (idn >= 0 && idn < ntot && double(i * i + j * j) < R * R) {
+          const size_t s = sidx(idn, nxr, a.pitch);
+          phi_pre = fmax(phi_pre, p64(ld<T>(a.f[2], s)) + p64(ld<T>(a.f[3], s)));
+        }
+      }
+    if (phi_pre < 1e-10) {
+      const size_t s = sidx(idx, nxr, a.pitch);
+      const double X = ld<T>(a.f[0], s), Y = ld<T>(a.f[1], s);
+      if (!surely_no_event(float(X), float(Y), a)) {
+        const unsigned long long call = *a.call_ptr;
+        const uint4 w = philox4x32_10(
+            make_uint4(uint32_t(idx), uint32_t(uint64_t(idx) >> 32), uint32_t(call),
+                       uint32_t(call >> 32)),
+            make_uint2(uint32_t(a.seed), uint32_t(a.seed >> 32)));
+        const double u[2] = {u53(w.x, w.y), u53(w.z, w.w)};
+        const double dG = g64<0>(X, Y);
+        double dcc, dnn;
+        diffusivities(X, Y, dcc, dnn);
+        int mask = 0;
+        double rp[2] = {0.0, 0.0};
+#pragma unroll
+        for (int ph = 0; ph < 2; ph++) {
+          double Rstar = 0.0, P = 0.0;
+          probability_sphere(X, Y, dG, dcc, dnn, a.sigma[ph], a.Vatom, a.n_gam, a.dV, a.dt, Rstar, P);
+          if (Rstar > 0.) {
+            rp[ph] = Rstar / a.dx;
+            if (P - u[ph] > 0) mask |= 1 << ph;
+          }
+        }
+        if (mask) {
+          ev = true;
+          e.cell = idx;
+          e.mask = mask;
+          e.pad = 0;
+          e.xcr = X;
+          e.xnb = Y;
+          e.r[0] = rp[0];
+          e.r[1] = rp[1];
+        }
+      }
+    }
+  }
+  // warp-aggregated append
+  const unsigned bal = __ballot_sync(0xffffffffu, ev);
+  if (bal == 0) return;
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(bal) - 1;
+  unsigned base = 0;
+  if (lane == leader) base = atomicAdd(a.count, unsigned(__popc(bal)));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (ev) {
+    const unsigned slot = base + __popc(bal & ((1u << lane) - 1u));
+    if (slot < unsigned(a.cap)) a.events[slot] = e;
+  }
+}
+
+template <class T>
+__device__ __forceinline__ void put(void* f, float* c, size_t s, double v) {
+  static_cast<T*>(f)[s] = T(v);
+  if (c) c[s] = float(double(T(v)) - v);
+}
+
+// embed_OPC_kernel, src/discretization.cu:1046-1077, painted cooperatively
+template <class T>
+__device__ void paint(const NucArgs& a, const NucEvent& e, int ph) {
+  const int nxr = a.Nx + 2;
+  const long long ntot = (long long)nxr * (a.Ny + 2);
+  const int x = int(e.cell % nxr), y = int(e.cell / nxr);
+  const double R = e.r[ph];
+  constexpr double xgCr = kXe[0][0], xgNb = kXe[0][1];
+  constexpr double xdCr = kXe[1][0], xdNb = kXe[1][1], xlCr = kXe[2][0], xlNb = kXe[2][1];
+  const double parCr = ph == 0 ? xdCr : xlCr, parNb = ph == 0 ? xdNb : xlNb;
+  const double RdCr = R * sqrt((parCr - e.xcr) / (e.xcr - xgCr));
+  const double RdNb = R * sqrt((parNb - e.xnb) / (e.xnb - xgNb));
+  const int lo = int(-R);
+  int hi = lo;
+  while (double(hi) < R) hi++;  // loop bound of `for (i = -R; i < R; i++)`
+  const int w = hi - lo;
+  if (w <= 0) return;
+  const long long n = (long long)w * w;
+  void* phi = a.f[2 + ph];
+  float* cphi = a.comp[2 + ph];
+  float* ccr = a.comp[0];
+  float* cnb = a.comp[1];
+  for (long long t = threadIdx.x; t < n; t += blockDim.x) {
+    const int i = lo + int(t / w), j = lo + int(t % w);
+    const long long idn = (long long)nxr * (y + j) + (x + i);
+    if (idn < 0 || idn >= ntot) continue;
+    const size_t s = sidx(idn, nxr, a.pitch);
+    const double r = sqrt(double(i * i + j * j));
+    if (r <= R) {
+      put<T>(a.f[0], ccr, s, parCr);
+      put<T>(a.f[1], cnb, s, parNb);
+      put<T>(phi, cphi, s, 1.0);
+    } else {
+      if (r <= RdCr) put<T>(a.f[0], ccr, s, xgCr);
+      if (r <= RdNb) put<T>(a.f[1], cnb, s, xgNb);
+    }
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(1024) k_nuc_apply(NucArgs a) {
+  extern __shared__ unsigned long long s_key[];
+  const unsigned n = *a.count;
+  __syncthreads();
+  // the decision kernel of this call has read the counter: advance it
+  if (threadIdx.x == 0) *a.call_ptr += 1ull;
+  if (n == 0) return;
+  if (n > unsigned(a.cap)) {
+    if (threadIdx.x == 0) *a.status = 1;  // overflow: nothing painted
+    return;
+  }
+  unsigned m = 1;
+  while (m < n) m <<= 1;
+  for (unsigned t = threadIdx.x; t < m; t += blockDim.x)
+    s_key[t] = t < n ? ((unsigned long long)a.events[t].cell << kNucIdxBits) | t : ~0ull;
+  __syncthreads();
+  // bitonic sort, ascending
+  for (unsigned k = 2; k <= m; k <<= 1)
+    for (unsigned j = k >> 1; j > 0; j >>= 1) {
+      for (unsigned t = threadIdx.x; t < m; t += blockDim.x) {
+        const unsigned p = t ^ j;
+        if (p > t) {
+          const unsigned long long u = s_key[t], v = s_key[p];
+          const bool up = (t & k) == 0;
+          if ((u > v) == up) {
+            s_key[t] = v;
+            s_key[p] = u;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  for (unsigned q = 0; q < n; q++) {
+    const NucEvent e = a.events[s_key[q] & ((1ull << kNucIdxBits) - 1)];
+    for (int ph = 0; ph < 2; ph++) {
+      if (e.mask & (1 << ph)) paint<T>(a, e, ph);
+      __syncthreads();
+    }
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_nucleation(const NucArgs& a, cudaStream_t s) {
+  cudaError_t err = cudaMemsetAsync(a.count, 0, sizeof(unsigned), s);
+  if (err != cudaSuccess) return err;
+  dim3 grid((a.Nx + 31) / 32, (a.Ny + 7) / 8);
+  const size_t smem = sizeof(unsigned long long) * size_t(kNucCap);
+  if (a.is_f32) {
+    k_nuc_decide<float><<<grid, 256, 0, s>>>(a);
+    k_nuc_apply<float><<<1, 1024, smem, s>>>(a);
+  } else {
+    k_nuc_decide<double><<<grid, 256, 0, s>>>(a);
+    k_nuc_apply<double><<<1, 1024, smem, s>>>(a);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t nucleation_setup() {
+  const int smem = int(sizeof(unsigned long long) * kNucCap);
+  cudaError_t e = cudaFuncSetAttribute(k_nuc_apply<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_nuc_apply<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+}
+
+// Philox exposed for the generator test (one block of counters).
+__global__ void k_philox_block(const uint4* ctr, uint2 key, uint4* out, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = philox4x32_10(ctr[i], key);
+}
+
+cudaError_t launch_philox_block(const void* ctr, uint64_t key, void* out, int n, cudaStream_t s) {
+  k_philox_block<<<(n + 255) / 256, 256, 0, s>>>(static_cast<const uint4*>(ctr),
+                                                  make_uint2(uint32_t(key), uint32_t(key >> 32)),
+                                                  static_cast<uint4*>(out), n);
+  return cudaGetLastError();
+}
+
+}  // namespace pfa

@@ -1,0 +1,42 @@
+// pfa_nucleation.h -- nucleation kernels of libpfa_gb300.
+#pragma once
+
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace pfa {
+
+constexpr int kNucCap = 1 << 14;  // events per nucleation call (scratch capacity)
+constexpr int kNucIdxBits = 14;   // low key bits carrying the event index
+
+struct NucEvent {
+  long long cell;  // reference linear index nx * y + x (halo layout)
+  int mask;        // bit 0 delta, bit 1 laves
+  int pad;
+  double xcr, xnb; // composition before painting
+  double r[2];     // nucleus radius in cells (delta, laves)
+};
+
+struct NucArgs {
+  void* f[4];          // x_Cr, x_Nb, phi_del, phi_lav (halo layout, row pitch `pitch`)
+  float* comp[4];      // FP32 form: compensation arrays (reset where painted), or nullptr
+  int is_f32;
+  int Nx, Ny, pitch;
+  double sigma[2];
+  double dx;           // kernel spacing (the reference passes dx * nx here)
+  double dV, Vatom, n_gam, dt, R_scan;
+  double ln_dtdV, ln_ngam;
+  uint64_t seed;
+  unsigned long long* call_ptr;  // scratch: nucleation call counter (Philox counter word)
+  NucEvent* events;    // scratch: kNucCap events
+  unsigned* count;     // scratch: event counter
+  int* status;         // scratch: 1 = overflow
+  int cap;
+};
+
+cudaError_t launch_nucleation(const NucArgs& a, cudaStream_t s);
+cudaError_t nucleation_setup();
+cudaError_t launch_philox_block(const void* ctr, uint64_t key, void* out, int n, cudaStream_t s);
+
+}  // namespace pfa

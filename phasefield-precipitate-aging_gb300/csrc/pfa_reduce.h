@@ -1,0 +1,21 @@
+// pfa_reduce.h -- field summary kernels of libpfa_gb300.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace pfa {
+
+constexpr int kSumBlocks = 256;  // fixed partial-sum count (deterministic order)
+
+struct SumArgs {
+  const void* f[4];   // fields in the halo layout
+  const float* c[2];  // FP32 form: compensation of x_Cr, x_Nb (value = f - c), or nullptr
+  int is_f32, is3d;
+  int Nx, Ny, Nz, pitch;
+  double* partial;    // scratch: kSumBlocks * 5 doubles
+  double* out;        // 5 doubles (device)
+};
+
+cudaError_t launch_summarize(const SumArgs& a, cudaStream_t s);
+
+}  // namespace pfa

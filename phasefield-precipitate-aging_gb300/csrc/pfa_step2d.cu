@@ -1,0 +1,341 @@
+// pfa_step2d.cu -- 2D step kernels of libpfa_gb300 (sm_103a).
+//
+// One fused kernel per explicit Euler step replaces the reference's 29
+// launches (src/main.cpp:289-305): zero-flux boundary fill, fictitious
+// gamma compositions (src/discretization.cu:50-74), 5- or 9-point mask
+// convolution (:550-603), Cahn-Hilliard (:843-886) and Allen-Cahn (:888-980).
+// Each CTA stages one tile plus its one-cell halo in shared memory, computes
+// p(phi) and x^gamma once per staged cell, then the Laplacians and both
+// updates for its interior cells.  Domain edges are handled by clamped
+// (mirrored) indexing, which is what the reference's halo fill produces.
+//
+// Layouts.  FP64 fields use the reference's layout: (Ny + 2) rows of pitch
+// elements, a one-cell ghost ring, interior cell (x, y) at (y + 1) * pitch +
+// x + 1.  The FP32 precision form keeps its own buffers in the same
+// convention with the pitch padded to 32 elements (128-byte rows).
+#include <cstdint>
+
+#include "pfa_device.cuh"
+#include "pfa_kernels.h"
+
+namespace pfa {
+
+using namespace dev;
+
+namespace {
+
+constexpr int kTX = 32;   // tile width (one warp)
+constexpr int kTY = 16;   // tile height
+constexpr int kBY = 8;    // thread rows per CTA
+constexpr int kEX = kTX + 2;
+constexpr int kEY = kTY + 2;
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// Write a value to interior cell (gx, gy) and, for cells on the domain edge,
+// to the ghost cells that mirror it (corners take the diagonal value).
+template <class T>
+__device__ __forceinline__ void store_with_halo(T* f, int pitch, int gx, int gy, int Nx, int Ny,
+                                                T v, bool halo) {
+  const size_t row = size_t(gy + 1) * pitch;
+  f[row + gx + 1] = v;
+  if (!halo) return;
+  const bool l = gx == 0, r = gx == Nx - 1, b = gy == 0, t = gy == Ny - 1;
+  if (l) f[row] = v;
+  if (r) f[row + Nx + 1] = v;
+  if (b) {
+    f[gx + 1] = v;
+    if (l) f[0] = v;
+    if (r) f[Nx + 1] = v;
+  }
+  if (t) {
+    const size_t top = size_t(Ny + 1) * pitch;
+    f[top + gx + 1] = v;
+    if (l) f[top] = v;
+    if (r) f[top + Nx + 1] = v;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Plain FP64 fused step (faithful to the reference's formulas).
+// NINE: the mask has non-zero corners (9-point stencil, src/mesh.cpp:198-213).
+template <bool NINE>
+__global__ void __launch_bounds__(kTX* kBY) k_step2d_f64(Step2DArgs a) {
+  __shared__ double s_phd[kEY][kEX], s_phl[kEY][kEX], s_gcr[kEY][kEX], s_gnb[kEY][kEX];
+  __shared__ double s_pd[kEY][kEX], s_pl[kEY][kEX], s_rden[kEY][kEX];
+  const double* __restrict__ icr = static_cast<const double*>(a.in[0]);
+  const double* __restrict__ inb = static_cast<const double*>(a.in[1]);
+  const double* __restrict__ ipd = static_cast<const double*>(a.in[2]);
+  const double* __restrict__ ipl = static_cast<const double*>(a.in[3]);
+  const int x0 = blockIdx.x * kTX, y0 = blockIdx.y * kTY;
+  const int tid = threadIdx.y * kTX + threadIdx.x;
+
+  for (int e = tid; e < kEX * kEY; e += kTX * kBY) {
+    const int ex = e % kEX, ey = e / kEX;
+    const int gx = clampi(x0 + ex - 1, 0, a.Nx - 1);
+    const int gy = clampi(y0 + ey - 1, 0, a.Ny - 1);
+    const size_t i = size_t(gy + 1) * a.pitch + gx + 1;
+    const double X = icr[i], Y = inb[i], phd = ipd[i], phl = ipl[i];
+    const double pD = p64(phd), pL = p64(phl), pG = 1.0 - pD - pL;
+    Poly64 m;
+    poly64(pD, pG, pL, m);
+    s_phd[ey][ex] = phd;
+    s_phl[ey][ex] = phl;
+    s_gcr[ey][ex] = fict64<0, 0>(X, Y, m);
+    s_gnb[ey][ex] = fict64<0, 1>(X, Y, m);
+    s_pd[ey][ex] = pD;
+    s_pl[ey][ex] = pL;
+    s_rden[ey][ex] = m.rden;
+  }
+  __syncthreads();
+
+  const ModelConst& M = a.m;
+  for (int r = threadIdx.y; r < kTY; r += kBY) {
+    const int gx = x0 + threadIdx.x, gy = y0 + r;
+    if (gx >= a.Nx || gy >= a.Ny) continue;
+    const int ex = threadIdx.x + 1, ey = r + 1;
+    // Mask convolution in the reference's order (rows j = y-1..y+1, columns
+    // i = x-1..x+1, value += mask * tile, contracted to FMA); zero mask
+    // entries are exact no-ops there and are skipped for the 5-point mask.
+    auto lap = [&](double (*s)[kEX]) {
+      double v;
+      if (NINE) {
+        v = a.mask9[0] * s[ey - 1][ex - 1];
+        v = fma(a.mask9[1], s[ey - 1][ex], v);
+        v = fma(a.mask9[2], s[ey - 1][ex + 1], v);
+        v = fma(a.mask9[3], s[ey][ex - 1], v);
+        v = fma(a.mask9[4], s[ey][ex], v);
+        v = fma(a.mask9[5], s[ey][ex + 1], v);
+        v = fma(a.mask9[6], s[ey + 1][ex - 1], v);
+        v = fma(a.mask9[7], s[ey + 1][ex], v);
+        v = fma(a.mask9[8], s[ey + 1][ex + 1], v);
+      } else {
+        v = M.mask[0] * s[ey - 1][ex];
+        v = fma(M.mask[1], s[ey][ex - 1], v);
+        v = fma(M.mask[2], s[ey][ex], v);
+        v = fma(M.mask[3], s[ey][ex + 1], v);
+        v = fma(M.mask[4], s[ey + 1][ex], v);
+      }
+      return v;
+    };
+    const double lapCr = lap(s_gcr), lapNb = lap(s_gnb), lapD = lap(s_phd), lapL = lap(s_phl);
+    const size_t i = size_t(gy + 1) * a.pitch + gx + 1;
+    const double X = icr[i], Y = inb[i];
+    const double phd = s_phd[ey][ex], phl = s_phl[ey][ex];
+
+    // Cahn-Hilliard, composition_kernel src/discretization.cu:843-865
+    const double ocr = X + M.dt * (M.D[0][0] * lapCr + M.D[0][1] * lapNb);
+    const double onb = Y + M.dt * (M.D[1][0] * lapCr + M.D[1][1] * lapNb);
+
+    // Allen-Cahn, src/discretization.cu:888-980
+    Poly64 m;
+    m.lin[0] = s_pd[ey][ex];
+    m.lin[2] = s_pl[ey][ex];
+    m.lin[1] = 1.0 - m.lin[0] - m.lin[2];
+    m.mono[0] = m.lin[0] * m.lin[0];
+    m.mono[1] = m.lin[0] * m.lin[1];
+    m.mono[2] = m.lin[0] * m.lin[2];
+    m.mono[3] = m.lin[1] * m.lin[1];
+    m.mono[4] = m.lin[1] * m.lin[2];
+    m.mono[5] = m.lin[2] * m.lin[2];
+    m.rden = s_rden[ey][ex];
+    const double gam_Cr = s_gcr[ey][ex], gam_Nb = s_gnb[ey][ex];
+    const double gam_nrg = g64<0>(gam_Cr, gam_Nb);
+    const double dgGdxCr = dg64<0>(gam_Cr, gam_Nb);
+    const double dgGdxNb = dg64<1>(gam_Cr, gam_Nb);
+    double od, ol;
+    {
+      const double del_Cr = fict64<1, 0>(X, Y, m), del_Nb = fict64<1, 1>(X, Y, m);
+      const double del_nrg = g64<1>(del_Cr, del_Nb);
+      const double gp = gam_nrg - del_nrg - dgGdxCr * (gam_Cr - del_Cr) - dgGdxNb * (gam_Nb - del_Nb);
+      const double dF = -pp64(phd) * gp + 2.0 * M.omega[0] * phd * (phd - 1.0) * (2.0 * phd - 1.0) +
+                        2.0 * M.alpha * phd * phl * phl - M.kappa[0] * lapD;
+      od = phd - M.dt * M.L[0] * dF;
+    }
+    {
+      const double lav_Cr = fict64<2, 0>(X, Y, m), lav_Nb = fict64<2, 1>(X, Y, m);
+      const double lav_nrg = g64<2>(lav_Cr, lav_Nb);
+      const double gp = gam_nrg - lav_nrg - dgGdxCr * (gam_Cr - lav_Cr) - dgGdxNb * (gam_Nb - lav_Nb);
+      const double dF = -pp64(phl) * gp + 2.0 * M.omega[1] * phl * (phl - 1.0) * (2.0 * phl - 1.0) +
+                        2.0 * M.alpha * phl * phd * phd - M.kappa[1] * lapL;
+      ol = phl - M.dt * M.L[1] * dF;
+    }
+    const bool h = a.write_halo;
+    store_with_halo(static_cast<double*>(a.out[0]), a.pitch, gx, gy, a.Nx, a.Ny, ocr, h);
+    store_with_halo(static_cast<double*>(a.out[1]), a.pitch, gx, gy, a.Nx, a.Ny, onb, h);
+    store_with_halo(static_cast<double*>(a.out[2]), a.pitch, gx, gy, a.Nx, a.Ny, od, h);
+    store_with_halo(static_cast<double*>(a.out[3]), a.pitch, gx, gy, a.Nx, a.Ny, ol, h);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FP32 precision form.  Fields FP32; x_Cr, x_Nb carry Kahan compensation
+// arrays (and phi too when KPHI); Laplacians in difference form; the delta
+// and laves grand-potential differences as quadratics in x^gamma - xe.
+template <bool KPHI>
+__global__ void __launch_bounds__(kTX* kBY) k_step2d_f32(Step2DArgs a) {
+  __shared__ float s_phd[kEY][kEX], s_phl[kEY][kEX], s_gcr[kEY][kEX], s_gnb[kEY][kEX];
+  __shared__ float s_x[kEY][kEX], s_y[kEY][kEX];
+  const float* __restrict__ icr = static_cast<const float*>(a.in[0]);
+  const float* __restrict__ inb = static_cast<const float*>(a.in[1]);
+  const float* __restrict__ ipd = static_cast<const float*>(a.in[2]);
+  const float* __restrict__ ipl = static_cast<const float*>(a.in[3]);
+  const FastCoef& K = a.k;
+  const int x0 = blockIdx.x * kTX, y0 = blockIdx.y * kTY;
+  const int tid = threadIdx.y * kTX + threadIdx.x;
+
+  for (int e = tid; e < kEX * kEY; e += kTX * kBY) {
+    const int ex = e % kEX, ey = e / kEX;
+    const int gx = clampi(x0 + ex - 1, 0, a.Nx - 1);
+    const int gy = clampi(y0 + ey - 1, 0, a.Ny - 1);
+    const size_t i = size_t(gy + 1) * a.pitch + gx + 1;
+    const float X = icr[i], Y = inb[i], phd = ipd[i], phl = ipl[i];
+    const float pD = p32(phd), pL = p32(phl);
+    float gcr, gnb;
+    fict_gam32(K, X, Y, pD, p_gamma32(phd, phl, pD, pL), pL, gcr, gnb);
+    s_phd[ey][ex] = phd;
+    s_phl[ey][ex] = phl;
+    s_gcr[ey][ex] = gcr;
+    s_gnb[ey][ex] = gnb;
+    s_x[ey][ex] = X;
+    s_y[ey][ex] = Y;
+  }
+  __syncthreads();
+
+  const float idx2 = float(a.m.idx2[0]), idy2 = float(a.m.idx2[1]);
+  for (int r = threadIdx.y; r < kTY; r += kBY) {
+    const int gx = x0 + threadIdx.x, gy = y0 + r;
+    if (gx >= a.Nx || gy >= a.Ny) continue;
+    const int ex = threadIdx.x + 1, ey = r + 1;
+    auto lap = [&](float (*s)[kEX]) {
+      const float c = s[ey][ex];
+      const float sx = (s[ey][ex - 1] - c) + (s[ey][ex + 1] - c);
+      const float sy = (s[ey - 1][ex] - c) + (s[ey + 1][ex] - c);
+      return fmaf(sx, idx2, sy * idy2);
+    };
+    const float lapCr = lap(s_gcr), lapNb = lap(s_gnb), lapD = lap(s_phd), lapL = lap(s_phl);
+    const size_t i = size_t(gy + 1) * a.pitch + gx + 1;
+    const float X = s_x[ey][ex], Y = s_y[ey][ex];
+    const float phd = s_phd[ey][ex], phl = s_phl[ey][ex];
+
+    // Cahn-Hilliard with Kahan-compensated accumulation
+    float ocr, onb, ccr, cnb;
+    {
+      const float inc = fmaf(a.dtD[0][0], lapCr, a.dtD[0][1] * lapNb);
+      const float y = inc - a.cin[0][i];
+      const float t = X + y;
+      ccr = (t - X) - y;
+      ocr = t;
+    }
+    {
+      const float inc = fmaf(a.dtD[1][0], lapCr, a.dtD[1][1] * lapNb);
+      const float y = inc - a.cin[1][i];
+      const float t = Y + y;
+      cnb = (t - Y) - y;
+      onb = t;
+    }
+
+    // Allen-Cahn
+    const float u1 = s_gcr[ey][ex] - K.xe_gam[0], u2 = s_gnb[ey][ex] - K.xe_gam[1];
+    const float dPd = quad2(K.dP[0], u1, u2), dPl = quad2(K.dP[1], u1, u2);
+    const float dFd = -pp32(phd) * dPd + a.om2[0] * phd * (phd - 1.0f) * (2.0f * phd - 1.0f) +
+                      a.alpha2 * phd * phl * phl - a.kap[0] * lapD;
+    const float dFl = -pp32(phl) * dPl + a.om2[1] * phl * (phl - 1.0f) * (2.0f * phl - 1.0f) +
+                      a.alpha2 * phl * phd * phd - a.kap[1] * lapL;
+    float od, ol, cd = 0.f, cl = 0.f;
+    if (KPHI) {
+      const float yd = -a.dtL[0] * dFd - a.cin[2][i];
+      const float td = phd + yd;
+      cd = (td - phd) - yd;
+      od = td;
+      const float yl = -a.dtL[1] * dFl - a.cin[3][i];
+      const float tl = phl + yl;
+      cl = (tl - phl) - yl;
+      ol = tl;
+    } else {
+      od = fmaf(-a.dtL[0], dFd, phd);
+      ol = fmaf(-a.dtL[1], dFl, phl);
+    }
+    float* const* o = reinterpret_cast<float* const*>(a.out);
+    o[0][i] = ocr;
+    o[1][i] = onb;
+    o[2][i] = od;
+    o[3][i] = ol;
+    a.cout[0][i] = ccr;
+    a.cout[1][i] = cnb;
+    if (KPHI) {
+      a.cout[2][i] = cd;
+      a.cout[3][i] = cl;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Layout conversion between the reference's FP64 fields and the FP32 form.
+__global__ void k_import_f32(ConvArgs a) {
+  const int gx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int gy = blockIdx.y * blockDim.y + threadIdx.y;
+  if (gx >= a.Nx || gy >= a.Ny) return;
+  const size_t i64 = size_t(gy + 1) * a.pitch64 + gx + 1;
+  const size_t i32 = size_t(gy + 1) * a.pitch32 + gx + 1;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const double v = a.f64[k][i64];
+    const float hi = float(v);
+    a.f32[k][i32] = hi;
+    // compensation c holds -(low part) so that value = hi - c
+    if (a.c32[k]) a.c32[k][i32] = float(double(hi) - v);
+  }
+}
+
+__global__ void k_export_f32(ConvArgs a) {
+  const int gx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int gy = blockIdx.y * blockDim.y + threadIdx.y;
+  if (gx >= a.Nx || gy >= a.Ny) return;
+  const size_t i32 = size_t(gy + 1) * a.pitch32 + gx + 1;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    double v = double(a.f32[k][i32]);
+    if (a.c32[k]) v -= double(a.c32[k][i32]);
+    store_with_halo(a.f64[k], a.pitch64, gx, gy, a.Nx, a.Ny, v, true);
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+cudaError_t launch_step2d_f64(const Step2DArgs& a, cudaStream_t s) {
+  dim3 grid((a.Nx + kTX - 1) / kTX, (a.Ny + kTY - 1) / kTY);
+  dim3 block(kTX, kBY);
+  if (a.nine)
+    k_step2d_f64<true><<<grid, block, 0, s>>>(a);
+  else
+    k_step2d_f64<false><<<grid, block, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_step2d_f32(const Step2DArgs& a, cudaStream_t s) {
+  dim3 grid((a.Nx + kTX - 1) / kTX, (a.Ny + kTY - 1) / kTY);
+  dim3 block(kTX, kBY);
+  if (a.kahan_phi)
+    k_step2d_f32<true><<<grid, block, 0, s>>>(a);
+  else
+    k_step2d_f32<false><<<grid, block, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_import_f32(const ConvArgs& a, cudaStream_t s) {
+  dim3 block(32, 8);
+  dim3 grid((a.Nx + 31) / 32, (a.Ny + 7) / 8);
+  k_import_f32<<<grid, block, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_export_f32(const ConvArgs& a, cudaStream_t s) {
+  dim3 block(32, 8);
+  dim3 grid((a.Nx + 31) / 32, (a.Ny + 7) / 8);
+  k_export_f32<<<grid, block, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace pfa

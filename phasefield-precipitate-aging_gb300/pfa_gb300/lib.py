@@ -1,0 +1,285 @@
+"""ctypes binding of libpfa_gb300.so (the extern "C" surface of include/pfa_gb300.h).
+
+``Grid2D`` follows the reference's call sequence (src/main.cpp:229-321):
+init_cuda with the host fields, a step loop of device_evolution + pointer
+swap (optionally with nucleation), read_out_result.  The library is loaded
+from this package directory; if it is missing, import fails loudly -- there
+is no CPU fallback.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libpfa_gb300.so")
+
+FP64, FP32, FP32_KPHI = 0, 1, 2
+MODE_FUSED, MODE_COMPAT = 0, 1
+NUC_REFERENCE_GEOMETRY, NUC_FIXED_GEOMETRY = 0, 1
+PRECISIONS = {"fp64": FP64, "fp32": FP32, "fp32k": FP32_KPHI}
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_fp = ctypes.POINTER(ctypes.c_float)
+_i, _d = ctypes.c_int, ctypes.c_double
+
+
+class CudaData(ctypes.Structure):
+    """Layout of struct CudaData, src/type.h:58-107."""
+    _fields_ = ([("prng", ctypes.c_void_p)] +
+                [(n, ctypes.c_void_p) for n in ("str_A", "str_B", "str_C", "str_D")] +
+                [(n, ctypes.c_void_p) for n in ("ev_A", "ev_B", "ev_C", "ev_D")] +
+                [(n, _dp) for n in ("conc_Ni", "phi", "conc_Cr_old", "conc_Cr_new",
+                                    "conc_Nb_old", "conc_Nb_new", "phi_del_old", "phi_del_new",
+                                    "phi_lav_old", "phi_lav_new", "conc_Cr_gam", "conc_Cr_del",
+                                    "conc_Cr_lav", "conc_Nb_gam", "conc_Nb_del", "conc_Nb_lav")])
+
+
+_lib = None
+
+
+def load():
+    """Load (and type) the library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: build it with pfa_gb300.build.build()")
+    L = ctypes.CDLL(LIB_PATH)
+    P = ctypes.POINTER(CudaData)
+    sig = {
+        "pfa_last_error": (_i, []),
+        "pfa_error_string": (ctypes.c_char_p, [_i]),
+        "pfa_last_error_message": (ctypes.c_char_p, []),
+        "pfa_clear_error": (None, []),
+        "pfa_set_device": (_i, [_i]),
+        "pfa_device_count": (_i, []),
+        "pfa_set_mode": (_i, [P, _i]),
+        "pfa_set_precision": (_i, [P, _i]),
+        "pfa_set_nucleation": (_i, [P, ctypes.c_uint64, _i]),
+        "pfa_set_nucleation_args": (_i, [P, _i, _d, _d, _d, _d, _d, _d, _d]),
+        "pfa_init_cuda": (_i, [P, _i, _i, _i, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
+        "pfa_free_cuda": (_i, [P]),
+        "pfa_read_out_result": (_i, [P, _dp, _dp, _dp, _dp, _i, _i]),
+        "pfa_upload_fields": (_i, [P, _dp, _dp, _dp, _dp, _i, _i]),
+        "pfa_device_boundaries": (_i, [P, _i, _i, _i, _i, _i]),
+        "pfa_device_fictitious": (_i, [P, _i, _i, _i, _i, _i]),
+        "pfa_fictitious_boundaries": (_i, [P, _i, _i, _i, _i, _i]),
+        "pfa_device_laplacian": (_i, [P, _i, _i, _i, _i, _i, _d, _d]),
+        "pfa_device_laplacian_boundaries": (_i, [P, _i, _i, _i, _i, _i]),
+        "pfa_device_evolution": (_i, [P, _i, _i, _i, _i, _i, _d, _d]),
+        "pfa_device_init_prng": (_i, [P, _i, _i, _i, _i, _i]),
+        "pfa_device_nucleation": (_i, [P, _i, _i, _i, _i, _i] + [_d] * 8),
+        "pfa_device_dataviz": (_i, [P, _dp, _dp, _dp, _dp, _dp, _dp, _i, _i]),
+        "pfa_swap": (_i, [P]),
+        "pfa_run": (_i, [P, _i, _d, _d]),
+        "pfa_run_timed": (_i, [P, _i, _d, _d, _fp]),
+        "pfa_sync": (_i, [P]),
+        "pfa_stream": (ctypes.c_void_p, [P]),
+        "pfa_last_nucleation_events": (_i, [P, ctypes.POINTER(ctypes.c_int64),
+                                            ctypes.POINTER(ctypes.c_int32), _i]),
+        "pfa_summarize": (_i, [P, _dp]),
+        "pfa_model_params": (_i, [_d, _d, _d, _d, _d, _i, _i, _dp]),
+        "pfa_model_fast_coef": (_i, [_fp, _i]),
+        "pfa_philox_block": (_i, [ctypes.POINTER(ctypes.c_uint32), ctypes.c_uint64,
+                                  ctypes.POINTER(ctypes.c_uint32), _i]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+class PfaError(RuntimeError):
+    pass
+
+
+def check(rc, what=""):
+    if rc != 0:
+        L = load()
+        msg = L.pfa_last_error_message().decode(errors="replace")
+        raise PfaError(f"{what}: {L.pfa_error_string(rc).decode()} ({msg})")
+    return rc
+
+
+def _ptr(a):
+    return a.ctypes.data_as(_dp)
+
+
+def five_point_mask(dx, dy):
+    """3x3 mask of five_point_Laplacian_stencil, src/mesh.cpp:187-196 (same
+    floating-point expressions)."""
+    m = np.zeros((3, 3))
+    m[0, 1] = 1. / (dy * dy)
+    m[1, 0] = 1. / (dx * dx)
+    m[1, 1] = -2. * (dx * dx + dy * dy) / (dx * dx * dy * dy)
+    m[1, 2] = 1. / (dx * dx)
+    m[2, 1] = 1. / (dy * dy)
+    return m
+
+
+def nine_point_mask(dx, dy):
+    """nine_point_Laplacian_stencil, src/mesh.cpp:198-213."""
+    m = np.zeros((3, 3))
+    m[0, 0] = 1. / (6. * dx * dy)
+    m[0, 1] = 4. / (6. * dy * dy)
+    m[0, 2] = 1. / (6. * dx * dy)
+    m[1, 0] = 4. / (6. * dx * dx)
+    m[1, 1] = -10. * (dx * dx + dy * dy) / (6. * dx * dx * dy * dy)
+    m[1, 2] = 4. / (6. * dx * dx)
+    m[2, 0] = 1. / (6. * dx * dy)
+    m[2, 1] = 4. / (6. * dy * dy)
+    m[2, 2] = 1. / (6. * dx * dy)
+    return m
+
+
+def model_params(dx=5e-9, ifce_width=10e-9, xcr0=0.30, xnb0=0.02, meshres=None, dim=2,
+                 dt_rule=1):
+    """Model parameters from the library (src/main.cpp:252-268; see pfa_gb300.h)."""
+    out = np.zeros(13)
+    check(load().pfa_model_params(dx, ifce_width, xcr0, xnb0, dx if meshres is None else meshres,
+                                  dim, dt_rule, _ptr(out)), "pfa_model_params")
+    return {"D_Cr": [out[0], out[1]], "D_Nb": [out[2], out[3]], "kappa": [out[4], out[5]],
+            "omega": [out[6], out[7]], "Lmob": [out[8], out[9]], "alpha": out[10],
+            "dt": out[11], "rho": out[12], "dx": dx, "dy": dx, "dz": dx}
+
+
+class Grid2D:
+    """One 2D grid behind the reference's CudaData interface."""
+
+    def __init__(self, fields, params, precision="fp64", mode="fused", mask=None):
+        L = load()
+        self.L = L
+        f = [np.ascontiguousarray(a, dtype=np.float64) for a in fields]
+        self.ny, self.nx = f[0].shape
+        self.params = dict(params)
+        self.dev = CudaData()
+        if mask is None:
+            mask = five_point_mask(params["dx"], params.get("dy", params["dx"]))
+        self.mask = np.ascontiguousarray(mask, dtype=np.float64)
+        arr = lambda v: np.ascontiguousarray(v, dtype=np.float64)
+        self._consts = [arr(params["kappa"]), arr(params["omega"]), arr(params["Lmob"]),
+                        arr(params["D_Cr"]), arr(params["D_Nb"])]
+        check(L.pfa_init_cuda(ctypes.byref(self.dev), self.nx, self.ny, 3, _ptr(self.mask),
+                              *[_ptr(c) for c in self._consts], *[_ptr(a) for a in f]),
+              "pfa_init_cuda")
+        self._live = True
+        if mode == "compat":
+            check(L.pfa_set_mode(ctypes.byref(self.dev), MODE_COMPAT), "pfa_set_mode")
+        self.set_precision(precision)
+
+    @property
+    def ref(self):
+        return ctypes.byref(self.dev)
+
+    def set_precision(self, precision):
+        check(self.L.pfa_set_precision(self.ref, PRECISIONS[precision]), "pfa_set_precision")
+        self.precision = precision
+
+    def set_nucleation(self, seed=42, geometry=NUC_REFERENCE_GEOMETRY, interval=0,
+                       sigma=(0.13, 0.13), unit_a=0.352e-9, d=None, dt_nuc=None):
+        check(self.L.pfa_set_nucleation(self.ref, seed, geometry), "pfa_set_nucleation")
+        d = d or (self.params["dx"],) * 3
+        dt_nuc = dt_nuc if dt_nuc is not None else interval * self.params["dt"]
+        check(self.L.pfa_set_nucleation_args(self.ref, interval, sigma[0], sigma[1], unit_a,
+                                             d[0], d[1], d[2], dt_nuc), "pfa_set_nucleation_args")
+
+    def run(self, nsteps, dt=None, alpha=None):
+        dt = self.params["dt"] if dt is None else dt
+        alpha = self.params["alpha"] if alpha is None else alpha
+        check(self.L.pfa_run(self.ref, int(nsteps), alpha, dt), "pfa_run")
+
+    def run_timed(self, nsteps):
+        ms = ctypes.c_float()
+        check(self.L.pfa_run_timed(self.ref, int(nsteps), self.params["alpha"], self.params["dt"],
+                                   ctypes.byref(ms)), "pfa_run_timed")
+        return ms.value
+
+    def step_stages(self, dt=None, alpha=None):
+        """One step through the reference's six stage calls + swap (src/main.cpp:289-321)."""
+        dt = self.params["dt"] if dt is None else dt
+        alpha = self.params["alpha"] if alpha is None else alpha
+        a = (self.ref, self.nx, self.ny, 3, 13, 13)
+        L = self.L
+        check(L.pfa_device_boundaries(*a), "device_boundaries")
+        check(L.pfa_device_fictitious(*a), "device_fictitious")
+        check(L.pfa_fictitious_boundaries(*a), "fictitious_boundaries")
+        check(L.pfa_device_laplacian(*a, self.params["dx"], self.params.get("dy", self.params["dx"])),
+              "device_laplacian")
+        check(L.pfa_device_laplacian_boundaries(*a), "device_laplacian_boundaries")
+        check(L.pfa_device_evolution(*a, alpha, dt), "device_evolution")
+        check(L.pfa_swap(self.ref), "swap")
+
+    def nucleate(self, sigma=(0.13, 0.13), unit_a=0.352e-9, d=None, dt_nuc=None):
+        """device_nucleation on the *_new fields (call before the swap in a manual loop)."""
+        d = d or (self.params["dx"],) * 3
+        check(self.L.pfa_device_nucleation(self.ref, self.nx, self.ny, 3, 13, 13, sigma[0],
+                                           sigma[1], unit_a, 0.0, d[0], d[1], d[2], dt_nuc),
+              "device_nucleation")
+
+    def swap(self):
+        check(self.L.pfa_swap(self.ref), "swap")
+
+    def events(self, cap=1 << 16):
+        cells = (ctypes.c_int64 * cap)()
+        ph = (ctypes.c_int32 * cap)()
+        n = self.L.pfa_last_nucleation_events(self.ref, cells, ph, cap)
+        if n < 0:
+            check(self.L.pfa_last_error(), "events")
+        return [(cells[k], ph[k]) for k in range(min(n, cap))]
+
+    def read(self, out=None):
+        out = out or [np.empty((self.ny, self.nx)) for _ in range(4)]
+        check(self.L.pfa_read_out_result(self.ref, *[_ptr(a) for a in out], self.nx, self.ny),
+              "read_out_result")
+        return out
+
+    def upload(self, fields):
+        f = [np.ascontiguousarray(a, dtype=np.float64) for a in fields]
+        check(self.L.pfa_upload_fields(self.ref, *[_ptr(a) for a in f], self.nx, self.ny),
+              "upload_fields")
+
+    def dataviz(self):
+        out = [np.empty((self.ny, self.nx)) for _ in range(6)]
+        check(self.L.pfa_device_dataviz(self.ref, *[_ptr(a) for a in out], self.nx, self.ny),
+              "device_dataviz")
+        return out
+
+    def summarize(self):
+        out = np.zeros(5)
+        check(self.L.pfa_summarize(self.ref, _ptr(out)), "summarize")
+        return out
+
+    def sync(self):
+        check(self.L.pfa_sync(self.ref), "sync")
+
+    def close(self):
+        if self._live:
+            self._live = False
+            check(self.L.pfa_free_cuda(self.ref), "free_cuda")
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def philox_device(ctr, key):
+    """Philox4x32-10 of n counters (n x 4 uint32) on the device."""
+    ctr = np.ascontiguousarray(ctr, dtype=np.uint32)
+    n = ctr.shape[0]
+    out = np.zeros((n, 4), dtype=np.uint32)
+    u32p = ctypes.POINTER(ctypes.c_uint32)
+    check(load().pfa_philox_block(ctr.ctypes.data_as(u32p), int(key), out.ctypes.data_as(u32p), n),
+          "pfa_philox_block")
+    return out
+
+
+def fast_coef():
+    out = np.zeros(44, dtype=np.float32)
+    check(load().pfa_model_fast_coef(out.ctypes.data_as(_fp), 44), "pfa_model_fast_coef")
+    return {"den": out[0:6], "num": out[6:30].reshape(2, 12), "dP": out[30:42].reshape(2, 6),
+            "xe_gam": out[42:44]}

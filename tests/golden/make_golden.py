@@ -1,0 +1,175 @@
+"""Generate the golden vectors under tests/golden/ (run in the build container).
+
+The vectors come from the reference's own compiled code: oracle/Makefile's
+`ref` target compiles usnistgov/phasefield-precipitate-aging's
+thermo/parabola625.c and thermo/nucleation.c where they lie and links them to
+the oracle's step semantics (oracle/ref_shim.cpp).  The tests then pin the
+oracle's restated energies and the CUDA library against these files; the
+reference checkout itself is not needed to run them.
+
+    python tests/golden/make_golden.py [--ref /path/to/reference]
+"""
+import argparse
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(REPO, "oracle"))
+sys.path.insert(0, os.path.join(REPO, "phasefield-precipitate-aging_gb300"))
+
+import oracle as O  # noqa: E402
+from pfa_gb300 import ic  # noqa: E402
+
+# Nucleation parameters that give P_nuc of a few percent per cell at the
+# enriched compositions (the physical ones give exactly 0): fixed geometry.
+NUC_A = dict(sigma=(0.05, 0.05), unit_a=0.352e-9, d=(2e-10, 2e-10, 1.0), dt=1e6)
+NUC_B = dict(sigma=(0.05, 0.05), unit_a=0.352e-9, d=(1e-10, 1e-10, 4.0), dt=1e6)
+
+
+def nuc_struct(p):
+    s = O.OrcNucParams()
+    s.sigma[0], s.sigma[1] = p["sigma"]
+    s.unit_a = p["unit_a"]
+    s.dx, s.dy, s.dz = p["d"]
+    s.dt = p["dt"]
+    return s
+
+
+def energies(ref, rng):
+    n = 400
+    xcr = rng.uniform(0.0, 0.6, n)
+    xnb = rng.uniform(0.0, 0.3, n)
+    pd = rng.uniform(0, 1, n)
+    pl = rng.uniform(0, 1, n) * (1 - pd)
+    pd[:25], pl[:25] = 1.0, 0.0     # pure delta
+    pd[25:50], pl[25:50] = 0.0, 1.0  # pure laves
+    pd[50:75], pl[50:75] = 0.0, 0.0  # pure gamma
+    pg = 1 - pd - pl
+    phi = rng.uniform(-0.1, 1.1, n)
+    out = dict(xcr=xcr, xnb=xnb, pd=pd, pl=pl, pg=pg, phi=phi,
+               p=ref.p(phi), pprime=ref.pprime(phi))
+    for ph in range(3):
+        for c in range(2):
+            out[f"fict_{ph}_{c}"] = ref.fict(ph, c, xcr, xnb, pd, pg, pl)
+        out[f"g_{ph}"] = ref.g(ph, xcr, xnb)
+    mx = rng.uniform(0.05, 0.5, n)
+    my = rng.uniform(0.005, 0.3, n)
+    out["dx_cr"], out["dx_nb"] = mx, my
+    for r in range(2):
+        for c in range(2):
+            out[f"D_{r}_{c}"] = ref.D(r, c, mx, my)
+    # nucleation probability at enriched and matrix compositions
+    nx_ = 200
+    x = np.concatenate([rng.uniform(0.2473, 0.2967, nx_), rng.uniform(0.2794, 0.3288, nx_)])
+    y = np.concatenate([rng.uniform(0.1659, 0.1726, nx_), rng.uniform(0.0202, 0.0269, nx_)])
+    sig = np.where(np.arange(2 * nx_) % 2 == 0, 0.05, 0.13)
+    dV = (2e-10) ** 2 * 1.0
+    Va = 0.25 * 0.352e-9 ** 3
+    R, P = [], []
+    for a, b, s in zip(x, y, sig):
+        dG = ref.g(0, [a], [b])[0]
+        r_, p_ = ref.nucleation_probability_sphere(a, b, dG, ref.D(0, 0, [a], [b])[0],
+                                                   ref.D(1, 1, [a], [b])[0], s, Va, dV / Va, dV, 1e6)
+        R.append(r_)
+        P.append(p_)
+    out.update(nuc_x=x, nuc_y=y, nuc_sigma=sig, nuc_R=np.array(R), nuc_P=np.array(P))
+    np.savez_compressed(os.path.join(HERE, "energies.npz"), **out)
+
+
+def steps(ref):
+    prm = O.model_params()
+    f0 = ic.grid2d(30, 22, seed=11, stripe_width=10, n_particles=4, radius=4.0)
+    snaps = {}
+    cur = f0
+    done = 0
+    for k in (1, 10, 100, 400):
+        cur = ref.run2d(cur, prm, k - done)
+        done = k
+        for j, name in enumerate(("cr", "nb", "pd", "pl")):
+            snaps[f"s{k}_{name}"] = cur[j]
+    np.savez_compressed(os.path.join(HERE, "step2d.npz"),
+                        **{f"ic_{n}": f0[j] for j, n in enumerate(("cr", "nb", "pd", "pl"))},
+                        **snaps, params=np.array([prm.dt, prm.dx]))
+    # reference dt rule (stable for a particle-free grid over a short run)
+    prm0 = O.model_params(dt_rule=0)
+    g0 = ic.grid2d(17, 13, seed=12, stripe_width=6, n_particles=0)
+    r0 = ref.run2d(g0, prm0, 50)
+    np.savez_compressed(os.path.join(HERE, "step2d_refdt.npz"),
+                        **{f"ic_{n}": g0[j] for j, n in enumerate(("cr", "nb", "pd", "pl"))},
+                        **{f"s50_{n}": r0[j] for j, n in enumerate(("cr", "nb", "pd", "pl"))},
+                        params=np.array([prm0.dt, prm0.dx]))
+
+
+def nucleation(ref):
+    out = {}
+    for tag, p in (("a", NUC_A), ("b", NUC_B)):
+        f = ic.grid2d(64, 48, seed=21, matrix=(0.2720, 0.1692), enrich=(0.2720, 0.1692),
+                      stripes=[], n_particles=1, radius=5.0)
+        res, events, n = ref.nucleation2d(f, nuc_struct(p), seed=42, call=0)
+        for j, name in enumerate(("cr", "nb", "pd", "pl")):
+            out[f"{tag}_ic_{name}"] = f[j]
+            out[f"{tag}_out_{name}"] = res[j]
+        out[f"{tag}_cells"] = np.array([e[0] for e in events], dtype=np.int64)
+        out[f"{tag}_phases"] = np.array([e[1] for e in events], dtype=np.int32)
+        out[f"{tag}_r"] = np.array([e[4] for e in events])
+    np.savez_compressed(os.path.join(HERE, "nucleation.npz"), **out)
+
+
+def summary(ref):
+    f = ic.grid2d(40, 31, seed=31)
+    np.savez_compressed(os.path.join(HERE, "summary.npz"),
+                        **{f"ic_{n}": f[j] for j, n in enumerate(("cr", "nb", "pd", "pl"))},
+                        summary=ref.summarize(f))
+
+
+def abi_symbols(refdir):
+    """Mangled names the reference's caller links against: compile a stub
+    that calls every host entry point through the reference's own headers."""
+    stub = os.path.join(HERE, "_abi_stub.cpp")
+    with open(stub, "w") as fh:
+        fh.write('#include "data.cuh"\n#include "discretization.cuh"\n'
+                 "void use(HostData* h, CudaData* d, double* k) {\n"
+                 "  checkCuda(cudaSuccess); init_cuda(h, 3, 3, 3, k, k, k, k, k, d);\n"
+                 "  free_cuda(d); read_out_result(d, h, 3, 3); nTiles(1, 2, 3);\n"
+                 "  device_fictitious(d, 1, 1, 1, 1, 1); device_boundaries(d, 1, 1, 1, 1, 1);\n"
+                 "  fictitious_boundaries(d, 1, 1, 1, 1, 1);\n"
+                 "  device_laplacian_boundaries(d, 1, 1, 1, 1, 1);\n"
+                 "  device_laplacian(d, 1, 1, 1, 1, 1, 1.0, 1.0);\n"
+                 "  device_evolution(d, 1, 1, 1, 1, 1, 1.0, 1.0);\n"
+                 "  device_init_prng(d, 1, 1, 1, 1, 1);\n"
+                 "  device_nucleation(d, 1, 1, 1, 1, 1, 1., 1., 1., 1., 1., 1., 1., 1.);\n"
+                 "  device_dataviz(d, h, 1, 1, 1, 1, 1);\n}\n")
+    obj = stub + ".o"
+    subprocess.run(["nvcc", "-x", "cu", "-c", stub, "-o", obj, "-I", os.path.join(refdir, "src"),
+                    "-I", os.path.join(refdir, "thermo")], check=True)
+    nm = subprocess.run(["nm", "-u", obj], capture_output=True, text=True, check=True).stdout
+    # C++ (mangled) entry points only; the CUDA runtime's own symbols have C names
+    syms = sorted({ln.split()[-1] for ln in nm.splitlines() if ln.split()[-1].startswith("_Z")})
+    with open(os.path.join(HERE, "reference_abi_symbols.txt"), "w") as fh:
+        fh.write("\n".join(syms) + "\n")
+    os.remove(stub)
+    os.remove(obj)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    args = ap.parse_args()
+    subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "ref", f"REF={args.ref}"],
+                   check=True)
+    ref = O.load_ref()
+    rng = np.random.default_rng(20261203)
+    energies(ref, rng)
+    steps(ref)
+    nucleation(ref)
+    summary(ref)
+    abi_symbols(args.ref)
+    print("golden vectors written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,116 @@
+"""The CPU oracle against the reference's own compiled code (golden vectors).
+
+tests/golden/*.npz were produced by tests/golden/make_golden.py from the
+reference's thermo/parabola625.c and thermo/nucleation.c; these tests pin
+the oracle's restated energy tables and step semantics to them.
+"""
+import numpy as np
+
+import oracle as O
+from conftest import field_err, fields_of, golden
+
+
+def test_energies_match_reference(orc):
+    g = golden("energies.npz")
+    x, y, pd, pg, pl = g["xcr"], g["xnb"], g["pd"], g["pg"], g["pl"]
+    np.testing.assert_allclose(orc.p(g["phi"]), g["p"], rtol=0, atol=1e-15)
+    np.testing.assert_allclose(orc.pprime(g["phi"]), g["pprime"], rtol=0, atol=1e-14)
+    for ph in range(3):
+        for c in range(2):
+            ref = g[f"fict_{ph}_{c}"]
+            got = orc.fict(ph, c, x, y, pd, pg, pl)
+            assert np.max(np.abs(got - ref)) <= 1e-14 * np.max(np.abs(ref)), (ph, c)
+        ref = g[f"g_{ph}"]
+        assert np.max(np.abs(orc.g(ph, x, y) - ref)) <= 1e-14 * np.max(np.abs(ref))
+    for r in range(2):
+        for c in range(2):
+            ref = g[f"D_{r}_{c}"]
+            got = orc.D(r, c, g["dx_cr"], g["dx_nb"])
+            assert np.max(np.abs(got - ref)) <= 1e-14 * np.max(np.abs(ref)), (r, c)
+
+
+def test_nucleation_probability_matches_reference(orc):
+    g = golden("energies.npz")
+    Va = 0.25 * 0.352e-9 ** 3
+    dV = (2e-10) ** 2 * 1.0
+    for a, b, s, R, P in zip(g["nuc_x"], g["nuc_y"], g["nuc_sigma"], g["nuc_R"], g["nuc_P"]):
+        dG = orc.g(0, [a], [b])[0]
+        r_, p_ = orc.nucleation_probability_sphere(a, b, dG, orc.D(0, 0, [a], [b])[0],
+                                                   orc.D(1, 1, [a], [b])[0], s, Va, dV / Va, dV, 1e6)
+        assert abs(r_ - R) <= 1e-14 * abs(R)
+        assert abs(p_ - P) <= 1e-12 * max(abs(P), 1e-3)
+
+
+def test_step_matches_reference(orc):
+    g = golden("step2d.npz")
+    prm = O.model_params()
+    assert prm.dt == g["params"][0] and prm.dx == g["params"][1]
+    cur = fields_of(g, "ic")
+    done = 0
+    for k in (1, 10, 100, 400):
+        cur = orc.run2d(cur, prm, k - done)
+        done = k
+        err = field_err(cur, fields_of(g, f"s{k}"))
+        assert max(err) <= 1e-13, (k, err)
+
+
+def test_step_reference_dt_rule(orc):
+    g = golden("step2d_refdt.npz")
+    prm = O.model_params(dt_rule=0)
+    assert prm.dt == g["params"][0]
+    out = orc.run2d(fields_of(g, "ic"), prm, 50)
+    assert max(field_err(out, fields_of(g, "s50"))) <= 1e-13
+
+
+def test_nucleation_replica_matches_reference(orc):
+    from golden.make_golden import NUC_A, NUC_B, nuc_struct
+    g = golden("nucleation.npz")
+    for tag, p in (("a", NUC_A), ("b", NUC_B)):
+        res, events, n = orc.nucleation2d(fields_of(g, f"{tag}_ic"), nuc_struct(p), 42, 0)
+        assert n == len(g[f"{tag}_cells"]) and n > 10
+        assert [e[0] for e in events] == list(g[f"{tag}_cells"])
+        assert [e[1] for e in events] == list(g[f"{tag}_phases"])
+        for a, b in zip(res, fields_of(g, f"{tag}_out")):
+            assert np.array_equal(a, b)
+
+
+def test_summary_matches_reference(orc):
+    g = golden("summary.npz")
+    s = orc.summarize(fields_of(g, "ic"))
+    np.testing.assert_allclose(s, g["summary"], rtol=1e-14, atol=0)
+
+
+def test_philox_known_answers():
+    # Known-answer vectors of Philox4x32-10 published with the Random123
+    # library (Salmon et al., SC'11).
+    kat = [
+        ([0, 0, 0, 0], [0, 0], [0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8]),
+        ([0xffffffff] * 4, [0xffffffff] * 2, [0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd]),
+        ([0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344], [0xa4093822, 0x299f31d0],
+         [0xd16cfe09, 0x94fdcceb, 0x5001e420, 0x24126ea1]),
+    ]
+    for c, k, want in kat:
+        assert O.philox(c, k) == want
+
+
+def test_oracle_conserves_mass(orc):
+    from pfa_gb300 import ic
+    prm = O.model_params()
+    f = ic.grid2d(40, 30, seed=3, stripe_width=10, n_particles=3, radius=4.0)
+    s0 = orc.summarize(f)
+    out = orc.run2d(f, prm, 200)
+    s1 = orc.summarize(out)
+    assert abs(s1[0] - s0[0]) < 1e-13 and abs(s1[1] - s0[1]) < 1e-13
+
+
+def test_oracle_3d_reduces_to_2d(orc):
+    """A 3D grid uniform along z evolves like the 2D grid (7-point stencil with
+    zero z-flux)."""
+    from pfa_gb300 import ic
+    prm = O.model_params()
+    f2 = ic.grid2d(12, 10, seed=4, stripe_width=4, n_particles=2, radius=3.0)
+    f3 = [np.repeat(a[None, :, :], 5, axis=0) for a in f2]
+    o2 = orc.run2d(f2, prm, 20)
+    o3 = orc.run3d(f3, prm, 20)
+    for a, b in zip(o3, o2):
+        assert np.max(np.abs(a[2, 1:-1, 1:-1] - b[1:-1, 1:-1])) <= 1e-12 * np.max(np.abs(b))

@@ -1,0 +1,201 @@
+"""GPU parity of the 2D step (through the C ABI) against the oracle and the
+reference-generated golden vectors.
+
+Tolerances: the plain FP64 step within 1e-12 of the reference (per field,
+max|a - b| / max|b| over the interior and the ghost edges); the FP32
+precision form within 1e-5 absolute of FP64 (fields are O(0.01 - 1)).
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import field_err, fields_of, golden, interior
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12
+FP32_TOL = 1e-5
+
+
+def _params(pfa):
+    return pfa.model_params()
+
+
+def test_fp64_matches_reference_golden(pfa):
+    g = golden("step2d.npz")
+    p = _params(pfa)
+    assert p["dt"] == g["params"][0]
+    grid = pfa.Grid2D(fields_of(g, "ic"), p)
+    done = 0
+    for k in (1, 10, 100, 400):
+        grid.run(k - done)
+        done = k
+        err = field_err(grid.read(), fields_of(g, f"s{k}"))
+        assert max(err) <= FP64_TOL, (k, err)
+    grid.close()
+
+
+def test_fp64_reference_dt_rule_golden(pfa):
+    g = golden("step2d_refdt.npz")
+    p = pfa.model_params(dt_rule=0)
+    grid = pfa.Grid2D(fields_of(g, "ic"), p)
+    grid.run(50)
+    assert max(field_err(grid.read(), fields_of(g, "s50"))) <= FP64_TOL
+    grid.close()
+
+
+@pytest.mark.parametrize("shape", [(1, 1), (5, 7), (17, 13), (33, 65), (100, 3), (64, 64)])
+def test_fp64_odd_sizes_match_oracle(pfa, orc, shape):
+    from pfa_gb300 import ic
+    ny, nx = shape
+    p = _params(pfa)
+    f = ic.grid2d(nx, ny, seed=nx * 100 + ny, stripe_width=max(1, nx // 3),
+                  n_particles=1 if min(nx, ny) > 12 else 0, radius=3.0)
+    want = orc.run2d(f, O.model_params(), 60)
+    grid = pfa.Grid2D(f, p)
+    grid.run(60)
+    got = grid.read()
+    assert max(field_err(got, want)) <= FP64_TOL
+    grid.close()
+
+
+def test_fp64_config1_1000_steps(pfa, orc):
+    """The 256 x 256 workload (one stripe, four particles), 1000 steps."""
+    from pfa_gb300 import ic
+    f = ic.config1()
+    want = orc.run2d(f, O.model_params(), 1000)
+    grid = pfa.Grid2D(f, _params(pfa))
+    grid.run(1000)
+    err = field_err(grid.read(), want)
+    assert max(err) <= FP64_TOL, err
+    grid.close()
+
+
+def test_halo_mirrors_interior(pfa):
+    from pfa_gb300 import ic
+    f = ic.grid2d(40, 30, seed=5, stripe_width=8, n_particles=2, radius=4.0)
+    grid = pfa.Grid2D(f, _params(pfa))
+    grid.run(7)
+    for a in grid.read():
+        assert np.array_equal(a[0, 1:-1], a[1, 1:-1])
+        assert np.array_equal(a[-1, 1:-1], a[-2, 1:-1])
+        assert np.array_equal(a[1:-1, 0], a[1:-1, 1])
+        assert np.array_equal(a[1:-1, -1], a[1:-1, -2])
+    grid.close()
+
+
+def test_stage_calls_match_oracle_and_fused(pfa, orc):
+    """Compat mode runs the reference's six stage functions; each step must
+    match the oracle, and the fused path, to 1e-12."""
+    from pfa_gb300 import ic
+    f = ic.grid2d(45, 37, seed=8, stripe_width=9, n_particles=2, radius=4.0)
+    p = _params(pfa)
+    want = orc.run2d(f, O.model_params(), 25)
+    stages = pfa.Grid2D(f, p, mode="compat")
+    for _ in range(25):
+        stages.step_stages()
+    got = stages.read()
+    assert max(field_err(got, want)) <= FP64_TOL
+    fused = pfa.Grid2D(f, p)
+    fused.run(25)
+    assert max(field_err(fused.read(), got)) <= FP64_TOL
+    # the intermediate gamma compositions of the last device_fictitious
+    stages.close()
+    fused.close()
+
+
+def test_nine_point_mask_fused_matches_stages(pfa):
+    from pfa_gb300 import ic
+    f = ic.grid2d(33, 29, seed=9, stripe_width=7, n_particles=2, radius=4.0)
+    p = _params(pfa)
+    m9 = pfa.nine_point_mask(p["dx"], p["dx"])
+    a = pfa.Grid2D(f, p, mask=m9)
+    b = pfa.Grid2D(f, p, mask=m9, mode="compat")
+    a.run(30)
+    for _ in range(30):
+        b.step_stages()
+    assert max(field_err(a.read(), b.read())) <= FP64_TOL
+    a.close()
+    b.close()
+
+
+def test_graph_run_equals_single_steps(pfa):
+    from pfa_gb300 import ic
+    f = ic.grid2d(50, 40, seed=10, stripe_width=10, n_particles=2, radius=4.0)
+    p = _params(pfa)
+    for prec in ("fp64", "fp32"):
+        a = pfa.Grid2D(f, p, precision=prec)
+        a.run(37)
+        b = pfa.Grid2D(f, p, precision=prec)
+        for _ in range(37):
+            b.run(1)
+        for x, y in zip(a.read(), b.read()):
+            assert np.array_equal(x, y), prec
+        a.close()
+        b.close()
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp32k"])
+def test_fp32_error_against_fp64(pfa, orc, precision):
+    """The precision form's per-field max error after 1000 steps of the
+    256 x 256 workload, against the FP64 oracle."""
+    from pfa_gb300 import ic
+    f = ic.config1()
+    want = orc.run2d(f, O.model_params(), 1000)
+    grid = pfa.Grid2D(f, _params(pfa), precision=precision)
+    grid.run(1000)
+    got = grid.read()
+    err = [float(np.max(np.abs(interior(a) - interior(b)))) for a, b in zip(got, want)]
+    print(precision, "max field error", err)
+    assert max(err) <= FP32_TOL, err
+    grid.close()
+
+
+def test_read_upload_roundtrip_and_summary(pfa, orc):
+    from pfa_gb300 import ic
+    f = ic.grid2d(70, 52, seed=12)
+    grid = pfa.Grid2D(f, _params(pfa))
+    got = grid.read()
+    for a, b in zip(got, f):
+        assert np.array_equal(a, b)
+    np.testing.assert_allclose(grid.summarize(), orc.summarize(f), rtol=1e-14)
+    g = golden("summary.npz")
+    grid2 = pfa.Grid2D(fields_of(g, "ic"), _params(pfa))
+    np.testing.assert_allclose(grid2.summarize(), g["summary"], rtol=1e-13)
+    grid.run(5)
+    grid.upload(f)
+    assert all(np.array_equal(a, b) for a, b in zip(grid.read(), f))
+    grid.close()
+    grid2.close()
+
+
+def test_dataviz(pfa, orc):
+    from pfa_gb300 import ic
+    f = ic.grid2d(30, 20, seed=13, stripe_width=6, n_particles=1, radius=4.0)
+    grid = pfa.Grid2D(f, _params(pfa))
+    grid.run(3)
+    cr, nb, ni, pd, pl, phi = grid.dataviz()
+    np.testing.assert_array_equal(ni, 1.0 - cr - nb)
+    np.testing.assert_allclose(phi, orc.p(pd).reshape(pd.shape) + orc.p(pl).reshape(pl.shape),
+                               rtol=0, atol=1e-15)
+    grid.close()
+
+
+def test_fp32_summary_conserves_mass(pfa):
+    from pfa_gb300 import ic
+    f = ic.grid2d(128, 96, seed=14, stripe_width=20, n_particles=4, radius=6.0)
+    grid = pfa.Grid2D(f, _params(pfa), precision="fp32")
+    s0 = grid.summarize()
+    grid.run(500)
+    s1 = grid.summarize()
+    # Kahan-compensated compositions: the mean moves by less than FP32 rounding
+    assert abs(s1[0] - s0[0]) < 1e-8 and abs(s1[1] - s0[1]) < 1e-8
+    grid.close()
+
+
+def test_errors_are_reported_not_fallen_back(pfa):
+    import ctypes
+    L = pfa.load()
+    dev = pfa.CudaData()
+    assert L.pfa_run(ctypes.byref(dev), 1, 1.0, 1.0) == 3  # PFA_ESTATE
+    L.pfa_clear_error()
