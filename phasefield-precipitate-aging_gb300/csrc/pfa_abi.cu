@@ -266,6 +266,12 @@ static int nucleate(CudaData* dev, State* s, double sig_d, double sig_l, double 
   // dx * nx and dy * ny; the fixed geometry passes the spacing itself.
   const double kdx = s->geometry == PFA_NUC_REFERENCE_GEOMETRY ? dx * s->nx : dx;
   const double kdy = s->geometry == PFA_NUC_REFERENCE_GEOMETRY ? dy * s->ny : dy;
+  const bool ok = std::isfinite(kdx) && std::isfinite(kdy) && std::isfinite(dz) &&
+                  std::isfinite(dt) && std::isfinite(unit_a) && kdx > 0 && kdy > 0 && dz > 0 &&
+                  dt > 0 && unit_a > 0 && std::isfinite(sig_d) && std::isfinite(sig_l);
+  if (!ok) return fail(PFA_EINVAL, "nucleation: spacing, time and lattice must be finite and > 0");
+  if (!(1.75e-9 / kdx <= kNucMaxScan))
+    return fail(PFA_EINVAL, "nucleation: neighbourhood scan radius 1.75 nm / dx exceeds 64 cells");
   a.dx = kdx;
   a.dV = kdx * kdy * dz;
   a.Vatom = 0.25 * unit_a * unit_a * unit_a;
@@ -649,6 +655,7 @@ static int check_nucleation_status(State* s) {
   CK(cudaStreamSynchronize(s->st));
   if (st) {
     CK(cudaMemsetAsync(s->ev_status, 0, sizeof(int), s->st));
+    if (st == 2) return fail(PFA_EINVAL, "nucleation: a nucleus radius exceeded 256 cells (not painted)");
     return fail(PFA_EOVERFLOW, "nucleation: more events than the event buffer holds");
   }
   return 0;

@@ -177,7 +177,12 @@ __global__ void __launch_bounds__(256) k_nuc_decide(NucArgs a) {
           probability_sphere(X, Y, dG, dcc, dnn, a.sigma[ph], a.Vatom, a.n_gam, a.dV, a.dt, Rstar, P);
           if (Rstar > 0.) {
             rp[ph] = Rstar / a.dx;
-            if (P - u[ph] > 0) mask |= 1 << ph;
+            if (P - u[ph] > 0) {
+              if (rp[ph] <= kNucMaxRadius)
+                mask |= 1 << ph;
+              else
+                atomicExch(a.status, 2);  // nucleus wider than the paint limit: reported
+            }
           }
         }
         if (mask) {

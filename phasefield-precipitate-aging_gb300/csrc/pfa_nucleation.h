@@ -9,6 +9,8 @@ namespace pfa {
 
 constexpr int kNucCap = 1 << 14;  // events per nucleation call (scratch capacity)
 constexpr int kNucIdxBits = 14;   // low key bits carrying the event index
+constexpr double kNucMaxScan = 64.0;    // largest neighbourhood scan radius (cells)
+constexpr double kNucMaxRadius = 256.0; // largest nucleus radius painted (cells)
 
 struct NucEvent {
   long long cell;  // reference linear index nx * y + x (halo layout)
