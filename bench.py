@@ -165,6 +165,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp32k"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    ap.add_argument("--only", default="all", choices=["all", "value"],
+                    help="'value': only the device-resident timed run (for profiler captures)")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if args.warmup < 3:
@@ -218,6 +220,12 @@ def main():
     barrier()
     t = max_over_ranks(ms / 1e3)
     value = ws * cells * STEPS_PER_BENCH_STEP * args.steps / t
+    if args.only == "value":
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": "cell-updates/s",
+                              "ms_per_step": 1e3 * t / args.steps, "partial": "value only"}))
+        g.close()
+        return
 
     # kernel-only time of the step kernel (no nucleation): average launch
     g2 = pl.Grid2D(fields, params, precision=args.precision)

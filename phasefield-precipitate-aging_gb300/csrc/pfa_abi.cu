@@ -163,6 +163,7 @@ static ConvArgs conv_args(CudaData* dev, State* s) {
   c.Ny = s->Ny;
   c.pitch64 = s->nx;
   c.pitch32 = s->pitch32;
+  c.phi_fix = !kphi;
   return c;
 }
 
@@ -257,6 +258,7 @@ static int nucleate(CudaData* dev, State* s, double sig_d, double sig_l, double 
     }
     a.pitch = s->pitch32;
     a.is_f32 = 1;
+    a.phi_fix = s->precision == PFA_FP32;
   }
   a.Nx = s->Nx;
   a.Ny = s->Ny;
@@ -996,6 +998,7 @@ int pfa_summarize(struct CudaData* dev, double* out) {
     a.c[0] = s->c32[s->cur][0];
     a.c[1] = s->c32[s->cur][1];
     a.is_f32 = 1;
+    a.phi_fix = s->precision == PFA_FP32;
     a.pitch = s->pitch32;
   } else {
     a.f[0] = dev->conc_Cr_old;

@@ -94,6 +94,33 @@ __device__ __forceinline__ float quad2(const float* c, float a, float b) {
   return fmaf(a, fmaf(c[3], a, fmaf(c[4], b, c[1])), fmaf(b, fmaf(c[5], b, c[2]), c[0]));
 }
 
+// ---- fixed-point phase fields of the FP32 form: phi = q 2^-29 ----
+// Resolution 1.9e-9 everywhere on [-1.99, 1.99] (FP32 has 6e-8 near
+// phi = 1), so Allen-Cahn increments far below FP32's half-ulp still move
+// the field; q is saturated so that the difference of two values fits int32.
+constexpr float kPhiScale = 536870912.0f;  // 2^29
+constexpr float kPhiInvScale = 1.0f / 536870912.0f;
+constexpr double kPhiInvScaleD = 1.0 / 536870912.0;
+constexpr int kPhiQMax = 1068373114;  // floor(1.99 * 2^29)
+
+__device__ __forceinline__ float phi_of(int q) { return float(q) * kPhiInvScale; }
+
+__device__ __forceinline__ int phi_sat(long long q) {
+  return int(q > kPhiQMax ? kPhiQMax : (q < -kPhiQMax ? -kPhiQMax : q));
+}
+
+// q + round(inc 2^29), saturated (the increment is clamped first so its
+// integer form cannot overflow)
+__device__ __forceinline__ int phi_add(int q, float inc) {
+  const float c = fminf(fmaxf(inc, -3.9f), 3.9f);
+  return phi_sat((long long)q + __float2int_rn(c * kPhiScale));
+}
+
+__device__ __forceinline__ int phi_quantize(double v) {
+  const double c = fmin(fmax(v, -1.99), 1.99);
+  return phi_sat(__double2ll_rn(c * 536870912.0));
+}
+
 // 1 - p(x) = p(1 - x): the gamma fraction without cancellation near a pure
 // precipitate (1 - phi is exact in FP32 for phi >= 1/2).
 __device__ __forceinline__ float p_gamma32(float phd, float phl, float pD, float pL) {

@@ -18,7 +18,8 @@ struct Step2DArgs {
   int Nx, Ny, pitch;    // interior size and row pitch (elements)
   int write_halo;       // also write the mirrored ghost ring
   int nine;             // 3x3 mask has non-zero corners
-  int kahan_phi;        // FP32 form: compensate the phase fields too
+  int kahan_phi;        // FP32 form: FP32 phases with Kahan compensation
+                        // (otherwise 32-bit fixed-point phases)
   ModelConst m;
   double mask9[9];      // full 3x3 mask, row-major (rows y-1..y+1)
   FastCoef k;
@@ -32,9 +33,10 @@ struct Step2DArgs {
 // Layout conversion between FP64 reference fields and FP32 form fields.
 struct ConvArgs {
   double* f64[4];
-  float* f32[4];
+  float* f32[4];   // phases hold int32 fixed point when phi_fix
   float* c32[4];
   int Nx, Ny, pitch64, pitch32;
+  int phi_fix;
 };
 
 // Arguments of the reference's per-stage kernels (compat mode).

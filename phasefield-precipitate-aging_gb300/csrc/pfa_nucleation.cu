@@ -57,6 +57,13 @@ __device__ __forceinline__ double ld(const void* p, size_t i) {
   return double(static_cast<const T*>(p)[i]);
 }
 
+// a phase field: FP64, FP32, or the FP32 form's fixed point
+template <class T>
+__device__ __forceinline__ double ldphi(const NucArgs& a, int k, size_t i) {
+  if (a.phi_fix) return double(static_cast<const int*>(a.f[k])[i]) * kPhiInvScaleD;
+  return ld<T>(a.f[k], i);
+}
+
 // Storage index of the reference linear index idn (row width nx = Nx + 2).
 __device__ __forceinline__ size_t sidx(long long idn, int nxr, int pitch) {
   return size_t(idn / nxr) * pitch + size_t(idn % nxr);
@@ -98,41 +105,53 @@ __device__ void probability_sphere(double xCr, double xNb, double dG, double dcc
   Rstar = (2. * sigma) / dG;
 }
 
-// True when no event is possible for either phase (see file comment).
-__device__ bool surely_no_event(float X, float Y, const NucArgs& a) {
+// Upper bound, in FP32, of ln z with z = dt dV (J_Cr + J_Nb) for each phase;
+// +inf where no bound is attempted (compositions outside the simplex, or
+// above the gamma equilibrium composition, where the exponents change sign).
+// The diffusivities are bounded by the magnitudes of their three mobility
+// terms, so the bound holds whatever the signs of D_CrCr and D_NbNb.
+__device__ void ln_z_bound(float X, float Y, const NucArgs& a, float lnz[2]) {
+  lnz[0] = lnz[1] = INFINITY;
   const float dcCr = float(kXe[0][0]) - X, dcNb = Y - float(kXe[0][1]);
-  if (!(dcCr > 0.0f && dcNb > 0.0f && X > 0.0f && Y > 0.0f && X + Y < 1.0f)) return false;
-  // g_gam in FP32
+  if (!(dcCr > 0.0f && dcNb > 0.0f && X > 0.0f && Y > 0.0f && X + Y < 1.0f)) return;
   const float u = X - float(kXe[0][0]), v = Y - float(kXe[0][1]);
   const float dG = float(kG[0][0]) * u * u + (float(kG[0][1]) * X - float(kG[0][2])) * v +
                    float(kG[0][3]) * v * v;
-  if (!(dG > 0.0f)) return false;
-  // |D| bound: the three mobility terms of D are each bounded by
-  // pre * exp(e) * (|s| + add) (times compositions <= 1)
+  if (!(dG > 1.0f)) return;
   const float xni = 1.0f - X - Y;
   const float eNb = -34.982563536715503f * Y * xni + 14.437947842988088f * Y;
   const float eCr = -7.1543718172640256f * X * xni + 3.3541967644499233f * X;
   const float eNi = -8.5221193705645018f * X * xni + 4.0036674816806448f * X -
                     442.62877981749585f * Y * xni - 0.82164267100913768f * Y;
-  const float emax = fmaxf(eNb, fmaxf(eCr, eNi));
-  const float lnDmax = logf(3.0f * 1.5e-20f * 2.5e6f) + emax;  // 3 terms, pre <= 1.5e-20, |s|+add <= 2.5e6
-  float lnz = -INFINITY;
+  // |D| <= 3 terms x prefactor (<= 1.5e-20) x exp(e) x (|s| + add <= 2.5e6)
+  const float lnDmax = -35.33f + fmaxf(eNb, fmaxf(eCr, eNi));  // ln(3 * 1.5e-20 * 2.5e6) = -36.04
+  const float a4 = float(kLatticeConst * kLatticeConst * kLatticeConst * kLatticeConst);
 #pragma unroll
   for (int ph = 0; ph < 2; ph++) {
     const float sigma = float(a.sigma[ph]);
     const float s3 = sigma * sigma * sigma;
-    // ln(k1) <= ln(3 G* Dmax x / (sigma a^4) * Zeldov * n_gam), x <= 1
     const float Gstar = (16.0f * float(kPi) * s3) / (3.0f * dG * dG);
     const float Z = float(a.Vatom) * dG * dG / (8.0f * float(kPi) * sqrtf(float(kKT) * s3));
-    const float a4 = float(kLatticeConst * kLatticeConst * kLatticeConst * kLatticeConst);
+    // ln k1 <= ln(3 G* Dmax / (sigma a^4)) + ln Zeldovich + ln n_gam  (x <= 1)
     const float lnk1 = logf(3.0f * Gstar / (sigma * a4)) + lnDmax + logf(Z) + float(a.ln_ngam);
     const float k2 = Gstar / float(kKT);
-    // max(J_Cr, J_Nb) <= k1_max exp(-min(k2 / dc_Cr, k2 / dc_Nb))
-    const float lnJ = lnk1 - fminf(k2 / dcCr, k2 / dcNb);
-    lnz = fmaxf(lnz, lnJ + 0.6931472f);  // J_Cr + J_Nb <= 2 max
+    // J_Cr + J_Nb <= 2 k1_max exp(-min(k2 / dc_Cr, k2 / dc_Nb))
+    const float l = lnk1 - fminf(k2 / dcCr, k2 / dcNb) + 0.6931472f + float(a.ln_dtdV);
+    if (l == l) lnz[ph] = l;  // NaN stays +inf
   }
-  lnz += float(a.ln_dtdV);
-  return isfinite(lnz) ? (lnz < -39.1439f - 12.0f) : false;  // ln(1e-17) - 12
+}
+
+// p(phi_del) + p(phi_lav) < 1e-10 as the reference's FP64 test decides it:
+// in FP32 when the FP32 sum is farther from the threshold than its error
+// bound (1e-6 of |p_del| + |p_lav|; p < 0 for phi < 0 allows cancellation),
+// in FP64 otherwise.
+__device__ __forceinline__ bool clear_of_precipitate(double phd, double phl) {
+  const float a = p32(float(phd)), b = p32(float(phl));
+  const float q = a + b, err = 1e-6f * (fabsf(a) + fabsf(b)) + 1e-20f;
+  if (q - err > 1e-10f) return false;
+  if (q + err < 1e-10f) return true;
+  // the reference takes max(phi_pre, sum), which skips a NaN sum
+  return !(p64(phd) + p64(phl) >= 1e-10);
 }
 
 template <class T>
@@ -145,27 +164,47 @@ __global__ void __launch_bounds__(256) k_nuc_decide(NucArgs a) {
   if (gx < a.Nx && gy < a.Ny) {
     const int x = gx + 1, y = gy + 1;
     const long long idx = (long long)nxr * y + x;
-    const long long ntot = (long long)nxr * nyr;
     const double R = a.R_scan;
-    double phi_pre = 0.0;
-    for (int i = int(-R); i < R; i++)
-      for (int j = int(-R); j < R; j++) {
-        const long long idn = (long long)nxr * (y + j) + (x + i);
-        if (idn >= 0 && idn < ntot && double(i * i + j * j) < R * R) {
-          const size_t s = sidx(idn, nxr, a.pitch);
-          phi_pre = fmax(phi_pre, p64(ld<T>(a.f[2], s)) + p64(ld<T>(a.f[3], s)));
+    bool clear = true;
+    // neighbourhood scan of src/discretization.cu:1104-1117; the reference
+    // bounds-checks the linear index nx (y + j) + (x + i), so offsets past a
+    // row end wrap onto the next row -- reproduced by normalising (xx, yy)
+    for (int i = int(-R); i < R && clear; i++)
+      for (int j = int(-R); j < R && clear; j++) {
+        if (!(double(i * i + j * j) < R * R)) continue;
+        int xx = x + i, yy = y + j;
+        while (xx < 0) {
+          xx += nxr;
+          yy--;
         }
+        while (xx >= nxr) {
+          xx -= nxr;
+          yy++;
+        }
+        if (yy < 0 || yy >= nyr) continue;
+        const size_t s = size_t(yy) * a.pitch + xx;
+        clear = clear_of_precipitate(ldphi<T>(a, 2, s), ldphi<T>(a, 3, s));
       }
-    if (phi_pre < 1e-10) {
-      const size_t s = sidx(idx, nxr, a.pitch);
+    if (clear) {
+      const size_t s = size_t(y) * a.pitch + x;
       const double X = ld<T>(a.f[0], s), Y = ld<T>(a.f[1], s);
-      if (!surely_no_event(float(X), float(Y), a)) {
-        const unsigned long long call = *a.call_ptr;
-        const uint4 w = philox4x32_10(
-            make_uint4(uint32_t(idx), uint32_t(uint64_t(idx) >> 32), uint32_t(call),
-                       uint32_t(call >> 32)),
-            make_uint2(uint32_t(a.seed), uint32_t(a.seed >> 32)));
-        const double u[2] = {u53(w.x, w.y), u53(w.z, w.w)};
+      const unsigned long long call = *a.call_ptr;
+      const uint4 w = philox4x32_10(
+          make_uint4(uint32_t(idx), uint32_t(uint64_t(idx) >> 32), uint32_t(call),
+                     uint32_t(call >> 32)),
+          make_uint2(uint32_t(a.seed), uint32_t(a.seed >> 32)));
+      const double u[2] = {u53(w.x, w.y), u53(w.z, w.w)};
+      // P_FP64 = 1 - exp(-z) <= max(z, 0) (1 + 1e-15) + 2^-53, so a draw
+      // u >= 2 exp(ln z_up + 12) + 2^-52 cannot produce an event
+      float lnz[2];
+      ln_z_bound(float(X), float(Y), a, lnz);
+      bool need = false;
+#pragma unroll
+      for (int ph = 0; ph < 2; ph++) {
+        const double pup = double(2.0f * __expf(fminf(lnz[ph] + 12.0f, 88.0f))) + 0x1p-52;
+        if (!(lnz[ph] + 12.0f < 88.0f) || u[ph] < pup) need = true;
+      }
+      if (need) {
         const double dG = g64<0>(X, Y);
         double dcc, dnn;
         diffusivities(X, Y, dcc, dnn);
@@ -249,7 +288,10 @@ __device__ void paint(const NucArgs& a, const NucEvent& e, int ph) {
     if (r <= R) {
       put<T>(a.f[0], ccr, s, parCr);
       put<T>(a.f[1], cnb, s, parNb);
-      put<T>(phi, cphi, s, 1.0);
+      if (a.phi_fix)
+        static_cast<int*>(phi)[s] = phi_quantize(1.0);
+      else
+        put<T>(phi, cphi, s, 1.0);
     } else {
       if (r <= RdCr) put<T>(a.f[0], ccr, s, xgCr);
       if (r <= RdNb) put<T>(a.f[1], cnb, s, xgNb);

@@ -24,6 +24,7 @@ struct NucArgs {
   void* f[4];          // x_Cr, x_Nb, phi_del, phi_lav (halo layout, row pitch `pitch`)
   float* comp[4];      // FP32 form: compensation arrays (reset where painted), or nullptr
   int is_f32;
+  int phi_fix;         // phases in 32-bit fixed point (FP32 form)
   int Nx, Ny, pitch;
   double sigma[2];
   double dx;           // kernel spacing (the reference passes dx * nx here)

@@ -39,12 +39,18 @@ __global__ void __launch_bounds__(kThreads) k_sum_partial(SumArgs a) {
     const size_t i = (size_t(a.is3d ? z + 1 : 0) * (a.Ny + 2) + (y + 1)) * a.pitch + (x + 1);
     const T* f0 = static_cast<const T*>(a.f[0]);
     const T* f1 = static_cast<const T*>(a.f[1]);
-    const T* f2 = static_cast<const T*>(a.f[2]);
-    const T* f3 = static_cast<const T*>(a.f[3]);
     double xcr = double(f0[i]), xnb = double(f1[i]);
     if (a.c[0]) xcr -= double(a.c[0][i]);
     if (a.c[1]) xnb -= double(a.c[1][i]);
-    const double pd = p64(double(f2[i])), pl = p64(double(f3[i]));
+    double phd, phl;
+    if (a.phi_fix) {
+      phd = double(static_cast<const int*>(a.f[2])[i]) * kPhiInvScaleD;
+      phl = double(static_cast<const int*>(a.f[3])[i]) * kPhiInvScaleD;
+    } else {
+      phd = double(static_cast<const T*>(a.f[2])[i]);
+      phl = double(static_cast<const T*>(a.f[3])[i]);
+    }
+    const double pd = p64(phd), pl = p64(phl);
     acc.add(0, xcr);
     acc.add(1, xnb);
     acc.add(2, (1.0 - pd) - pl);

@@ -169,13 +169,16 @@ __global__ void __launch_bounds__(kTX* kBY) k_step2d_f64(Step2DArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// FP32 precision form.  Fields FP32; x_Cr, x_Nb carry Kahan compensation
-// arrays (and phi too when KPHI); Laplacians in difference form; the delta
-// and laves grand-potential differences as quadratics in x^gamma - xe.
-template <bool KPHI>
+// FP32 precision form.  Arithmetic in FP32; x_Cr, x_Nb stored FP32 with Kahan
+// compensation arrays; the phases stored either as 32-bit fixed point
+// (FIX: phi = q 2^-29, integer accumulation) or as FP32 with Kahan
+// compensation (!FIX).  Laplacians in difference form; the delta and laves
+// grand-potential differences as quadratics in x^gamma - xe.
+template <bool FIX>
 __global__ void __launch_bounds__(kTX* kBY) k_step2d_f32(Step2DArgs a) {
   __shared__ float s_phd[kEY][kEX], s_phl[kEY][kEX], s_gcr[kEY][kEX], s_gnb[kEY][kEX];
   __shared__ float s_x[kEY][kEX], s_y[kEY][kEX];
+  __shared__ int s_qd[FIX ? kEY : 1][kEX], s_ql[FIX ? kEY : 1][kEX];
   const float* __restrict__ icr = static_cast<const float*>(a.in[0]);
   const float* __restrict__ inb = static_cast<const float*>(a.in[1]);
   const float* __restrict__ ipd = static_cast<const float*>(a.in[2]);
@@ -189,7 +192,19 @@ __global__ void __launch_bounds__(kTX* kBY) k_step2d_f32(Step2DArgs a) {
     const int gx = clampi(x0 + ex - 1, 0, a.Nx - 1);
     const int gy = clampi(y0 + ey - 1, 0, a.Ny - 1);
     const size_t i = size_t(gy + 1) * a.pitch + gx + 1;
-    const float X = icr[i], Y = inb[i], phd = ipd[i], phl = ipl[i];
+    const float X = icr[i], Y = inb[i];
+    float phd, phl;
+    if (FIX) {
+      const int qd = reinterpret_cast<const int*>(ipd)[i];
+      const int ql = reinterpret_cast<const int*>(ipl)[i];
+      s_qd[ey][ex] = qd;
+      s_ql[ey][ex] = ql;
+      phd = phi_of(qd);
+      phl = phi_of(ql);
+    } else {
+      phd = ipd[i];
+      phl = ipl[i];
+    }
     const float pD = p32(phd), pL = p32(phl);
     float gcr, gnb;
     fict_gam32(K, X, Y, pD, p_gamma32(phd, phl, pD, pL), pL, gcr, gnb);
@@ -213,7 +228,17 @@ __global__ void __launch_bounds__(kTX* kBY) k_step2d_f32(Step2DArgs a) {
       const float sy = (s[ey - 1][ex] - c) + (s[ey + 1][ex] - c);
       return fmaf(sx, idx2, sy * idy2);
     };
-    const float lapCr = lap(s_gcr), lapNb = lap(s_gnb), lapD = lap(s_phd), lapL = lap(s_phl);
+    // fixed-point phases: exact integer differences (|q| < 2^30.99, so a
+    // difference of two stays inside int32)
+    auto lapq = [&](int (*s)[kEX]) {
+      const int c = s[ey][ex];
+      const float sx = float(s[ey][ex - 1] - c) + float(s[ey][ex + 1] - c);
+      const float sy = float(s[ey - 1][ex] - c) + float(s[ey + 1][ex] - c);
+      return fmaf(sx, idx2, sy * idy2) * kPhiInvScale;
+    };
+    const float lapCr = lap(s_gcr), lapNb = lap(s_gnb);
+    const float lapD = FIX ? lapq(s_qd) : lap(s_phd);
+    const float lapL = FIX ? lapq(s_ql) : lap(s_phl);
     const size_t i = size_t(gy + 1) * a.pitch + gx + 1;
     const float X = s_x[ey][ex], Y = s_y[ey][ex];
     const float phd = s_phd[ey][ex], phl = s_phl[ey][ex];
@@ -242,30 +267,26 @@ __global__ void __launch_bounds__(kTX* kBY) k_step2d_f32(Step2DArgs a) {
                       a.alpha2 * phd * phl * phl - a.kap[0] * lapD;
     const float dFl = -pp32(phl) * dPl + a.om2[1] * phl * (phl - 1.0f) * (2.0f * phl - 1.0f) +
                       a.alpha2 * phl * phd * phd - a.kap[1] * lapL;
-    float od, ol, cd = 0.f, cl = 0.f;
-    if (KPHI) {
-      const float yd = -a.dtL[0] * dFd - a.cin[2][i];
-      const float td = phd + yd;
-      cd = (td - phd) - yd;
-      od = td;
-      const float yl = -a.dtL[1] * dFl - a.cin[3][i];
-      const float tl = phl + yl;
-      cl = (tl - phl) - yl;
-      ol = tl;
-    } else {
-      od = fmaf(-a.dtL[0], dFd, phd);
-      ol = fmaf(-a.dtL[1], dFl, phl);
-    }
     float* const* o = reinterpret_cast<float* const*>(a.out);
     o[0][i] = ocr;
     o[1][i] = onb;
-    o[2][i] = od;
-    o[3][i] = ol;
     a.cout[0][i] = ccr;
     a.cout[1][i] = cnb;
-    if (KPHI) {
-      a.cout[2][i] = cd;
-      a.cout[3][i] = cl;
+    if (FIX) {
+      // integer accumulation of the FP32 increment: no increment is lost
+      // below FP32's half-ulp of phi
+      reinterpret_cast<int*>(o[2])[i] = phi_add(s_qd[ey][ex], -a.dtL[0] * dFd);
+      reinterpret_cast<int*>(o[3])[i] = phi_add(s_ql[ey][ex], -a.dtL[1] * dFl);
+    } else {
+      // Kahan-compensated phases
+      const float yd = -a.dtL[0] * dFd - a.cin[2][i];
+      const float td = phd + yd;
+      a.cout[2][i] = (td - phd) - yd;
+      o[2][i] = td;
+      const float yl = -a.dtL[1] * dFl - a.cin[3][i];
+      const float tl = phl + yl;
+      a.cout[3][i] = (tl - phl) - yl;
+      o[3][i] = tl;
     }
   }
 }
@@ -281,6 +302,10 @@ __global__ void k_import_f32(ConvArgs a) {
 #pragma unroll
   for (int k = 0; k < 4; k++) {
     const double v = a.f64[k][i64];
+    if (k >= 2 && a.phi_fix) {
+      reinterpret_cast<int*>(a.f32[k])[i32] = phi_quantize(v);
+      continue;
+    }
     const float hi = float(v);
     a.f32[k][i32] = hi;
     // compensation c holds -(low part) so that value = hi - c
@@ -295,8 +320,13 @@ __global__ void k_export_f32(ConvArgs a) {
   const size_t i32 = size_t(gy + 1) * a.pitch32 + gx + 1;
 #pragma unroll
   for (int k = 0; k < 4; k++) {
-    double v = double(a.f32[k][i32]);
-    if (a.c32[k]) v -= double(a.c32[k][i32]);
+    double v;
+    if (k >= 2 && a.phi_fix) {
+      v = double(reinterpret_cast<const int*>(a.f32[k])[i32]) * kPhiInvScaleD;
+    } else {
+      v = double(a.f32[k][i32]);
+      if (a.c32[k]) v -= double(a.c32[k][i32]);
+    }
     store_with_halo(a.f64[k], a.pitch64, gx, gy, a.Nx, a.Ny, v, true);
   }
 }
@@ -318,9 +348,9 @@ cudaError_t launch_step2d_f32(const Step2DArgs& a, cudaStream_t s) {
   dim3 grid((a.Nx + kTX - 1) / kTX, (a.Ny + kTY - 1) / kTY);
   dim3 block(kTX, kBY);
   if (a.kahan_phi)
-    k_step2d_f32<true><<<grid, block, 0, s>>>(a);
-  else
     k_step2d_f32<false><<<grid, block, 0, s>>>(a);
+  else
+    k_step2d_f32<true><<<grid, block, 0, s>>>(a);
   return cudaGetLastError();
 }
 

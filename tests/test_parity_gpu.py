@@ -177,7 +177,7 @@ def test_dataviz(pfa, orc):
     cr, nb, ni, pd, pl, phi = grid.dataviz()
     np.testing.assert_array_equal(ni, 1.0 - cr - nb)
     np.testing.assert_allclose(phi, orc.p(pd).reshape(pd.shape) + orc.p(pl).reshape(pl.shape),
-                               rtol=0, atol=1e-15)
+                               rtol=1e-14, atol=1e-16)
     grid.close()
 
 
