@@ -134,10 +134,12 @@ static int ensure_fict(CudaData* dev, State* s) {
   return 0;
 }
 
+// FP32 form buffers, compact layout: Ny rows of pitch32 (a multiple of 32
+// elements), interior only; every array starts on a 256-byte boundary.
 static int ensure_f32(State* s) {
   if (s->f32mem) return 0;
-  s->pitch32 = ((s->nx + 31) / 32) * 32;
-  const size_t per = size_t(s->pitch32) * s->ny;
+  s->pitch32 = ((s->Nx + 31) / 32) * 32;
+  const size_t per = ((size_t(s->pitch32) * s->Ny + 63) / 64) * 64;
   CK(cudaMalloc(reinterpret_cast<void**>(&s->f32mem), per * 16 * sizeof(float)));
   CK(cudaMemsetAsync(s->f32mem, 0, per * 16 * sizeof(float), s->st));
   for (int b = 0; b < 2; b++)
@@ -202,6 +204,8 @@ static Step2DArgs step_args(State* s, double alpha, double dt) {
     a.kap[i] = float(s->m.kappa[i]);
   }
   a.alpha2 = float(2.0 * alpha);
+  a.idx2f[0] = float(s->m.idx2[0]);
+  a.idx2f[1] = float(s->m.idx2[1]);
   return a;
 }
 
@@ -258,6 +262,7 @@ static int nucleate(CudaData* dev, State* s, double sig_d, double sig_l, double 
     }
     a.pitch = s->pitch32;
     a.is_f32 = 1;
+    a.compact = 1;
     a.phi_fix = s->precision == PFA_FP32;
   }
   a.Nx = s->Nx;
@@ -998,6 +1003,7 @@ int pfa_summarize(struct CudaData* dev, double* out) {
     a.c[0] = s->c32[s->cur][0];
     a.c[1] = s->c32[s->cur][1];
     a.is_f32 = 1;
+    a.compact = 1;
     a.phi_fix = s->precision == PFA_FP32;
     a.pitch = s->pitch32;
   } else {

@@ -28,9 +28,11 @@ struct Step2DArgs {
   float om2[2];         // 2 omega
   float alpha2;         // 2 alpha
   float kap[2];         // kappa
+  float idx2f[2];       // 1/dx^2, 1/dy^2
 };
 
-// Layout conversion between FP64 reference fields and FP32 form fields.
+// Layout conversion between FP64 reference fields (ghost ring, pitch64) and
+// the FP32 form's compact fields (interior only, rows of pitch32).
 struct ConvArgs {
   double* f64[4];
   float* f32[4];   // phases hold int32 fixed point when phi_fix

@@ -57,16 +57,28 @@ __device__ __forceinline__ double ld(const void* p, size_t i) {
   return double(static_cast<const T*>(p)[i]);
 }
 
-// a phase field: FP64, FP32, or the FP32 form's fixed point
+// Storage index of reference cell (xx, yy) (ghost-ring coordinates).  The
+// FP32 form stores the interior only: a ghost cell reads its mirror.
+__device__ __forceinline__ size_t stor(const NucArgs& a, int xx, int yy) {
+  if (a.compact) {
+    const int cx = min(max(xx - 1, 0), a.Nx - 1), cy = min(max(yy - 1, 0), a.Ny - 1);
+    return size_t(cy) * a.pitch + cx;
+  }
+  return size_t(yy) * a.pitch + xx;
+}
+
+// a phase field as stored (FP64, FP32 or the FP32 form's fixed point), exact
 template <class T>
 __device__ __forceinline__ double ldphi(const NucArgs& a, int k, size_t i) {
   if (a.phi_fix) return double(static_cast<const int*>(a.f[k])[i]) * kPhiInvScaleD;
   return ld<T>(a.f[k], i);
 }
 
-// Storage index of the reference linear index idn (row width nx = Nx + 2).
-__device__ __forceinline__ size_t sidx(long long idn, int nxr, int pitch) {
-  return size_t(idn / nxr) * pitch + size_t(idn % nxr);
+// the same, rounded to FP32 without touching the FP64 pipe in the FP32 form
+template <class T>
+__device__ __forceinline__ float ldphi_f(const NucArgs& a, int k, size_t i) {
+  if (a.phi_fix) return phi_of(static_cast<const int*>(a.f[k])[i]);
+  return float(static_cast<const T*>(a.f[k])[i]);
 }
 
 // composition-dependent diffusivities D_CrCr, D_NbNb (thermo/parabola625.c:1860-1894)
@@ -144,14 +156,15 @@ __device__ void ln_z_bound(float X, float Y, const NucArgs& a, float lnz[2]) {
 // p(phi_del) + p(phi_lav) < 1e-10 as the reference's FP64 test decides it:
 // in FP32 when the FP32 sum is farther from the threshold than its error
 // bound (1e-6 of |p_del| + |p_lav|; p < 0 for phi < 0 allows cancellation),
-// in FP64 otherwise.
-__device__ __forceinline__ bool clear_of_precipitate(double phd, double phl) {
-  const float a = p32(float(phd)), b = p32(float(phl));
-  const float q = a + b, err = 1e-6f * (fabsf(a) + fabsf(b)) + 1e-20f;
+// in FP64 from the exact stored values otherwise.
+template <class T>
+__device__ __forceinline__ bool clear_at(const NucArgs& a, size_t s) {
+  const float fa = p32(ldphi_f<T>(a, 2, s)), fb = p32(ldphi_f<T>(a, 3, s));
+  const float q = fa + fb, err = 1e-6f * (fabsf(fa) + fabsf(fb)) + 1e-20f;
   if (q - err > 1e-10f) return false;
   if (q + err < 1e-10f) return true;
   // the reference takes max(phi_pre, sum), which skips a NaN sum
-  return !(p64(phd) + p64(phl) >= 1e-10);
+  return !(p64(ldphi<T>(a, 2, s)) + p64(ldphi<T>(a, 3, s)) >= 1e-10);
 }
 
 template <class T>
@@ -182,29 +195,32 @@ __global__ void __launch_bounds__(256) k_nuc_decide(NucArgs a) {
           yy++;
         }
         if (yy < 0 || yy >= nyr) continue;
-        const size_t s = size_t(yy) * a.pitch + xx;
-        clear = clear_of_precipitate(ldphi<T>(a, 2, s), ldphi<T>(a, 3, s));
+        clear = clear_at<T>(a, stor(a, xx, yy));
       }
     if (clear) {
-      const size_t s = size_t(y) * a.pitch + x;
-      const double X = ld<T>(a.f[0], s), Y = ld<T>(a.f[1], s);
+      const size_t s = stor(a, x, y);
+      const T Xs = static_cast<const T*>(a.f[0])[s], Ys = static_cast<const T*>(a.f[1])[s];
       const unsigned long long call = *a.call_ptr;
       const uint4 w = philox4x32_10(
           make_uint4(uint32_t(idx), uint32_t(uint64_t(idx) >> 32), uint32_t(call),
                      uint32_t(call >> 32)),
           make_uint2(uint32_t(a.seed), uint32_t(a.seed >> 32)));
-      const double u[2] = {u53(w.x, w.y), u53(w.z, w.w)};
-      // P_FP64 = 1 - exp(-z) <= max(z, 0) (1 + 1e-15) + 2^-53, so a draw
-      // u >= 2 exp(ln z_up + 12) + 2^-52 cannot produce an event
+      // Screen in FP32: u >= hi32 2^-32 (rounded toward zero), and the FP64
+      // P_nuc = 1 - exp(-z) <= max(z, 0) (1 + 1e-15) + 2^-53 <= P_up, so a cell
+      // with u_lower >= P_up cannot nucleate.
       float lnz[2];
-      ln_z_bound(float(X), float(Y), a, lnz);
+      ln_z_bound(float(Xs), float(Ys), a, lnz);
+      const float ulo[2] = {__uint2float_rz(w.x) * 0x1p-32f, __uint2float_rz(w.z) * 0x1p-32f};
       bool need = false;
 #pragma unroll
       for (int ph = 0; ph < 2; ph++) {
-        const double pup = double(2.0f * __expf(fminf(lnz[ph] + 12.0f, 88.0f))) + 0x1p-52;
-        if (!(lnz[ph] + 12.0f < 88.0f) || u[ph] < pup) need = true;
+        const bool bounded = lnz[ph] + 12.0f < 80.0f;
+        const float pup = 2.0f * __expf(fminf(lnz[ph] + 12.0f, 80.0f)) + 0x1p-52f;
+        if (!bounded || !(ulo[ph] >= pup)) need = true;
       }
       if (need) {
+        const double X = double(Xs), Y = double(Ys);
+        const double u[2] = {u53(w.x, w.y), u53(w.z, w.w)};
         const double dG = g64<0>(X, Y);
         double dcc, dnn;
         diffusivities(X, Y, dcc, dnn);
@@ -283,7 +299,10 @@ __device__ void paint(const NucArgs& a, const NucEvent& e, int ph) {
     const int i = lo + int(t / w), j = lo + int(t % w);
     const long long idn = (long long)nxr * (y + j) + (x + i);
     if (idn < 0 || idn >= ntot) continue;
-    const size_t s = sidx(idn, nxr, a.pitch);
+    const int yy = int(idn / nxr), xx = int(idn % nxr);
+    // the FP32 form keeps no ghost ring: a nucleus never paints one there
+    if (a.compact && (xx == 0 || yy == 0 || xx == nxr - 1 || yy == a.Ny + 1)) continue;
+    const size_t s = stor(a, xx, yy);
     const double r = sqrt(double(i * i + j * j));
     if (r <= R) {
       put<T>(a.f[0], ccr, s, parCr);

@@ -25,6 +25,8 @@ struct NucArgs {
   float* comp[4];      // FP32 form: compensation arrays (reset where painted), or nullptr
   int is_f32;
   int phi_fix;         // phases in 32-bit fixed point (FP32 form)
+  int compact;         // FP32 form layout: interior rows only (ghost cells read
+                       // as their mirrored interior cell, never painted)
   int Nx, Ny, pitch;
   double sigma[2];
   double dx;           // kernel spacing (the reference passes dx * nx here)

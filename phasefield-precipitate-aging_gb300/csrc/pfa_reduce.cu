@@ -36,7 +36,9 @@ __global__ void __launch_bounds__(kThreads) k_sum_partial(SumArgs a) {
        t += (long long)gridDim.x * kThreads) {
     const long long z = t / plane, r = t % plane;
     const int y = int(r / a.Nx), x = int(r % a.Nx);
-    const size_t i = (size_t(a.is3d ? z + 1 : 0) * (a.Ny + 2) + (y + 1)) * a.pitch + (x + 1);
+    const size_t i = a.compact
+                         ? (size_t(z) * a.Ny + y) * a.pitch + x
+                         : (size_t(a.is3d ? z + 1 : 0) * (a.Ny + 2) + (y + 1)) * a.pitch + (x + 1);
     const T* f0 = static_cast<const T*>(a.f[0]);
     const T* f1 = static_cast<const T*>(a.f[1]);
     double xcr = double(f0[i]), xnb = double(f1[i]);

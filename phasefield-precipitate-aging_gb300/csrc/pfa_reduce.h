@@ -12,6 +12,7 @@ struct SumArgs {
   const float* c[2];  // FP32 form: compensation of x_Cr, x_Nb (value = f - c), or nullptr
   int is_f32, is3d;
   int phi_fix;        // phases in the FP32 form's 32-bit fixed point
+  int compact;        // interior-only rows (FP32 form) instead of the ghost-ring layout
   int Nx, Ny, Nz, pitch;
   double* partial;    // scratch: kSumBlocks * 5 doubles
   double* out;        // 5 doubles (device)

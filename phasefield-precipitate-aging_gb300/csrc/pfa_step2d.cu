@@ -9,10 +9,9 @@
 // updates for its interior cells.  Domain edges are handled by clamped
 // (mirrored) indexing, which is what the reference's halo fill produces.
 //
-// Layouts.  FP64 fields use the reference's layout: (Ny + 2) rows of pitch
-// elements, a one-cell ghost ring, interior cell (x, y) at (y + 1) * pitch +
-// x + 1.  The FP32 precision form keeps its own buffers in the same
-// convention with the pitch padded to 32 elements (128-byte rows).
+// Layout: the reference's, (Ny + 2) rows of pitch elements with a one-cell
+// ghost ring, interior cell (x, y) at (y + 1) * pitch + x + 1.  The FP32
+// precision form has its own kernel and layout (pfa_step2d_f32.cu).
 #include <cstdint>
 
 #include "pfa_device.cuh"
@@ -168,169 +167,6 @@ __global__ void __launch_bounds__(kTX* kBY) k_step2d_f64(Step2DArgs a) {
   }
 }
 
-// ---------------------------------------------------------------------------
-// FP32 precision form.  Arithmetic in FP32; x_Cr, x_Nb stored FP32 with Kahan
-// compensation arrays; the phases stored either as 32-bit fixed point
-// (FIX: phi = q 2^-29, integer accumulation) or as FP32 with Kahan
-// compensation (!FIX).  Laplacians in difference form; the delta and laves
-// grand-potential differences as quadratics in x^gamma - xe.
-template <bool FIX>
-__global__ void __launch_bounds__(kTX* kBY) k_step2d_f32(Step2DArgs a) {
-  __shared__ float s_phd[kEY][kEX], s_phl[kEY][kEX], s_gcr[kEY][kEX], s_gnb[kEY][kEX];
-  __shared__ float s_x[kEY][kEX], s_y[kEY][kEX];
-  __shared__ int s_qd[FIX ? kEY : 1][kEX], s_ql[FIX ? kEY : 1][kEX];
-  const float* __restrict__ icr = static_cast<const float*>(a.in[0]);
-  const float* __restrict__ inb = static_cast<const float*>(a.in[1]);
-  const float* __restrict__ ipd = static_cast<const float*>(a.in[2]);
-  const float* __restrict__ ipl = static_cast<const float*>(a.in[3]);
-  const FastCoef& K = a.k;
-  const int x0 = blockIdx.x * kTX, y0 = blockIdx.y * kTY;
-  const int tid = threadIdx.y * kTX + threadIdx.x;
-
-  for (int e = tid; e < kEX * kEY; e += kTX * kBY) {
-    const int ex = e % kEX, ey = e / kEX;
-    const int gx = clampi(x0 + ex - 1, 0, a.Nx - 1);
-    const int gy = clampi(y0 + ey - 1, 0, a.Ny - 1);
-    const size_t i = size_t(gy + 1) * a.pitch + gx + 1;
-    const float X = icr[i], Y = inb[i];
-    float phd, phl;
-    if (FIX) {
-      const int qd = reinterpret_cast<const int*>(ipd)[i];
-      const int ql = reinterpret_cast<const int*>(ipl)[i];
-      s_qd[ey][ex] = qd;
-      s_ql[ey][ex] = ql;
-      phd = phi_of(qd);
-      phl = phi_of(ql);
-    } else {
-      phd = ipd[i];
-      phl = ipl[i];
-    }
-    const float pD = p32(phd), pL = p32(phl);
-    float gcr, gnb;
-    fict_gam32(K, X, Y, pD, p_gamma32(phd, phl, pD, pL), pL, gcr, gnb);
-    s_phd[ey][ex] = phd;
-    s_phl[ey][ex] = phl;
-    s_gcr[ey][ex] = gcr;
-    s_gnb[ey][ex] = gnb;
-    s_x[ey][ex] = X;
-    s_y[ey][ex] = Y;
-  }
-  __syncthreads();
-
-  const float idx2 = float(a.m.idx2[0]), idy2 = float(a.m.idx2[1]);
-  for (int r = threadIdx.y; r < kTY; r += kBY) {
-    const int gx = x0 + threadIdx.x, gy = y0 + r;
-    if (gx >= a.Nx || gy >= a.Ny) continue;
-    const int ex = threadIdx.x + 1, ey = r + 1;
-    auto lap = [&](float (*s)[kEX]) {
-      const float c = s[ey][ex];
-      const float sx = (s[ey][ex - 1] - c) + (s[ey][ex + 1] - c);
-      const float sy = (s[ey - 1][ex] - c) + (s[ey + 1][ex] - c);
-      return fmaf(sx, idx2, sy * idy2);
-    };
-    // fixed-point phases: exact integer differences (|q| < 2^30.99, so a
-    // difference of two stays inside int32)
-    auto lapq = [&](int (*s)[kEX]) {
-      const int c = s[ey][ex];
-      const float sx = float(s[ey][ex - 1] - c) + float(s[ey][ex + 1] - c);
-      const float sy = float(s[ey - 1][ex] - c) + float(s[ey + 1][ex] - c);
-      return fmaf(sx, idx2, sy * idy2) * kPhiInvScale;
-    };
-    const float lapCr = lap(s_gcr), lapNb = lap(s_gnb);
-    const float lapD = FIX ? lapq(s_qd) : lap(s_phd);
-    const float lapL = FIX ? lapq(s_ql) : lap(s_phl);
-    const size_t i = size_t(gy + 1) * a.pitch + gx + 1;
-    const float X = s_x[ey][ex], Y = s_y[ey][ex];
-    const float phd = s_phd[ey][ex], phl = s_phl[ey][ex];
-
-    // Cahn-Hilliard with Kahan-compensated accumulation
-    float ocr, onb, ccr, cnb;
-    {
-      const float inc = fmaf(a.dtD[0][0], lapCr, a.dtD[0][1] * lapNb);
-      const float y = inc - a.cin[0][i];
-      const float t = X + y;
-      ccr = (t - X) - y;
-      ocr = t;
-    }
-    {
-      const float inc = fmaf(a.dtD[1][0], lapCr, a.dtD[1][1] * lapNb);
-      const float y = inc - a.cin[1][i];
-      const float t = Y + y;
-      cnb = (t - Y) - y;
-      onb = t;
-    }
-
-    // Allen-Cahn
-    const float u1 = s_gcr[ey][ex] - K.xe_gam[0], u2 = s_gnb[ey][ex] - K.xe_gam[1];
-    const float dPd = quad2(K.dP[0], u1, u2), dPl = quad2(K.dP[1], u1, u2);
-    const float dFd = -pp32(phd) * dPd + a.om2[0] * phd * (phd - 1.0f) * (2.0f * phd - 1.0f) +
-                      a.alpha2 * phd * phl * phl - a.kap[0] * lapD;
-    const float dFl = -pp32(phl) * dPl + a.om2[1] * phl * (phl - 1.0f) * (2.0f * phl - 1.0f) +
-                      a.alpha2 * phl * phd * phd - a.kap[1] * lapL;
-    float* const* o = reinterpret_cast<float* const*>(a.out);
-    o[0][i] = ocr;
-    o[1][i] = onb;
-    a.cout[0][i] = ccr;
-    a.cout[1][i] = cnb;
-    if (FIX) {
-      // integer accumulation of the FP32 increment: no increment is lost
-      // below FP32's half-ulp of phi
-      reinterpret_cast<int*>(o[2])[i] = phi_add(s_qd[ey][ex], -a.dtL[0] * dFd);
-      reinterpret_cast<int*>(o[3])[i] = phi_add(s_ql[ey][ex], -a.dtL[1] * dFl);
-    } else {
-      // Kahan-compensated phases
-      const float yd = -a.dtL[0] * dFd - a.cin[2][i];
-      const float td = phd + yd;
-      a.cout[2][i] = (td - phd) - yd;
-      o[2][i] = td;
-      const float yl = -a.dtL[1] * dFl - a.cin[3][i];
-      const float tl = phl + yl;
-      a.cout[3][i] = (tl - phl) - yl;
-      o[3][i] = tl;
-    }
-  }
-}
-
-// ---------------------------------------------------------------------------
-// Layout conversion between the reference's FP64 fields and the FP32 form.
-__global__ void k_import_f32(ConvArgs a) {
-  const int gx = blockIdx.x * blockDim.x + threadIdx.x;
-  const int gy = blockIdx.y * blockDim.y + threadIdx.y;
-  if (gx >= a.Nx || gy >= a.Ny) return;
-  const size_t i64 = size_t(gy + 1) * a.pitch64 + gx + 1;
-  const size_t i32 = size_t(gy + 1) * a.pitch32 + gx + 1;
-#pragma unroll
-  for (int k = 0; k < 4; k++) {
-    const double v = a.f64[k][i64];
-    if (k >= 2 && a.phi_fix) {
-      reinterpret_cast<int*>(a.f32[k])[i32] = phi_quantize(v);
-      continue;
-    }
-    const float hi = float(v);
-    a.f32[k][i32] = hi;
-    // compensation c holds -(low part) so that value = hi - c
-    if (a.c32[k]) a.c32[k][i32] = float(double(hi) - v);
-  }
-}
-
-__global__ void k_export_f32(ConvArgs a) {
-  const int gx = blockIdx.x * blockDim.x + threadIdx.x;
-  const int gy = blockIdx.y * blockDim.y + threadIdx.y;
-  if (gx >= a.Nx || gy >= a.Ny) return;
-  const size_t i32 = size_t(gy + 1) * a.pitch32 + gx + 1;
-#pragma unroll
-  for (int k = 0; k < 4; k++) {
-    double v;
-    if (k >= 2 && a.phi_fix) {
-      v = double(reinterpret_cast<const int*>(a.f32[k])[i32]) * kPhiInvScaleD;
-    } else {
-      v = double(a.f32[k][i32]);
-      if (a.c32[k]) v -= double(a.c32[k][i32]);
-    }
-    store_with_halo(a.f64[k], a.pitch64, gx, gy, a.Nx, a.Ny, v, true);
-  }
-}
-
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -341,30 +177,6 @@ cudaError_t launch_step2d_f64(const Step2DArgs& a, cudaStream_t s) {
     k_step2d_f64<true><<<grid, block, 0, s>>>(a);
   else
     k_step2d_f64<false><<<grid, block, 0, s>>>(a);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_step2d_f32(const Step2DArgs& a, cudaStream_t s) {
-  dim3 grid((a.Nx + kTX - 1) / kTX, (a.Ny + kTY - 1) / kTY);
-  dim3 block(kTX, kBY);
-  if (a.kahan_phi)
-    k_step2d_f32<false><<<grid, block, 0, s>>>(a);
-  else
-    k_step2d_f32<true><<<grid, block, 0, s>>>(a);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_import_f32(const ConvArgs& a, cudaStream_t s) {
-  dim3 block(32, 8);
-  dim3 grid((a.Nx + 31) / 32, (a.Ny + 7) / 8);
-  k_import_f32<<<grid, block, 0, s>>>(a);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_export_f32(const ConvArgs& a, cudaStream_t s) {
-  dim3 block(32, 8);
-  dim3 grid((a.Nx + 31) / 32, (a.Ny + 7) / 8);
-  k_export_f32<<<grid, block, 0, s>>>(a);
   return cudaGetLastError();
 }
 
