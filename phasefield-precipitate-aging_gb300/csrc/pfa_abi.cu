@@ -558,6 +558,7 @@ static int init_core(CudaData* dev, int nx, int ny, int nm, const double* mask,
   static bool nuc_ready = false;
   if (!nuc_ready) {
     CK(nucleation_setup());
+    CK(prepare_step2d_f32());
     nuc_ready = true;
   }
   if (cr) {

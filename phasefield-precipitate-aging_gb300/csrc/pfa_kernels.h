@@ -29,6 +29,7 @@ struct Step2DArgs {
   float alpha2;         // 2 alpha
   float kap[2];         // kappa
   float idx2f[2];       // 1/dx^2, 1/dy^2
+  int rows;             // FP32 form: rows per warp segment (set by the launcher)
 };
 
 // Layout conversion between FP64 reference fields (ghost ring, pitch64) and
@@ -55,6 +56,7 @@ struct StageArgs {
 
 cudaError_t launch_step2d_f64(const Step2DArgs& a, cudaStream_t s);
 cudaError_t launch_step2d_f32(const Step2DArgs& a, cudaStream_t s);
+cudaError_t prepare_step2d_f32();
 cudaError_t launch_import_f32(const ConvArgs& a, cudaStream_t s);
 cudaError_t launch_export_f32(const ConvArgs& a, cudaStream_t s);
 
