@@ -76,10 +76,11 @@ struct State {
   FastCoef fk{};
   cudaStream_t st = nullptr;
   // FP32 precision form: two buffer sets (fields + compensation)
-  int pitch32 = 0;
+  int pitch32 = 0;      // records per row
   float* f32mem = nullptr;
-  float* f32[2][4] = {};
-  float* c32[2][4] = {};
+  float* recA[2] = {};  // {x_Cr, x_Nb, phi_del, phi_lav} records, ping-pong
+  float* recB[2] = {};  // Kahan compensation records
+  int bstride = 2;      // floats per B record (4 with compensated phases)
   int cur = 0;
   bool f32_live = false;
   // nucleation
@@ -134,19 +135,20 @@ static int ensure_fict(CudaData* dev, State* s) {
   return 0;
 }
 
-// FP32 form buffers, compact layout: Ny rows of pitch32 (a multiple of 32
-// elements), interior only; every array starts on a 256-byte boundary.
+// FP32 form buffers: two record sets (A 16 bytes, B 16 bytes per cell so
+// either precision variant fits), Ny rows of pitch32 records (a multiple of
+// 32), interior only; every array starts on a 256-byte boundary.
 static int ensure_f32(State* s) {
+  s->bstride = s->precision == PFA_FP32_KPHI ? 4 : 2;
   if (s->f32mem) return 0;
   s->pitch32 = ((s->Nx + 31) / 32) * 32;
-  const size_t per = ((size_t(s->pitch32) * s->Ny + 63) / 64) * 64;
-  CK(cudaMalloc(reinterpret_cast<void**>(&s->f32mem), per * 16 * sizeof(float)));
-  CK(cudaMemsetAsync(s->f32mem, 0, per * 16 * sizeof(float), s->st));
-  for (int b = 0; b < 2; b++)
-    for (int k = 0; k < 4; k++) {
-      s->f32[b][k] = s->f32mem + per * (b * 8 + k);
-      s->c32[b][k] = s->f32mem + per * (b * 8 + 4 + k);
-    }
+  const size_t per = ((size_t(s->pitch32) * s->Ny * 4 + 63) / 64) * 64;  // floats per array
+  CK(cudaMalloc(reinterpret_cast<void**>(&s->f32mem), per * 4 * sizeof(float)));
+  CK(cudaMemsetAsync(s->f32mem, 0, per * 4 * sizeof(float), s->st));
+  for (int b = 0; b < 2; b++) {
+    s->recA[b] = s->f32mem + per * (2 * b);
+    s->recB[b] = s->f32mem + per * (2 * b + 1);
+  }
   return 0;
 }
 
@@ -157,10 +159,9 @@ static ConvArgs conv_args(CudaData* dev, State* s) {
   c.f64[2] = dev->phi_del_old;
   c.f64[3] = dev->phi_lav_old;
   const bool kphi = s->precision == PFA_FP32_KPHI;
-  for (int k = 0; k < 4; k++) {
-    c.f32[k] = s->f32[s->cur][k];
-    c.c32[k] = (k < 2 || kphi) ? s->c32[s->cur][k] : nullptr;
-  }
+  c.A = s->recA[s->cur];
+  c.B = s->recB[s->cur];
+  c.bstride = s->bstride;
   c.Nx = s->Nx;
   c.Ny = s->Ny;
   c.pitch64 = s->nx;
@@ -229,12 +230,10 @@ static int fused_step(CudaData* dev, State* s, double alpha, double dt) {
   if (!s->five_point) return fail(PFA_EINVAL, "the FP32 form needs the 5-point mask");
   if (int r = f32_import(dev, s)) return r;
   const int c = s->cur, n = 1 - c;
-  for (int k = 0; k < 4; k++) {
-    a.in[k] = s->f32[c][k];
-    a.out[k] = s->f32[n][k];
-    a.cin[k] = s->c32[c][k];
-    a.cout[k] = s->c32[n][k];
-  }
+  a.in[0] = s->recA[c];
+  a.in[1] = s->recB[c];
+  a.out[0] = s->recA[n];
+  a.out[1] = s->recB[n];
   a.pitch = s->pitch32;
   a.kahan_phi = s->precision == PFA_FP32_KPHI;
   CK(launch_step2d_f32(a, s->st));
@@ -254,12 +253,15 @@ static int nucleate(CudaData* dev, State* s, double sig_d, double sig_l, double 
     a.f[3] = dev->phi_lav_new;
     a.pitch = s->nx;
     a.is_f32 = 0;
+    a.stride = a.cstride = 1;
   } else {
     if (int r = f32_import(dev, s)) return r;
     for (int k = 0; k < 4; k++) {
-      a.f[k] = s->f32[s->cur][k];
-      a.comp[k] = (k < 2 || s->precision == PFA_FP32_KPHI) ? s->c32[s->cur][k] : nullptr;
+      a.f[k] = s->recA[s->cur] + k;
+      a.comp[k] = k < s->bstride ? s->recB[s->cur] + k : nullptr;
     }
+    a.stride = 4;
+    a.cstride = s->bstride;
     a.pitch = s->pitch32;
     a.is_f32 = 1;
     a.compact = 1;
@@ -1000,9 +1002,11 @@ int pfa_summarize(struct CudaData* dev, double* out) {
   if (!s) return fail(PFA_ESTATE, "pfa_summarize: unknown CudaData");
   SumArgs a{};
   if (s->precision != PFA_FP64 && s->f32_live) {
-    for (int k = 0; k < 4; k++) a.f[k] = s->f32[s->cur][k];
-    a.c[0] = s->c32[s->cur][0];
-    a.c[1] = s->c32[s->cur][1];
+    for (int k = 0; k < 4; k++) a.f[k] = s->recA[s->cur] + k;
+    a.c[0] = s->recB[s->cur];
+    a.c[1] = s->recB[s->cur] + 1;
+    a.stride = 4;
+    a.cstride = s->bstride;
     a.is_f32 = 1;
     a.compact = 1;
     a.phi_fix = s->precision == PFA_FP32;
@@ -1014,6 +1018,7 @@ int pfa_summarize(struct CudaData* dev, double* out) {
     a.f[3] = dev->phi_lav_old;
     a.pitch = s->nx;
   }
+  if (a.stride == 0) a.stride = a.cstride = 1;
   a.Nx = s->Nx;
   a.Ny = s->Ny;
   a.Nz = 1;

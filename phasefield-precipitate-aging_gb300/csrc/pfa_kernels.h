@@ -11,10 +11,9 @@ namespace pfa {
 
 // Arguments of one fused 2D step (passed by value to the kernel).
 struct Step2DArgs {
-  const void* in[4];    // x_Cr, x_Nb, phi_del, phi_lav (double or float)
+  const void* in[4];    // FP64: x_Cr, x_Nb, phi_del, phi_lav; FP32 form: in[0] = A
+                        // records, in[1] = B (compensation) records
   void* out[4];
-  const float* cin[4];  // FP32 form: Kahan compensation in (x_Cr, x_Nb[, phi_del, phi_lav])
-  float* cout[4];
   int Nx, Ny, pitch;    // interior size and row pitch (elements)
   int write_halo;       // also write the mirrored ghost ring
   int nine;             // 3x3 mask has non-zero corners
@@ -33,11 +32,14 @@ struct Step2DArgs {
 };
 
 // Layout conversion between FP64 reference fields (ghost ring, pitch64) and
-// the FP32 form's compact fields (interior only, rows of pitch32).
+// the FP32 form's records (interior only, rows of pitch32 records):
+// A = {x_Cr, x_Nb, phi_del, phi_lav} per cell, B = Kahan compensations
+// (bstride = 2: {c_Cr, c_Nb}; 4: also the phases).
 struct ConvArgs {
   double* f64[4];
-  float* f32[4];   // phases hold int32 fixed point when phi_fix
-  float* c32[4];
+  float* A;        // phases hold int32 fixed-point bits when phi_fix
+  float* B;
+  int bstride;
   int Nx, Ny, pitch64, pitch32;
   int phi_fix;
 };

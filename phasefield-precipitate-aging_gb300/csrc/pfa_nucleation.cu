@@ -69,14 +69,16 @@ __device__ __forceinline__ size_t stor(const NucArgs& a, int xx, int yy) {
 
 // a phase field as stored (FP64, FP32 or the FP32 form's fixed point), exact
 template <class T>
-__device__ __forceinline__ double ldphi(const NucArgs& a, int k, size_t i) {
+__device__ __forceinline__ double ldphi(const NucArgs& a, int k, size_t cell) {
+  const size_t i = cell * a.stride;
   if (a.phi_fix) return double(static_cast<const int*>(a.f[k])[i]) * kPhiInvScaleD;
   return ld<T>(a.f[k], i);
 }
 
 // the same, rounded to FP32 without touching the FP64 pipe in the FP32 form
 template <class T>
-__device__ __forceinline__ float ldphi_f(const NucArgs& a, int k, size_t i) {
+__device__ __forceinline__ float ldphi_f(const NucArgs& a, int k, size_t cell) {
+  const size_t i = cell * a.stride;
   if (a.phi_fix) return phi_of(static_cast<const int*>(a.f[k])[i]);
   return float(static_cast<const T*>(a.f[k])[i]);
 }
@@ -199,7 +201,8 @@ __global__ void __launch_bounds__(256) k_nuc_decide(NucArgs a) {
       }
     if (clear) {
       const size_t s = stor(a, x, y);
-      const T Xs = static_cast<const T*>(a.f[0])[s], Ys = static_cast<const T*>(a.f[1])[s];
+      const T Xs = static_cast<const T*>(a.f[0])[s * a.stride];
+      const T Ys = static_cast<const T*>(a.f[1])[s * a.stride];
       const unsigned long long call = *a.call_ptr;
       const uint4 w = philox4x32_10(
           make_uint4(uint32_t(idx), uint32_t(uint64_t(idx) >> 32), uint32_t(call),
@@ -267,10 +270,11 @@ __global__ void __launch_bounds__(256) k_nuc_decide(NucArgs a) {
   }
 }
 
+// store v at cell s of field f (and reset its compensation: value = hi - c)
 template <class T>
-__device__ __forceinline__ void put(void* f, float* c, size_t s, double v) {
-  static_cast<T*>(f)[s] = T(v);
-  if (c) c[s] = float(double(T(v)) - v);
+__device__ __forceinline__ void put(const NucArgs& a, void* f, float* c, size_t s, double v) {
+  static_cast<T*>(f)[s * a.stride] = T(v);
+  if (c) c[s * a.cstride] = float(double(T(v)) - v);
 }
 
 // embed_OPC_kernel, src/discretization.cu:1046-1077, painted cooperatively
@@ -305,15 +309,15 @@ __device__ void paint(const NucArgs& a, const NucEvent& e, int ph) {
     const size_t s = stor(a, xx, yy);
     const double r = sqrt(double(i * i + j * j));
     if (r <= R) {
-      put<T>(a.f[0], ccr, s, parCr);
-      put<T>(a.f[1], cnb, s, parNb);
+      put<T>(a, a.f[0], ccr, s, parCr);
+      put<T>(a, a.f[1], cnb, s, parNb);
       if (a.phi_fix)
-        static_cast<int*>(phi)[s] = phi_quantize(1.0);
+        static_cast<int*>(phi)[s * a.stride] = phi_quantize(1.0);
       else
-        put<T>(phi, cphi, s, 1.0);
+        put<T>(a, phi, cphi, s, 1.0);
     } else {
-      if (r <= RdCr) put<T>(a.f[0], ccr, s, xgCr);
-      if (r <= RdNb) put<T>(a.f[1], cnb, s, xgNb);
+      if (r <= RdCr) put<T>(a, a.f[0], ccr, s, xgCr);
+      if (r <= RdNb) put<T>(a, a.f[1], cnb, s, xgNb);
     }
   }
 }

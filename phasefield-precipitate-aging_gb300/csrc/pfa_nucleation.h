@@ -27,6 +27,8 @@ struct NucArgs {
   int phi_fix;         // phases in 32-bit fixed point (FP32 form)
   int compact;         // FP32 form layout: interior rows only (ghost cells read
                        // as their mirrored interior cell, never painted)
+  int stride;          // elements between consecutive cells of f[k] (4 for FP32 records)
+  int cstride;         // elements between consecutive cells of comp[k]
   int Nx, Ny, pitch;
   double sigma[2];
   double dx;           // kernel spacing (the reference passes dx * nx here)

@@ -36,14 +36,15 @@ __global__ void __launch_bounds__(kThreads) k_sum_partial(SumArgs a) {
        t += (long long)gridDim.x * kThreads) {
     const long long z = t / plane, r = t % plane;
     const int y = int(r / a.Nx), x = int(r % a.Nx);
-    const size_t i = a.compact
-                         ? (size_t(z) * a.Ny + y) * a.pitch + x
-                         : (size_t(a.is3d ? z + 1 : 0) * (a.Ny + 2) + (y + 1)) * a.pitch + (x + 1);
+    const size_t cell = a.compact
+                            ? (size_t(z) * a.Ny + y) * a.pitch + x
+                            : (size_t(a.is3d ? z + 1 : 0) * (a.Ny + 2) + (y + 1)) * a.pitch + (x + 1);
+    const size_t i = cell * a.stride, ic = cell * a.cstride;
     const T* f0 = static_cast<const T*>(a.f[0]);
     const T* f1 = static_cast<const T*>(a.f[1]);
     double xcr = double(f0[i]), xnb = double(f1[i]);
-    if (a.c[0]) xcr -= double(a.c[0][i]);
-    if (a.c[1]) xnb -= double(a.c[1][i]);
+    if (a.c[0]) xcr -= double(a.c[0][ic]);
+    if (a.c[1]) xnb -= double(a.c[1][ic]);
     double phd, phl;
     if (a.phi_fix) {
       phd = double(static_cast<const int*>(a.f[2])[i]) * kPhiInvScaleD;

@@ -13,6 +13,8 @@ struct SumArgs {
   int is_f32, is3d;
   int phi_fix;        // phases in the FP32 form's 32-bit fixed point
   int compact;        // interior-only rows (FP32 form) instead of the ghost-ring layout
+  int stride;         // elements between consecutive cells of f (4 for FP32 records)
+  int cstride;        // elements between consecutive cells of c
   int Nx, Ny, Nz, pitch;
   double* partial;    // scratch: kSumBlocks * 5 doubles
   double* out;        // 5 doubles (device)

@@ -2,21 +2,24 @@
 //
 // Same step as the FP64 kernel (src/main.cpp:289-305 fused), arithmetic in
 // FP32, x_Cr / x_Nb Kahan-compensated, phases in 32-bit fixed point (or FP32
-// + Kahan).  Organised for instruction economy, since at 48 bytes per cell
-// the HBM budget leaves ~200 FP32 instructions per cell:
-//  * each warp owns a strip of 32 columns and streams down H rows; the three
-//    rows a 5-point Laplacian needs live in registers (a sliding window), so
-//    every cell's gamma solve runs once and nothing goes through shared
-//    memory;
-//  * left / right neighbours come from __shfl_up / __shfl_down; the two
-//    columns outside the strip are computed by lanes 0 and 31 in one
-//    divergent pass per row;
-//  * the raw fields of the row after next are loaded one iteration ahead.
+// + Kahan).  At 48 bytes per cell the HBM budget leaves ~250 instructions per
+// cell, so the kernel is organised for instruction economy:
+//  * each warp owns a strip of 30 output columns (lanes 1..30; lanes 0 and
+//    31 carry the neighbour columns) and streams down a segment of rows; the
+//    three rows a 5-point Laplacian needs live in registers, rotated by a
+//    3x-unrolled loop, so each cell's gamma solve runs once and nothing goes
+//    through shared memory;
+//  * left / right neighbours come from __shfl_up / __shfl_down;
+//  * the state is stored as two records per cell -- A = {x_Cr, x_Nb, phi_del,
+//    phi_lav} (16 bytes) and B = Kahan compensations {c_Cr, c_Nb} (8 bytes,
+//    or 16 with compensated phases) -- so a row costs one 128-bit and one
+//    64-bit load and store and a single address per lane; records of the row
+//    after next are loaded one iteration ahead.
 //
-// Compact layout: Ny rows of `pitch` elements (pitch a multiple of 32, rows
-// 128-byte aligned), interior cell (x, y) at y * pitch + x, no ghost ring;
-// zero-flux edges come from clamped indexing (the mirror the reference's
-// halo fill produces).
+// Record layout: Ny rows of `pitch` records (pitch a multiple of 32), interior
+// cell (x, y) at record y * pitch + x, no ghost ring; zero-flux edges come
+// from clamped indexing (the mirror the reference's halo fill produces).
+// Fixed-point phases (FIX) keep their int32 bits in the float slots.
 #include <cstdint>
 #include <type_traits>
 
@@ -29,30 +32,30 @@ using namespace dev;
 
 namespace {
 
-constexpr int kWarps = 4;         // warps (strips) per CTA
-constexpr int kCols = 30;         // output columns per warp; lanes 0 and 31 are halo
+constexpr int kWarps = 4;  // warps (strips) per CTA
+constexpr int kCols = 30;  // output columns per warp; lanes 0 and 31 are halo
 
 // The values a neighbour needs: gamma compositions and the phases (FP32).
 struct Nb {
   float gcr, gnb, pd, pl;
 };
 
+// Compensation record: {c_Cr, c_Nb} or {c_Cr, c_Nb, c_del, c_lav}.
 template <bool FIX>
-using PhiT = typename std::conditional<FIX, int, float>::type;
+using CompT = typename std::conditional<FIX, float2, float4>::type;
 
-// Raw stored values of one cell.
 template <bool FIX>
 struct Raw {
-  float x, y;
-  PhiT<FIX> pd, pl;
+  float4 a;      // x_Cr, x_Nb, phi_del, phi_lav (int bits when FIX)
+  CompT<FIX> c;  // Kahan compensations
 };
 
 template <bool FIX>
-__device__ __forceinline__ float phf(PhiT<FIX> v) {
+__device__ __forceinline__ float phf(float bits) {
   if constexpr (FIX)
-    return phi_of(v);
+    return phi_of(__float_as_int(bits));
   else
-    return v;
+    return bits;
 }
 
 // gamma solve of one cell (approximate reciprocal: 2 ulp is far inside the
@@ -92,8 +95,8 @@ __device__ __forceinline__ int phi_step(int q, float inc) {
 // dF/dphi_i without the Laplacian term: -p'(phi) dP + 2 omega phi (phi-1)(2 phi-1)
 // + 2 alpha phi phi_j^2, Horner forms
 __device__ __forceinline__ float dF_local(float ph, float pj, float dP, float om2, float alpha2) {
-  const float t = fmaf(-ph, ph, ph);                 // phi (1 - phi)
-  const float pp = 30.0f * t * t;                    // p'(phi)
+  const float t = fmaf(-ph, ph, ph);  // phi (1 - phi)
+  const float pp = 30.0f * t * t;     // p'(phi)
   const float well = ph * fmaf(ph, fmaf(2.0f * om2, ph, -3.0f * om2), om2);
   return fmaf(-pp, dP, fmaf(alpha2 * ph, pj * pj, well));
 }
@@ -101,29 +104,20 @@ __device__ __forceinline__ float dF_local(float ph, float pj, float dP, float om
 template <bool FIX>
 struct Stream {
   const Step2DArgs& a;
-  const float *px, *py, *pc0, *pc1, *pc2, *pc3;
-  const PhiT<FIX>*pd, *pl;
-  float *ox, *oy, *oc0, *oc1, *oc2, *oc3;
-  PhiT<FIX>*od, *ol;
+  const float4* A;        // this lane's column, row 0
+  const CompT<FIX>* B;
+  float4* Ao;
+  CompT<FIX>* Bo;
   int Ny, P;
   bool out;  // this lane writes its column
 
   __device__ __forceinline__ int row(int y) const { return min(max(y, 0), Ny - 1) * P; }
 
-  __device__ __forceinline__ Raw<FIX> load(int off) const {
-    return Raw<FIX>{__ldg(px + off), __ldg(py + off), __ldg(pd + off), __ldg(pl + off)};
-  }
+  __device__ __forceinline__ Raw<FIX> load(int off) const { return Raw<FIX>{__ldg(A + off), __ldg(B + off)}; }
 
-  // update row y from its window (up, c, dn); rc = raw centre values
+  // update row y from its window (up, c, dn); rc = raw centre record
   __device__ __forceinline__ void update(int y, const Nb& up, const Nb& c, const Nb& dn,
                                          const Raw<FIX>& rc) const {
-    const int i = y * P;
-    const float cin0 = __ldg(pc0 + i), cin1 = __ldg(pc1 + i);
-    float cin2 = 0.f, cin3 = 0.f;
-    if constexpr (!FIX) {
-      cin2 = __ldg(pc2 + i);
-      cin3 = __ldg(pc3 + i);
-    }
     Nb w, e;
     w.gcr = __shfl_up_sync(0xffffffffu, c.gcr, 1);
     w.gnb = __shfl_up_sync(0xffffffffu, c.gnb, 1);
@@ -144,30 +138,35 @@ struct Stream {
     const float lapD = lap(w.pd, e.pd, up.pd, dn.pd, c.pd);
     const float lapL = lap(w.pl, e.pl, up.pl, dn.pl, c.pl);
     // Cahn-Hilliard, Kahan-compensated
-    const float X = rc.x, Y = rc.y;
-    const float ycr = fmaf(a.dtD[0][0], lapCr, a.dtD[0][1] * lapNb) - cin0, tcr = X + ycr;
-    const float ynb = fmaf(a.dtD[1][0], lapCr, a.dtD[1][1] * lapNb) - cin1, tnb = Y + ynb;
+    const float X = rc.a.x, Y = rc.a.y;
+    const float ycr = fmaf(a.dtD[0][0], lapCr, a.dtD[0][1] * lapNb) - rc.c.x, tcr = X + ycr;
+    const float ynb = fmaf(a.dtD[1][0], lapCr, a.dtD[1][1] * lapNb) - rc.c.y, tnb = Y + ynb;
     // Allen-Cahn
     const FastCoef& K = a.k;
     const float u1 = c.gcr - K.xe_gam[0], u2 = c.gnb - K.xe_gam[1];
     const float dFd = fmaf(-a.kap[0], lapD, dF_local(c.pd, c.pl, quad2(K.dP[0], u1, u2), a.om2[0], a.alpha2));
     const float dFl = fmaf(-a.kap[1], lapL, dF_local(c.pl, c.pd, quad2(K.dP[1], u1, u2), a.om2[1], a.alpha2));
     if (out) {
-      ox[i] = tcr;
-      oy[i] = tnb;
-      oc0[i] = (tcr - X) - ycr;
-      oc1[i] = (tnb - Y) - ynb;
+      const int i = y * P;
+      float4 o;
+      CompT<FIX> oc;
+      o.x = tcr;
+      o.y = tnb;
+      oc.x = (tcr - X) - ycr;
+      oc.y = (tnb - Y) - ynb;
       if constexpr (FIX) {
-        od[i] = phi_step(rc.pd, -a.dtL[0] * dFd);
-        ol[i] = phi_step(rc.pl, -a.dtL[1] * dFl);
+        o.z = __int_as_float(phi_step(__float_as_int(rc.a.z), -a.dtL[0] * dFd));
+        o.w = __int_as_float(phi_step(__float_as_int(rc.a.w), -a.dtL[1] * dFl));
       } else {
-        const float yd = fmaf(-a.dtL[0], dFd, -cin2), td = c.pd + yd;
-        const float yl = fmaf(-a.dtL[1], dFl, -cin3), tl = c.pl + yl;
-        od[i] = td;
-        ol[i] = tl;
-        oc2[i] = (td - c.pd) - yd;
-        oc3[i] = (tl - c.pl) - yl;
+        const float yd = fmaf(-a.dtL[0], dFd, -rc.c.z), td = c.pd + yd;
+        const float yl = fmaf(-a.dtL[1], dFl, -rc.c.w), tl = c.pl + yl;
+        o.z = td;
+        o.w = tl;
+        oc.z = (td - c.pd) - yd;
+        oc.w = (tl - c.pl) - yl;
       }
+      Ao[i] = o;
+      Bo[i] = oc;
     }
   }
 };
@@ -183,20 +182,16 @@ __global__ void __launch_bounds__(32 * kWarps, 8) k_stream_f32(Step2DArgs a) {
   const int gx = x0 - 1 + lane;  // lanes 0 and 31 hold the neighbour columns
   const int cx = min(max(gx, 0), a.Nx - 1);
   const FastCoef& K = a.k;
-  Stream<FIX> S{a,
-                static_cast<const float*>(a.in[0]) + cx, static_cast<const float*>(a.in[1]) + cx,
-                a.cin[0] + cx, a.cin[1] + cx, FIX ? nullptr : a.cin[2] + cx,
-                FIX ? nullptr : a.cin[3] + cx,
-                static_cast<const PhiT<FIX>*>(a.in[2]) + cx, static_cast<const PhiT<FIX>*>(a.in[3]) + cx,
-                static_cast<float*>(a.out[0]) + cx, static_cast<float*>(a.out[1]) + cx,
-                a.cout[0] + cx, a.cout[1] + cx, FIX ? nullptr : a.cout[2] + cx,
-                FIX ? nullptr : a.cout[3] + cx,
-                static_cast<PhiT<FIX>*>(a.out[2]) + cx, static_cast<PhiT<FIX>*>(a.out[3]) + cx,
-                a.Ny, a.pitch, lane >= 1 && lane <= kCols && gx < a.Nx};
+  const Stream<FIX> S{a,
+                      static_cast<const float4*>(a.in[0]) + cx,
+                      static_cast<const CompT<FIX>*>(a.in[1]) + cx,
+                      static_cast<float4*>(a.out[0]) + cx,
+                      static_cast<CompT<FIX>*>(a.out[1]) + cx,
+                      a.Ny, a.pitch, lane >= 1 && lane <= kCols && gx < a.Nx};
   auto solve_raw = [&](const Raw<FIX>& r) {
-    return solve(K, r.x, r.y, phf<FIX>(r.pd), phf<FIX>(r.pl));
+    return solve(K, r.a.x, r.a.y, phf<FIX>(r.a.z), phf<FIX>(r.a.w));
   };
-  // window rows y-1, y, y+1 and raw rows y, y+1, y+2
+  // window rows y-1, y, y+1 and raw records of rows y, y+1, y+2
   Raw<FIX> r0 = S.load(S.row(y0)), r1 = S.load(S.row(y0 + 1)), r2;
   Nb n0 = solve_raw(S.load(S.row(y0 - 1))), n1 = solve_raw(r0), n2;
   // three rows per iteration with rotated roles: no register moves
@@ -224,57 +219,61 @@ __global__ void __launch_bounds__(32 * kWarps, 8) k_stream_f32(Step2DArgs a) {
 }
 
 // ---- layout conversion between the reference's FP64 fields and the form ----
-__global__ void k_import_compact(ConvArgs a) {
+__global__ void k_import_records(ConvArgs a) {
   const int gx = blockIdx.x * blockDim.x + threadIdx.x;
   const int gy = blockIdx.y * blockDim.y + threadIdx.y;
   if (gx >= a.Nx || gy >= a.Ny) return;
   const size_t i64 = size_t(gy + 1) * a.pitch64 + gx + 1;
-  const size_t i32 = size_t(gy) * a.pitch32 + gx;
+  const size_t r = size_t(gy) * a.pitch32 + gx;
+  float* A = a.A + 4 * r;
+  float* B = a.B + size_t(a.bstride) * r;
 #pragma unroll
   for (int k = 0; k < 4; k++) {
     const double v = a.f64[k][i64];
     if (k >= 2 && a.phi_fix) {
-      reinterpret_cast<int*>(a.f32[k])[i32] = phi_quantize(v);
+      A[k] = __int_as_float(phi_quantize(v));
       continue;
     }
     const float hi = float(v);
-    a.f32[k][i32] = hi;
+    A[k] = hi;
     // compensation c holds -(low part): value = hi - c
-    if (a.c32[k]) a.c32[k][i32] = float(double(hi) - v);
+    if (k < a.bstride) B[k] = float(double(hi) - v);
   }
 }
 
-__global__ void k_export_compact(ConvArgs a) {
+__global__ void k_export_records(ConvArgs a) {
   const int gx = blockIdx.x * blockDim.x + threadIdx.x;
   const int gy = blockIdx.y * blockDim.y + threadIdx.y;
   if (gx >= a.Nx || gy >= a.Ny) return;
-  const size_t i32 = size_t(gy) * a.pitch32 + gx;
+  const size_t r = size_t(gy) * a.pitch32 + gx;
+  const float* A = a.A + 4 * r;
+  const float* B = a.B + size_t(a.bstride) * r;
   const size_t row = size_t(gy + 1) * a.pitch64;
 #pragma unroll
   for (int k = 0; k < 4; k++) {
     double v;
     if (k >= 2 && a.phi_fix) {
-      v = double(reinterpret_cast<const int*>(a.f32[k])[i32]) * kPhiInvScaleD;
+      v = double(__float_as_int(A[k])) * kPhiInvScaleD;
     } else {
-      v = double(a.f32[k][i32]);
-      if (a.c32[k]) v -= double(a.c32[k][i32]);
+      v = double(A[k]);
+      if (k < a.bstride) v -= double(B[k]);
     }
     double* f = a.f64[k];
     f[row + gx + 1] = v;
     // ghost ring = mirror of the interior; corners take the diagonal cell
-    const bool l = gx == 0, r = gx == a.Nx - 1, b = gy == 0, t = gy == a.Ny - 1;
+    const bool l = gx == 0, rr = gx == a.Nx - 1, b = gy == 0, t = gy == a.Ny - 1;
     if (l) f[row] = v;
-    if (r) f[row + a.Nx + 1] = v;
+    if (rr) f[row + a.Nx + 1] = v;
     if (b) {
       f[gx + 1] = v;
       if (l) f[0] = v;
-      if (r) f[a.Nx + 1] = v;
+      if (rr) f[a.Nx + 1] = v;
     }
     if (t) {
       const size_t top = size_t(a.Ny + 1) * a.pitch64;
       f[top + gx + 1] = v;
       if (l) f[top] = v;
-      if (r) f[top + a.Nx + 1] = v;
+      if (rr) f[top + a.Nx + 1] = v;
     }
   }
 }
@@ -282,7 +281,7 @@ __global__ void k_export_compact(ConvArgs a) {
 // Rows per warp segment: the CTA count should fill whole waves of the
 // resident CTAs (a partial last wave idles SMs), while each segment pays two
 // extra rows of gamma solves at its ends.
-static int segment_rows(int Nx, int Ny, int resident) {
+int segment_rows(int Nx, int Ny, int resident) {
   const int nbx = ((Nx + kCols - 1) / kCols + kWarps - 1) / kWarps;
   int best = Ny;
   double best_score = 0.0;
@@ -302,10 +301,10 @@ static int segment_rows(int Nx, int Ny, int resident) {
   return best;
 }
 
-static int g_resident[2] = {0, 0};  // resident CTAs of the two variants
+int g_resident[2] = {0, 0};  // resident CTAs of the two variants
 
 template <bool FIX>
-static cudaError_t query_resident() {
+cudaError_t query_resident() {
   int dev = 0, sms = 0, per = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -316,7 +315,7 @@ static cudaError_t query_resident() {
 }
 
 template <bool FIX>
-static cudaError_t launch_stream(Step2DArgs a, cudaStream_t s) {
+cudaError_t launch_stream(Step2DArgs a, cudaStream_t s) {
   const int resident = g_resident[FIX] > 0 ? g_resident[FIX] : 152 * 8;
   a.rows = segment_rows(a.Nx, a.Ny, resident);
   const int strips = (a.Nx + kCols - 1) / kCols;
@@ -340,14 +339,14 @@ cudaError_t prepare_step2d_f32() {
 cudaError_t launch_import_f32(const ConvArgs& a, cudaStream_t s) {
   dim3 block(32, 8);
   dim3 grid((a.Nx + 31) / 32, (a.Ny + 7) / 8);
-  k_import_compact<<<grid, block, 0, s>>>(a);
+  k_import_records<<<grid, block, 0, s>>>(a);
   return cudaGetLastError();
 }
 
 cudaError_t launch_export_f32(const ConvArgs& a, cudaStream_t s) {
   dim3 block(32, 8);
   dim3 grid((a.Nx + 31) / 32, (a.Ny + 7) / 8);
-  k_export_compact<<<grid, block, 0, s>>>(a);
+  k_export_records<<<grid, block, 0, s>>>(a);
   return cudaGetLastError();
 }
 
