@@ -289,6 +289,18 @@ static int nucleate(CudaData* dev, State* s, double sig_d, double sig_l, double 
   a.R_scan = 1.75e-9 / kdx;
   a.ln_dtdV = std::log(dt * a.dV);
   a.ln_ngam = std::log(a.n_gam);
+  // constants of the FP32 screening bound (pfa_nucleation.cu, ln_z_bound):
+  // ln z <= lnC1 + max e - C2 / (dG^2 max dc)
+  for (int ph = 0; ph < 2; ph++) {
+    const double sg = a.sigma[ph], s3 = sg * sg * sg;
+    const double a4 = std::pow(kLatticeConst, 4);
+    const double lnDpre = std::log(3.0 * 1.5e-20 * 2.5e6);            // |D| prefactor bound
+    const double lnG = std::log(16.0 * kPi * s3 / 3.0);                  // G* dG^2
+    const double lnZ = std::log(a.Vatom / (8.0 * kPi * std::sqrt(kKT * s3)));  // Zeldovich / dG^2
+    a.lnC1[ph] = float(std::log(3.0) + lnG - std::log(sg) - std::log(a4) + lnDpre + lnZ +
+                       a.ln_ngam + std::log(2.0) + a.ln_dtdV);
+    a.C2[ph] = float(16.0 * kPi * s3 / (3.0 * kKT));
+  }
   a.seed = s->seed;
   a.call_ptr = s->call_dev;
   a.events = s->ev;

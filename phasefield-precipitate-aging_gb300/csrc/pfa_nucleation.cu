@@ -123,7 +123,13 @@ __device__ void probability_sphere(double xCr, double xNb, double dG, double dcc
 // +inf where no bound is attempted (compositions outside the simplex, or
 // above the gamma equilibrium composition, where the exponents change sign).
 // The diffusivities are bounded by the magnitudes of their three mobility
-// terms, so the bound holds whatever the signs of D_CrCr and D_NbNb.
+// terms, so the bound holds whatever the signs of D_CrCr and D_NbNb:
+//   |D| <= 3 x 1.5e-20 x exp(max e) x 2.5e6     (prefactors, |s| + add)
+//   k1  <= 3 G* |D| / (sigma a^4) x Zeldovich x n_gam      (x <= 1)
+//   J_Cr + J_Nb <= 2 k1 exp(-k2 / max(dc_Cr, dc_Nb)),  k2 = G* / kT.
+// With G* = 16 pi sigma^3 / (3 dG^2) and Zeldovich ~ dG^2 the dG factors of
+// k1 cancel, so ln z <= lnC1 + max e - C2 / (dG^2 max dc) with the per-phase
+// constants lnC1, C2 of the host (NucArgs).
 __device__ void ln_z_bound(float X, float Y, const NucArgs& a, float lnz[2]) {
   lnz[0] = lnz[1] = INFINITY;
   const float dcCr = float(kXe[0][0]) - X, dcNb = Y - float(kXe[0][1]);
@@ -137,20 +143,11 @@ __device__ void ln_z_bound(float X, float Y, const NucArgs& a, float lnz[2]) {
   const float eCr = -7.1543718172640256f * X * xni + 3.3541967644499233f * X;
   const float eNi = -8.5221193705645018f * X * xni + 4.0036674816806448f * X -
                     442.62877981749585f * Y * xni - 0.82164267100913768f * Y;
-  // |D| <= 3 terms x prefactor (<= 1.5e-20) x exp(e) x (|s| + add <= 2.5e6)
-  const float lnDmax = -35.33f + fmaxf(eNb, fmaxf(eCr, eNi));  // ln(3 * 1.5e-20 * 2.5e6) = -36.04
-  const float a4 = float(kLatticeConst * kLatticeConst * kLatticeConst * kLatticeConst);
+  const float emax = fmaxf(eNb, fmaxf(eCr, eNi));
+  const float inv = __fdividef(1.0f, dG * dG * fmaxf(dcCr, dcNb));
 #pragma unroll
   for (int ph = 0; ph < 2; ph++) {
-    const float sigma = float(a.sigma[ph]);
-    const float s3 = sigma * sigma * sigma;
-    const float Gstar = (16.0f * float(kPi) * s3) / (3.0f * dG * dG);
-    const float Z = float(a.Vatom) * dG * dG / (8.0f * float(kPi) * sqrtf(float(kKT) * s3));
-    // ln k1 <= ln(3 G* Dmax / (sigma a^4)) + ln Zeldovich + ln n_gam  (x <= 1)
-    const float lnk1 = logf(3.0f * Gstar / (sigma * a4)) + lnDmax + logf(Z) + float(a.ln_ngam);
-    const float k2 = Gstar / float(kKT);
-    // J_Cr + J_Nb <= 2 k1_max exp(-min(k2 / dc_Cr, k2 / dc_Nb))
-    const float l = lnk1 - fminf(k2 / dcCr, k2 / dcNb) + 0.6931472f + float(a.ln_dtdV);
+    const float l = a.lnC1[ph] + emax - a.C2[ph] * inv;
     if (l == l) lnz[ph] = l;  // NaN stays +inf
   }
 }
@@ -203,23 +200,28 @@ __global__ void __launch_bounds__(256) k_nuc_decide(NucArgs a) {
       const size_t s = stor(a, x, y);
       const T Xs = static_cast<const T*>(a.f[0])[s * a.stride];
       const T Ys = static_cast<const T*>(a.f[1])[s * a.stride];
-      const unsigned long long call = *a.call_ptr;
-      const uint4 w = philox4x32_10(
-          make_uint4(uint32_t(idx), uint32_t(uint64_t(idx) >> 32), uint32_t(call),
-                     uint32_t(call >> 32)),
-          make_uint2(uint32_t(a.seed), uint32_t(a.seed >> 32)));
-      // Screen in FP32: u >= hi32 2^-32 (rounded toward zero), and the FP64
-      // P_nuc = 1 - exp(-z) <= max(z, 0) (1 + 1e-15) + 2^-53 <= P_up, so a cell
-      // with u_lower >= P_up cannot nucleate.
+      // Screen in FP32 (margin e^12 on the bound z_up of z = dt dV (J_Cr + J_Nb)):
+      //  * z < 2^-55: FP64 exp(-z) is 1 or 1 - 2^-53, so P_nuc <= 2^-53 <= u for
+      //    every draw -- no event, no draw needed;
+      //  * else draw, and skip the FP64 path when u >= hi32 2^-32 (rounded
+      //    toward zero) >= P_up >= P_nuc.
       float lnz[2];
       ln_z_bound(float(Xs), float(Ys), a, lnz);
-      const float ulo[2] = {__uint2float_rz(w.x) * 0x1p-32f, __uint2float_rz(w.z) * 0x1p-32f};
+      const float lnz_max = fmaxf(lnz[0], lnz[1]) + 12.0f;
       bool need = false;
+      uint4 w = make_uint4(0, 0, 0, 0);
+      if (!(lnz_max < -38.8f)) {  // ln 2^-56
+        const unsigned long long call = *a.call_ptr;
+        w = philox4x32_10(make_uint4(uint32_t(idx), uint32_t(uint64_t(idx) >> 32),
+                                     uint32_t(call), uint32_t(call >> 32)),
+                          make_uint2(uint32_t(a.seed), uint32_t(a.seed >> 32)));
+        const float ulo[2] = {__uint2float_rz(w.x) * 0x1p-32f, __uint2float_rz(w.z) * 0x1p-32f};
 #pragma unroll
-      for (int ph = 0; ph < 2; ph++) {
-        const bool bounded = lnz[ph] + 12.0f < 80.0f;
-        const float pup = 2.0f * __expf(fminf(lnz[ph] + 12.0f, 80.0f)) + 0x1p-52f;
-        if (!bounded || !(ulo[ph] >= pup)) need = true;
+        for (int ph = 0; ph < 2; ph++) {
+          const bool bounded = lnz[ph] + 12.0f < 80.0f;
+          const float pup = 2.0f * __expf(fminf(lnz[ph] + 12.0f, 80.0f)) + 0x1p-52f;
+          if (!bounded || !(ulo[ph] >= pup)) need = true;
+        }
       }
       if (need) {
         const double X = double(Xs), Y = double(Ys);

@@ -34,6 +34,7 @@ struct NucArgs {
   double dx;           // kernel spacing (the reference passes dx * nx here)
   double dV, Vatom, n_gam, dt, R_scan;
   double ln_dtdV, ln_ngam;
+  float lnC1[2], C2[2];  // per-phase constants of the FP32 screening bound
   uint64_t seed;
   unsigned long long* call_ptr;  // scratch: nucleation call counter (Philox counter word)
   NucEvent* events;    // scratch: kNucCap events
