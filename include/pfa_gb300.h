@@ -111,6 +111,22 @@ int pfa_last_nucleation_events(struct CudaData* dev, int64_t* cells, int32_t* ph
 /* out[5] = mean x_Cr, mean x_Nb, f_gamma, f_delta, f_laves over the interior */
 int pfa_summarize(struct CudaData* dev, double* out);
 
+/* The same summary for callers that cannot let a library allocate device
+ * memory (a host that owns all device memory through its own pool or a fixed
+ * budget, or a step loop that must not see cudaMalloc's implicit device
+ * synchronisation).  No counterpart in the reference.  Inputs are four
+ * caller-owned device fields in the reference layout (ny rows of nx doubles
+ * with the ghost ring); out is a caller-owned device buffer of 5 doubles;
+ * the work is enqueued on `stream` (a cudaStream_t, NULL = default stream).
+ * Allocates nothing: its scratch is a static device array holding one row of
+ * partial sums per grid row, at most 16384 interior rows (ny - 2 <= 16384,
+ * else PFA_EINVAL).  The first call on a device looks up that array's device
+ * address (cudaGetSymbolAddress), so make it before any stream capture.
+ * Calls share the array: calls that overlap on the GPU race. */
+int pfa_summarize_fields_noalloc(const double* conc_Cr, const double* conc_Nb,
+                                 const double* phi_del, const double* phi_lav, int nx, int ny,
+                                 double* out, void* stream);
+
 /* ---- model helpers ---- */
 /* out[13]: D_Cr[2], D_Nb[2], kappa[2], omega[2], Lmob[2], alpha, dt, rho(D J).
  * dt_rule 0 = the reference's dt (src/main.cpp:260-268, with meshres);

@@ -83,6 +83,8 @@ def load():
         "pfa_model_fast_coef": (_i, [_fp, _i]),
         "pfa_philox_block": (_i, [ctypes.POINTER(ctypes.c_uint32), ctypes.c_uint64,
                                   ctypes.POINTER(ctypes.c_uint32), _i]),
+        "pfa_summarize_fields_noalloc": (_i, [ctypes.c_void_p] * 4 + [_i, _i, ctypes.c_void_p,
+                                                                      ctypes.c_void_p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
