@@ -289,6 +289,20 @@ static int nucleate(CudaData* dev, State* s, double sig_d, double sig_l, double 
   a.R_scan = 1.75e-9 / kdx;
   a.ln_dtdV = std::log(dt * a.dV);
   a.ln_ngam = std::log(a.n_gam);
+  // the reference's loop `for (int i = -R; i < R; i++)` with the test
+  // i*i + j*j < R*R, in integers: lo = (int)(-R), hi = first int >= R,
+  // r2 = largest int < R*R
+  {
+    const double R = a.R_scan;
+    a.scan_lo = int(-R);
+    int hi = a.scan_lo;
+    while (double(hi) < R) hi++;
+    a.scan_hi = hi;
+    const double R2 = R * R;
+    long long m = (long long)std::floor(R2);
+    if (double(m) >= R2) m--;  // strictly below R^2
+    a.scan_r2 = int(m);
+  }
   // constants of the FP32 screening bound (pfa_nucleation.cu, ln_z_bound):
   // ln z <= lnC1 + max e - C2 / (dG^2 max dc)
   for (int ph = 0; ph < 2; ph++) {

@@ -176,14 +176,15 @@ __global__ void __launch_bounds__(256) k_nuc_decide(NucArgs a) {
   if (gx < a.Nx && gy < a.Ny) {
     const int x = gx + 1, y = gy + 1;
     const long long idx = (long long)nxr * y + x;
-    const double R = a.R_scan;
     bool clear = true;
-    // neighbourhood scan of src/discretization.cu:1104-1117; the reference
+    // neighbourhood scan of src/discretization.cu:1104-1117 with the
+    // reference's double-valued bounds turned into integers on the host
+    // (i from (int)(-R) while i < R, i^2 + j^2 < R^2); the reference
     // bounds-checks the linear index nx (y + j) + (x + i), so offsets past a
     // row end wrap onto the next row -- reproduced by normalising (xx, yy)
-    for (int i = int(-R); i < R && clear; i++)
-      for (int j = int(-R); j < R && clear; j++) {
-        if (!(double(i * i + j * j) < R * R)) continue;
+    for (int i = a.scan_lo; i < a.scan_hi && clear; i++)
+      for (int j = a.scan_lo; j < a.scan_hi && clear; j++) {
+        if (i * i + j * j > a.scan_r2) continue;
         int xx = x + i, yy = y + j;
         while (xx < 0) {
           xx += nxr;
@@ -200,14 +201,19 @@ __global__ void __launch_bounds__(256) k_nuc_decide(NucArgs a) {
       const size_t s = stor(a, x, y);
       const T Xs = static_cast<const T*>(a.f[0])[s * a.stride];
       const T Ys = static_cast<const T*>(a.f[1])[s * a.stride];
-      // Screen in FP32 (margin e^12 on the bound z_up of z = dt dV (J_Cr + J_Nb)):
+      // Screen in FP32 on the bound z_up of z = dt dV (J_Cr + J_Nb), which
+      // carries several nats of analytic slack; kMargin covers the FP32
+      // evaluation error many times over:
       //  * z < 2^-55: FP64 exp(-z) is 1 or 1 - 2^-53, so P_nuc <= 2^-53 <= u for
       //    every draw -- no event, no draw needed;
       //  * else draw, and skip the FP64 path when u >= hi32 2^-32 (rounded
       //    toward zero) >= P_up >= P_nuc.
+      // A tight screen matters: one lane that needs the FP64 path makes its
+      // whole warp issue it.
+      constexpr float kMargin = 2.0f;
       float lnz[2];
       ln_z_bound(float(Xs), float(Ys), a, lnz);
-      const float lnz_max = fmaxf(lnz[0], lnz[1]) + 12.0f;
+      const float lnz_max = fmaxf(lnz[0], lnz[1]) + kMargin;
       bool need = false;
       uint4 w = make_uint4(0, 0, 0, 0);
       if (!(lnz_max < -38.8f)) {  // ln 2^-56
@@ -218,8 +224,8 @@ __global__ void __launch_bounds__(256) k_nuc_decide(NucArgs a) {
         const float ulo[2] = {__uint2float_rz(w.x) * 0x1p-32f, __uint2float_rz(w.z) * 0x1p-32f};
 #pragma unroll
         for (int ph = 0; ph < 2; ph++) {
-          const bool bounded = lnz[ph] + 12.0f < 80.0f;
-          const float pup = 2.0f * __expf(fminf(lnz[ph] + 12.0f, 80.0f)) + 0x1p-52f;
+          const bool bounded = lnz[ph] + kMargin < 80.0f;
+          const float pup = 2.0f * __expf(fminf(lnz[ph] + kMargin, 80.0f)) + 0x1p-52f;
           if (!bounded || !(ulo[ph] >= pup)) need = true;
         }
       }

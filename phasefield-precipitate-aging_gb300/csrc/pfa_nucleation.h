@@ -35,6 +35,8 @@ struct NucArgs {
   double dV, Vatom, n_gam, dt, R_scan;
   double ln_dtdV, ln_ngam;
   float lnC1[2], C2[2];  // per-phase constants of the FP32 screening bound
+  int scan_lo, scan_hi;  // scan offsets i in [scan_lo, scan_hi) (from R_scan)
+  int scan_r2;           // largest integer below R_scan^2
   uint64_t seed;
   unsigned long long* call_ptr;  // scratch: nucleation call counter (Philox counter word)
   NucEvent* events;    // scratch: kNucCap events
