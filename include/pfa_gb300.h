@@ -107,6 +107,24 @@ void* pfa_stream(struct CudaData* dev);
  * (cell index, phase) in canonical order; returns the count */
 int pfa_last_nucleation_events(struct CudaData* dev, int64_t* cells, int32_t* phases, int cap);
 
+/* ---- 3D grids (7-point Laplacian) ----
+ * No counterpart in the reference, which is 2D only (src/main.cpp:418-421):
+ * the same equations with six-face zero-flux ghost fill.  Fields are
+ * (nz x ny x nx) doubles with the ghost ring; params = D_Cr[2], D_Nb[2],
+ * kappa[2], omega[2], Lmob[2], alpha, dt (12 doubles, the layout of
+ * pfa_model_params' output); dxyz = dx, dy, dz; precision PFA_FP64 or
+ * PFA_FP32.  The handle owns its device buffers and stream. */
+int pfa3d_create(void** handle, int nx, int ny, int nz, const double* params, const double* dxyz,
+                 const double* conc_Cr, const double* conc_Nb, const double* phi_del,
+                 const double* phi_lav, int precision);
+int pfa3d_run(void* handle, int nsteps);
+int pfa3d_run_timed(void* handle, int nsteps, float* ms);
+int pfa3d_read(void* handle, double* conc_Cr, double* conc_Nb, double* phi_del, double* phi_lav);
+int pfa3d_upload(void* handle, const double* conc_Cr, const double* conc_Nb,
+                 const double* phi_del, const double* phi_lav);
+int pfa3d_summarize(void* handle, double* out);
+int pfa3d_destroy(void* handle);
+
 /* ---- on-device FP64 field summary (src/alloy625.cpp:811-863) ---- */
 /* out[5] = mean x_Cr, mean x_Nb, f_gamma, f_delta, f_laves over the interior */
 int pfa_summarize(struct CudaData* dev, double* out);

@@ -1,0 +1,335 @@
+// pfa_grid3d.cu -- 3D grids behind an extern "C" handle API.
+//
+// The reference is 2D only (src/main.cpp:418-421) and its CudaData has no
+// third dimension, so 3D grids get their own handle: create from host fields
+// in the ghost-ring layout ((nz x ny x nx) doubles, one ghost cell on every
+// face), run n explicit steps (graph-replayed), read back, summarise.  The
+// equations are the 2D ones with a 7-point Laplacian (pfa_step3d.cu).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "pfa_gb300.h"
+#include "pfa_internal.h"
+#include "pfa_kernels.h"
+#include "pfa_reduce.h"
+
+namespace pfa {
+namespace {
+
+struct Graph {
+  int len;
+  cudaGraphExec_t exec;
+};
+
+struct Grid3D {
+  int Nx = 0, Ny = 0, Nz = 0, precision = PFA_FP64;
+  ModelConst m{};
+  FastCoef fk{};
+  cudaStream_t st = nullptr;
+  double* f64[2][4] = {};
+  float* A[2] = {};
+  float* B[2] = {};
+  int pitch32 = 0;
+  int cur = 0;
+  bool f32_live = false;
+  double* sum_partial = nullptr;
+  double* sum_out = nullptr;
+  std::vector<Graph> graphs;
+};
+
+int err(int code, const char* what) {
+  std::fprintf(stderr, "pfa_gb300: %s\n", what);
+  set_error(code, what);
+  return code;
+}
+
+int cuda_err(cudaError_t e, const char* what) {
+  char buf[256];
+  std::snprintf(buf, sizeof(buf), "%s: %s", what, cudaGetErrorString(e));
+  std::fprintf(stderr, "CUDA Runtime Error: %s\n", buf);
+  set_error(PFA_ECUDA, buf);
+  return PFA_ECUDA;
+}
+
+#define CK3(expr)                                          \
+  do {                                                     \
+    cudaError_t e_ = (expr);                               \
+    if (e_ != cudaSuccess) return cuda_err(e_, #expr);     \
+  } while (0)
+
+size_t ghost_cells(const Grid3D* g) { return size_t(g->Nx + 2) * (g->Ny + 2) * (g->Nz + 2); }
+
+Conv3DArgs conv(Grid3D* g) {
+  Conv3DArgs c{};
+  for (int k = 0; k < 4; k++) c.f64[k] = g->f64[0][k];
+  c.A = g->A[g->cur];
+  c.B = g->B[g->cur];
+  c.Nx = g->Nx;
+  c.Ny = g->Ny;
+  c.Nz = g->Nz;
+  c.pitch32 = g->pitch32;
+  return c;
+}
+
+Step3DArgs step_args(Grid3D* g) {
+  Step3DArgs a{};
+  a.Nx = g->Nx;
+  a.Ny = g->Ny;
+  a.Nz = g->Nz;
+  a.m = g->m;
+  a.k = g->fk;
+  const double dt = g->m.dt;
+  for (int i = 0; i < 2; i++)
+    for (int j = 0; j < 2; j++) a.dtD[i][j] = float(dt * g->m.D[i][j]);
+  for (int i = 0; i < 2; i++) {
+    a.dtL[i] = float(dt * g->m.L[i]);
+    a.om2[i] = float(2.0 * g->m.omega[i]);
+    a.kap[i] = float(g->m.kappa[i]);
+  }
+  a.alpha2 = float(2.0 * g->m.alpha);
+  for (int i = 0; i < 3; i++) a.idx2f[i] = float(g->m.idx2[i]);
+  return a;
+}
+
+int step(Grid3D* g) {
+  Step3DArgs a = step_args(g);
+  const int c = g->cur, n = 1 - c;
+  if (g->precision == PFA_FP64) {
+    for (int k = 0; k < 4; k++) {
+      a.in[k] = g->f64[c][k];
+      a.out[k] = g->f64[n][k];
+    }
+    a.pitch = g->Nx + 2;
+    CK3(launch_step3d(a, true, g->st));
+  } else {
+    a.in[0] = g->A[c];
+    a.in[1] = g->B[c];
+    a.out[0] = g->A[n];
+    a.out[1] = g->B[n];
+    a.pitch = g->pitch32;
+    CK3(launch_step3d(a, false, g->st));
+  }
+  g->cur = n;
+  return 0;
+}
+
+int ensure_live(Grid3D* g) {
+  if (g->precision == PFA_FP64 || g->f32_live) return 0;
+  g->cur = 0;
+  CK3(launch_import3d(conv(g), g->st));
+  g->f32_live = true;
+  return 0;
+}
+
+// latest FP64 state in f64[0] (FP64 form: copy if it sits in f64[1])
+int sync_f64(Grid3D* g) {
+  if (g->precision == PFA_FP64) {
+    if (g->cur == 1) {
+      const size_t n = ghost_cells(g) * sizeof(double);
+      for (int k = 0; k < 4; k++)
+        CK3(cudaMemcpyAsync(g->f64[0][k], g->f64[1][k], n, cudaMemcpyDeviceToDevice, g->st));
+      g->cur = 0;
+    }
+    return 0;
+  }
+  if (g->f32_live) CK3(launch_export3d(conv(g), g->st));
+  return 0;
+}
+
+int run(Grid3D* g, int nsteps) {
+  if (int r = ensure_live(g)) return r;
+  while (nsteps > 0) {
+    if (nsteps == 1) {
+      if (int r = step(g)) return r;
+      nsteps = 0;
+      break;
+    }
+    const int len = std::min(nsteps - nsteps % 2, 100);
+    cudaGraphExec_t exec = nullptr;
+    for (auto& e : g->graphs)
+      if (e.len == len) exec = e.exec;
+    if (!exec) {
+      const int cur0 = g->cur;
+      cudaGraph_t graph;
+      CK3(cudaStreamBeginCapture(g->st, cudaStreamCaptureModeThreadLocal));
+      int r = 0;
+      for (int k = 0; k < len && !r; k++) r = step(g);
+      const cudaError_t e = cudaStreamEndCapture(g->st, &graph);
+      if (r) return r;
+      if (e != cudaSuccess) return cuda_err(e, "cudaStreamEndCapture");
+      CK3(cudaGraphInstantiate(&exec, graph, 0));
+      cudaGraphDestroy(graph);
+      g->graphs.push_back({len, exec});
+      g->cur = cur0;  // an even count returns the ping-pong to where it was
+    }
+    CK3(cudaGraphLaunch(exec, g->st));
+    nsteps -= len;
+  }
+  return 0;
+}
+
+}  // namespace
+}  // namespace pfa
+
+using namespace pfa;
+
+extern "C" {
+
+int pfa3d_create(void** handle, int nx, int ny, int nz, const double* params, const double* dxyz,
+                 const double* conc_Cr, const double* conc_Nb, const double* phi_del,
+                 const double* phi_lav, int precision) {
+  if (!handle || !params || !dxyz || !conc_Cr || !conc_Nb || !phi_del || !phi_lav)
+    return err(PFA_EINVAL, "pfa3d_create: null argument");
+  if (nx < 3 || ny < 3 || nz < 3) return err(PFA_EINVAL, "pfa3d_create: grid smaller than 3^3");
+  if (precision != PFA_FP64 && precision != PFA_FP32)
+    return err(PFA_EINVAL, "pfa3d_create: 3D grids run in PFA_FP64 or PFA_FP32");
+  Grid3D* g = new Grid3D();
+  *handle = g;
+  g->Nx = nx - 2;
+  g->Ny = ny - 2;
+  g->Nz = nz - 2;
+  g->precision = precision;
+  for (int i = 0; i < 2; i++) {
+    g->m.D[0][i] = params[i];
+    g->m.D[1][i] = params[2 + i];
+    g->m.kappa[i] = params[4 + i];
+    g->m.omega[i] = params[6 + i];
+    g->m.L[i] = params[8 + i];
+  }
+  g->m.alpha = params[10];
+  g->m.dt = params[11];
+  for (int i = 0; i < 3; i++) g->m.idx2[i] = 1.0 / (dxyz[i] * dxyz[i]);
+  model_fast_coef(&g->fk);
+  static bool ready = false;
+  if (!ready) {
+    CK3(prepare_step3d());
+    ready = true;
+  }
+  CK3(cudaStreamCreateWithFlags(&g->st, cudaStreamNonBlocking));
+  const size_t n = ghost_cells(g);
+  const double* src[4] = {conc_Cr, conc_Nb, phi_del, phi_lav};
+  const int sets = precision == PFA_FP64 ? 2 : 1;
+  for (int b = 0; b < sets; b++)
+    for (int k = 0; k < 4; k++) CK3(cudaMalloc(reinterpret_cast<void**>(&g->f64[b][k]), n * sizeof(double)));
+  for (int k = 0; k < 4; k++)
+    CK3(cudaMemcpyAsync(g->f64[0][k], src[k], n * sizeof(double), cudaMemcpyHostToDevice, g->st));
+  if (precision == PFA_FP32) {
+    g->pitch32 = ((g->Nx + 31) / 32) * 32;
+    const size_t recs = size_t(g->pitch32) * g->Ny * g->Nz;
+    for (int b = 0; b < 2; b++) {
+      CK3(cudaMalloc(reinterpret_cast<void**>(&g->A[b]), recs * 16));
+      CK3(cudaMalloc(reinterpret_cast<void**>(&g->B[b]), recs * 8));
+      CK3(cudaMemsetAsync(g->A[b], 0, recs * 16, g->st));
+      CK3(cudaMemsetAsync(g->B[b], 0, recs * 8, g->st));
+    }
+  }
+  CK3(cudaMalloc(reinterpret_cast<void**>(&g->sum_partial), sizeof(double) * kSumBlocks * 5));
+  CK3(cudaMalloc(reinterpret_cast<void**>(&g->sum_out), sizeof(double) * 5));
+  CK3(cudaStreamSynchronize(g->st));
+  return 0;
+}
+
+int pfa3d_run(void* handle, int nsteps) {
+  Grid3D* g = static_cast<Grid3D*>(handle);
+  if (!g) return err(PFA_ESTATE, "pfa3d_run: null handle");
+  if (nsteps < 0) return err(PFA_EINVAL, "pfa3d_run: negative step count");
+  return run(g, nsteps);
+}
+
+int pfa3d_run_timed(void* handle, int nsteps, float* ms) {
+  Grid3D* g = static_cast<Grid3D*>(handle);
+  if (!g) return err(PFA_ESTATE, "pfa3d_run_timed: null handle");
+  if (int r = ensure_live(g)) return r;
+  cudaEvent_t a, b;
+  CK3(cudaEventCreate(&a));
+  CK3(cudaEventCreate(&b));
+  CK3(cudaEventRecord(a, g->st));
+  const int r = run(g, nsteps);
+  CK3(cudaEventRecord(b, g->st));
+  CK3(cudaEventSynchronize(b));
+  float t = 0.f;
+  CK3(cudaEventElapsedTime(&t, a, b));
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (ms) *ms = t;
+  return r;
+}
+
+int pfa3d_read(void* handle, double* conc_Cr, double* conc_Nb, double* phi_del, double* phi_lav) {
+  Grid3D* g = static_cast<Grid3D*>(handle);
+  if (!g) return err(PFA_ESTATE, "pfa3d_read: null handle");
+  if (int r = sync_f64(g)) return r;
+  double* dst[4] = {conc_Cr, conc_Nb, phi_del, phi_lav};
+  const size_t n = ghost_cells(g) * sizeof(double);
+  for (int k = 0; k < 4; k++)
+    if (dst[k]) CK3(cudaMemcpyAsync(dst[k], g->f64[0][k], n, cudaMemcpyDeviceToHost, g->st));
+  CK3(cudaStreamSynchronize(g->st));
+  return 0;
+}
+
+int pfa3d_upload(void* handle, const double* conc_Cr, const double* conc_Nb,
+                 const double* phi_del, const double* phi_lav) {
+  Grid3D* g = static_cast<Grid3D*>(handle);
+  if (!g) return err(PFA_ESTATE, "pfa3d_upload: null handle");
+  const double* src[4] = {conc_Cr, conc_Nb, phi_del, phi_lav};
+  const size_t n = ghost_cells(g) * sizeof(double);
+  for (int k = 0; k < 4; k++)
+    CK3(cudaMemcpyAsync(g->f64[0][k], src[k], n, cudaMemcpyHostToDevice, g->st));
+  g->cur = 0;
+  g->f32_live = false;
+  return 0;
+}
+
+int pfa3d_summarize(void* handle, double* out) {
+  Grid3D* g = static_cast<Grid3D*>(handle);
+  if (!g) return err(PFA_ESTATE, "pfa3d_summarize: null handle");
+  SumArgs a{};
+  if (g->precision == PFA_FP32 && g->f32_live) {
+    for (int k = 0; k < 4; k++) a.f[k] = g->A[g->cur] + k;
+    a.c[0] = g->B[g->cur];
+    a.c[1] = g->B[g->cur] + 1;
+    a.stride = 4;
+    a.cstride = 2;
+    a.is_f32 = 1;
+    a.compact = 1;
+    a.phi_fix = 1;
+    a.pitch = g->pitch32;
+  } else {
+    if (int r = sync_f64(g)) return r;
+    for (int k = 0; k < 4; k++) a.f[k] = g->f64[0][k];
+    a.stride = a.cstride = 1;
+    a.pitch = g->Nx + 2;
+  }
+  a.is3d = 1;
+  a.Nx = g->Nx;
+  a.Ny = g->Ny;
+  a.Nz = g->Nz;
+  a.partial = g->sum_partial;
+  a.out = g->sum_out;
+  CK3(launch_summarize(a, g->st));
+  CK3(cudaMemcpyAsync(out, g->sum_out, 5 * sizeof(double), cudaMemcpyDeviceToHost, g->st));
+  CK3(cudaStreamSynchronize(g->st));
+  return 0;
+}
+
+int pfa3d_destroy(void* handle) {
+  Grid3D* g = static_cast<Grid3D*>(handle);
+  if (!g) return 0;
+  if (g->st) cudaStreamSynchronize(g->st);
+  for (auto& e : g->graphs) cudaGraphExecDestroy(e.exec);
+  for (int b = 0; b < 2; b++) {
+    for (int k = 0; k < 4; k++) cudaFree(g->f64[b][k]);
+    cudaFree(g->A[b]);
+    cudaFree(g->B[b]);
+  }
+  cudaFree(g->sum_partial);
+  cudaFree(g->sum_out);
+  if (g->st) cudaStreamDestroy(g->st);
+  delete g;
+  return 0;
+}
+
+}  // extern "C"

@@ -62,6 +62,31 @@ cudaError_t prepare_step2d_f32();
 cudaError_t launch_import_f32(const ConvArgs& a, cudaStream_t s);
 cudaError_t launch_export_f32(const ConvArgs& a, cudaStream_t s);
 
+// Arguments of one 3D step (pfa_step3d.cu).  F64: in/out = four ghost-ring
+// arrays ((Nz+2) x (Ny+2) x pitch, pitch = Nx + 2); FP32 form: in[0]/out[0]
+// = float4 A records, in[1]/out[1] = float2 B records, Nz x Ny x pitch.
+struct Step3DArgs {
+  const void* in[4];
+  void* out[4];
+  int Nx, Ny, Nz, pitch;
+  int zrows;            // z planes per segment (set by the launcher)
+  ModelConst m;         // m.idx2 = 1/dx^2, 1/dy^2, 1/dz^2
+  FastCoef k;
+  float dtD[2][2], dtL[2], om2[2], alpha2, kap[2], idx2f[3];
+};
+
+struct Conv3DArgs {
+  double* f64[4];  // ghost-ring layout
+  float* A;        // float4 records
+  float* B;        // float2 records
+  int Nx, Ny, Nz, pitch32;
+};
+
+cudaError_t prepare_step3d();
+cudaError_t launch_step3d(Step3DArgs a, bool f64, cudaStream_t s);
+cudaError_t launch_import3d(const Conv3DArgs& a, cudaStream_t s);
+cudaError_t launch_export3d(const Conv3DArgs& a, cudaStream_t s);
+
 // compat-mode stages (pfa_stages.cu)
 cudaError_t launch_bc(double* f, int nx, int ny, cudaStream_t s);
 cudaError_t launch_fictitious(const StageArgs& a, cudaStream_t s);

@@ -1,0 +1,383 @@
+// pfa_step3d.cu -- 3D step with the 7-point Laplacian (sm_103a).
+//
+// The reference supports 2D only (src/main.cpp:418-421); this extends its
+// equations unchanged to a 7-point stencil with six-face zero-flux ghost
+// fill.  One kernel template serves both forms:
+//   F64: plain FP64, the reference's formulas, ghost-ring layout
+//        ((Nz+2) planes of (Ny+2) rows of Nx+2 doubles, one array per field);
+//   F32: the precision form (FP32 arithmetic, Kahan-compensated x_Cr, x_Nb,
+//        fixed-point phases) on interior-only records (pfa_step2d_f32.cu):
+//        A = float4 {x_Cr, x_Nb, phi_del, phi_lav}, B = float2 {c_Cr, c_Nb}.
+// A CTA of 16 warps covers 30 x-columns (lanes 1..30) by 14 y-rows (warps
+// 1..14) and streams along z; lanes 0 / 31 and warps 0 / 15 carry the
+// neighbour columns and rows.  x-neighbours come from shuffles, y-neighbours
+// from a shared plane double-buffered by z parity (one barrier per plane),
+// z-neighbours from a three-plane register window rotated by a 3x-unrolled
+// loop.
+#include <cstdint>
+#include <type_traits>
+
+#include "pfa_device.cuh"
+#include "pfa_kernels.h"
+
+namespace pfa {
+
+using namespace dev;
+
+namespace {
+
+constexpr int kW = 16;  // warps per CTA (y-rows including the 2 halo rows)
+constexpr int kRowsOut = kW - 2;
+constexpr int kCols = 30;  // output columns per warp
+
+template <class R>
+struct Nb3 {
+  R gcr, gnb, pd, pl;
+};
+
+template <class R>
+struct Raw3 {
+  R x, y, pd, pl;  // F32: pd / pl hold the fixed-point bits
+  float cx, cy;    // F32: Kahan compensations
+};
+
+__device__ __forceinline__ int add_sat3(int a, int b) {
+  int r;
+  asm("add.sat.s32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
+  return r;
+}
+
+__device__ __forceinline__ int phi_step3(int q, float inc) {
+  const int d = __float2int_rn(inc * kPhiScale);
+  return max(-kPhiQMax, min(kPhiQMax, add_sat3(q, d)));
+}
+
+// FP64 store of the interior cell (x, y, z) and of every ghost cell whose
+// nearest interior cell it is (the six-face fill; edges and corners take the
+// nearest interior cell).
+__device__ __forceinline__ void store64(double* f, const Step3DArgs& a, int x, int y, int z,
+                                        double v) {
+  int xs[3] = {x, 0, 0}, ys[3] = {y, 0, 0}, zs[3] = {z, 0, 0};
+  int nx = 1, ny = 1, nz = 1;
+  if (x == 0) xs[nx++] = -1;
+  if (x == a.Nx - 1) xs[nx++] = a.Nx;
+  if (y == 0) ys[ny++] = -1;
+  if (y == a.Ny - 1) ys[ny++] = a.Ny;
+  if (z == 0) zs[nz++] = -1;
+  if (z == a.Nz - 1) zs[nz++] = a.Nz;
+  for (int k = 0; k < nz; k++)
+    for (int j = 0; j < ny; j++)
+      for (int i = 0; i < nx; i++)
+        f[((long long)(zs[k] + 1) * (a.Ny + 2) + (ys[j] + 1)) * a.pitch + (xs[i] + 1)] = v;
+}
+
+template <bool F64>
+struct S3 {
+  using R = typename std::conditional<F64, double, float>::type;
+  const Step3DArgs& a;
+  int cx, cy;  // clamped column / row of this thread
+  bool out;    // this thread owns an output column and row
+
+  __device__ __forceinline__ long long cell(int z) const {
+    const int zz = min(max(z, 0), a.Nz - 1);
+    if (F64) return ((long long)(zz + 1) * (a.Ny + 2) + (cy + 1)) * a.pitch + (cx + 1);
+    return ((long long)zz * a.Ny + cy) * a.pitch + cx;
+  }
+
+  __device__ __forceinline__ Raw3<R> load(int z) const {
+    const long long i = cell(z);
+    Raw3<R> r;
+    if constexpr (F64) {
+      r.x = __ldg(static_cast<const double*>(a.in[0]) + i);
+      r.y = __ldg(static_cast<const double*>(a.in[1]) + i);
+      r.pd = __ldg(static_cast<const double*>(a.in[2]) + i);
+      r.pl = __ldg(static_cast<const double*>(a.in[3]) + i);
+      r.cx = r.cy = 0.f;
+    } else {
+      const float4 v = __ldg(static_cast<const float4*>(a.in[0]) + i);
+      const float2 c = __ldg(static_cast<const float2*>(a.in[1]) + i);
+      r.x = v.x;
+      r.y = v.y;
+      r.pd = v.z;
+      r.pl = v.w;
+      r.cx = c.x;
+      r.cy = c.y;
+    }
+    return r;
+  }
+
+  __device__ __forceinline__ R ph(R bits) const {
+    if constexpr (F64)
+      return bits;
+    else
+      return phi_of(__float_as_int(bits));
+  }
+
+  // gamma solve of one cell
+  __device__ __forceinline__ Nb3<R> solve(const Raw3<R>& r) const {
+    const R d = ph(r.pd), l = ph(r.pl);
+    if constexpr (F64) {
+      const double pD = p64(d), pL = p64(l), pG = 1.0 - pD - pL;
+      Poly64 m;
+      poly64(pD, pG, pL, m);
+      return Nb3<R>{fict64<0, 0>(r.x, r.y, m), fict64<0, 1>(r.x, r.y, m), d, l};
+    } else {
+      const FastCoef& K = a.k;
+      const float pD = p32(d), pL = p32(l), pG = p_gamma32(d, l, pD, pL);
+      const float m0 = pD * pD, m1 = pD * pG, m2 = pD * pL, m3 = pG * pG, m4 = pG * pL, m5 = pL * pL;
+      const float* q = K.den;
+      const float den =
+          fmaf(q[0], m0, fmaf(q[1], m1, fmaf(q[2], m2, fmaf(q[3], m3, fmaf(q[4], m4, q[5] * m5)))));
+      const float rr = __fdividef(1.0f, den);
+      float n[2];
+#pragma unroll
+      for (int c = 0; c < 2; c++) {
+        const float* k = K.num[c];
+        const float lx = fmaf(k[0], pD, fmaf(k[1], pG, k[2] * pL));
+        const float ly = fmaf(k[3], pD, fmaf(k[4], pG, k[5] * pL));
+        const float qq =
+            fmaf(k[6], m0, fmaf(k[7], m1, fmaf(k[8], m2, fmaf(k[9], m3, fmaf(k[10], m4, k[11] * m5)))));
+        n[c] = fmaf(r.x, lx, fmaf(r.y, ly, qq));
+      }
+      return Nb3<R>{n[0] * rr, n[1] * rr, d, l};
+    }
+  }
+
+  // update plane z of this thread's column from the window (up, c, dn)
+  __device__ __forceinline__ void update(int z, const Nb3<R>& up, const Nb3<R>& c,
+                                         const Nb3<R>& dn, const Raw3<R>& rc,
+                                         Nb3<R> (*sh)[kW][32]) const {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    Nb3<R>(*b)[32] = sh[z & 1];
+    b[w][lane] = c;
+    __syncthreads();  // buffer z&1 was last read two planes ago, before the previous barrier
+    const Nb3<R> s = b[max(w - 1, 0)][lane], n = b[min(w + 1, kW - 1)][lane];
+    Nb3<R> wv, e;
+    wv.gcr = __shfl_up_sync(0xffffffffu, c.gcr, 1);
+    wv.gnb = __shfl_up_sync(0xffffffffu, c.gnb, 1);
+    wv.pd = __shfl_up_sync(0xffffffffu, c.pd, 1);
+    wv.pl = __shfl_up_sync(0xffffffffu, c.pl, 1);
+    e.gcr = __shfl_down_sync(0xffffffffu, c.gcr, 1);
+    e.gnb = __shfl_down_sync(0xffffffffu, c.gnb, 1);
+    e.pd = __shfl_down_sync(0xffffffffu, c.pd, 1);
+    e.pl = __shfl_down_sync(0xffffffffu, c.pl, 1);
+    if (!out) return;
+    const ModelConst& M = a.m;
+    if constexpr (F64) {
+      // 7-point mask in the order z-1, y-1, x-1, centre, x+1, y+1, z+1
+      const double mx = M.idx2[0], my = M.idx2[1], mz = M.idx2[2], mc = -2. * (mx + my + mz);
+      auto lap = [&](double z0, double y0, double x0, double vc, double x1, double y1, double z1) {
+        double v = mz * z0;
+        v = fma(my, y0, v);
+        v = fma(mx, x0, v);
+        v = fma(mc, vc, v);
+        v = fma(mx, x1, v);
+        v = fma(my, y1, v);
+        return fma(mz, z1, v);
+      };
+      const double lapCr = lap(up.gcr, s.gcr, wv.gcr, c.gcr, e.gcr, n.gcr, dn.gcr);
+      const double lapNb = lap(up.gnb, s.gnb, wv.gnb, c.gnb, e.gnb, n.gnb, dn.gnb);
+      const double lapD = lap(up.pd, s.pd, wv.pd, c.pd, e.pd, n.pd, dn.pd);
+      const double lapL = lap(up.pl, s.pl, wv.pl, c.pl, e.pl, n.pl, dn.pl);
+      const double X = rc.x, Y = rc.y, pd = c.pd, pl = c.pl;
+      const double ocr = X + M.dt * (M.D[0][0] * lapCr + M.D[0][1] * lapNb);
+      const double onb = Y + M.dt * (M.D[1][0] * lapCr + M.D[1][1] * lapNb);
+      const double pD = p64(pd), pL = p64(pl), pG = 1.0 - pD - pL;
+      Poly64 m;
+      poly64(pD, pG, pL, m);
+      const double gcr = c.gcr, gnb = c.gnb;
+      const double gam = g64<0>(gcr, gnb);
+      const double dgCr = dg64<0>(gcr, gnb), dgNb = dg64<1>(gcr, gnb);
+      const double dCr = fict64<1, 0>(X, Y, m), dNb = fict64<1, 1>(X, Y, m);
+      const double gpd = gam - g64<1>(dCr, dNb) - dgCr * (gcr - dCr) - dgNb * (gnb - dNb);
+      const double dFd = -pp64(pd) * gpd + 2.0 * M.omega[0] * pd * (pd - 1.0) * (2.0 * pd - 1.0) +
+                         2.0 * M.alpha * pd * pl * pl - M.kappa[0] * lapD;
+      const double lCr = fict64<2, 0>(X, Y, m), lNb = fict64<2, 1>(X, Y, m);
+      const double gpl = gam - g64<2>(lCr, lNb) - dgCr * (gcr - lCr) - dgNb * (gnb - lNb);
+      const double dFl = -pp64(pl) * gpl + 2.0 * M.omega[1] * pl * (pl - 1.0) * (2.0 * pl - 1.0) +
+                         2.0 * M.alpha * pl * pd * pd - M.kappa[1] * lapL;
+      const int x = cx, y = cy;
+      store64(static_cast<double*>(a.out[0]), a, x, y, z, ocr);
+      store64(static_cast<double*>(a.out[1]), a, x, y, z, onb);
+      store64(static_cast<double*>(a.out[2]), a, x, y, z, pd - M.dt * M.L[0] * dFd);
+      store64(static_cast<double*>(a.out[3]), a, x, y, z, pl - M.dt * M.L[1] * dFl);
+    } else {
+      const float i2x = a.idx2f[0], i2y = a.idx2f[1], i2z = a.idx2f[2];
+      auto lap = [&](float z0, float y0, float x0, float vc, float x1, float y1, float z1) {
+        const float sx = (x0 - vc) + (x1 - vc);
+        const float sy = (y0 - vc) + (y1 - vc);
+        const float sz = (z0 - vc) + (z1 - vc);
+        return fmaf(sx, i2x, fmaf(sy, i2y, sz * i2z));
+      };
+      const float lapCr = lap(up.gcr, s.gcr, wv.gcr, c.gcr, e.gcr, n.gcr, dn.gcr);
+      const float lapNb = lap(up.gnb, s.gnb, wv.gnb, c.gnb, e.gnb, n.gnb, dn.gnb);
+      const float lapD = lap(up.pd, s.pd, wv.pd, c.pd, e.pd, n.pd, dn.pd);
+      const float lapL = lap(up.pl, s.pl, wv.pl, c.pl, e.pl, n.pl, dn.pl);
+      const float X = rc.x, Y = rc.y;
+      const float ycr = fmaf(a.dtD[0][0], lapCr, a.dtD[0][1] * lapNb) - rc.cx, tcr = X + ycr;
+      const float ynb = fmaf(a.dtD[1][0], lapCr, a.dtD[1][1] * lapNb) - rc.cy, tnb = Y + ynb;
+      const FastCoef& K = a.k;
+      const float u1 = c.gcr - K.xe_gam[0], u2 = c.gnb - K.xe_gam[1];
+      auto dF = [&](float p, float q, float dP, float om2) {
+        const float t = fmaf(-p, p, p);
+        const float pp = 30.0f * t * t;
+        const float well = p * fmaf(p, fmaf(2.0f * om2, p, -3.0f * om2), om2);
+        return fmaf(-pp, dP, fmaf(a.alpha2 * p, q * q, well));
+      };
+      const float dFd = fmaf(-a.kap[0], lapD, dF(c.pd, c.pl, quad2(K.dP[0], u1, u2), a.om2[0]));
+      const float dFl = fmaf(-a.kap[1], lapL, dF(c.pl, c.pd, quad2(K.dP[1], u1, u2), a.om2[1]));
+      const long long i = cell(z);
+      float4 o;
+      o.x = tcr;
+      o.y = tnb;
+      o.z = __int_as_float(phi_step3(__float_as_int(rc.pd), -a.dtL[0] * dFd));
+      o.w = __int_as_float(phi_step3(__float_as_int(rc.pl), -a.dtL[1] * dFl));
+      static_cast<float4*>(a.out[0])[i] = o;
+      static_cast<float2*>(a.out[1])[i] = make_float2((tcr - X) - ycr, (tnb - Y) - ynb);
+    }
+  }
+};
+
+template <bool F64>
+__global__ void __launch_bounds__(32 * kW) k_stream3d(Step3DArgs a) {
+  using R = typename S3<F64>::R;
+  __shared__ Nb3<R> sh[2][kW][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int x = blockIdx.x * kCols - 1 + lane;
+  const int y = blockIdx.y * kRowsOut - 1 + w;
+  const int z0 = blockIdx.z * a.zrows;
+  const int z1 = min(z0 + a.zrows, a.Nz);
+  const S3<F64> S{a, min(max(x, 0), a.Nx - 1), min(max(y, 0), a.Ny - 1),
+                  lane >= 1 && lane <= kCols && w >= 1 && w <= kRowsOut && x < a.Nx && y < a.Ny};
+  Raw3<R> r0 = S.load(z0), r1 = S.load(z0 + 1), r2;
+  Nb3<R> n0 = S.solve(S.load(z0 - 1)), n1 = S.solve(r0), n2;
+  int z = z0;
+  for (; z + 2 < z1; z += 3) {
+    r2 = S.load(z + 2);
+    n2 = S.solve(r1);
+    S.update(z, n0, n1, n2, r0, sh);
+    r0 = S.load(z + 3);
+    n0 = S.solve(r2);
+    S.update(z + 1, n1, n2, n0, r1, sh);
+    r1 = S.load(z + 4);
+    n1 = S.solve(r0);
+    S.update(z + 2, n2, n0, n1, r2, sh);
+  }
+  for (; z < z1; z++) {
+    r2 = S.load(z + 2);
+    n2 = S.solve(r1);
+    S.update(z, n0, n1, n2, r0, sh);
+    n0 = n1;
+    n1 = n2;
+    r0 = r1;
+    r1 = r2;
+  }
+}
+
+// FP64 ghost-ring fields <-> FP32 records (3D)
+__global__ void k_import3d(Conv3DArgs a) {
+  const long long n = (long long)a.Nx * a.Ny * a.Nz;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int x = int(t % a.Nx), y = int((t / a.Nx) % a.Ny), z = int(t / ((long long)a.Nx * a.Ny));
+    const long long i64 = ((long long)(z + 1) * (a.Ny + 2) + (y + 1)) * (a.Nx + 2) + (x + 1);
+    const long long r = ((long long)z * a.Ny + y) * a.pitch32 + x;
+    float4 v;
+    float2 c;
+    const double X = a.f64[0][i64], Y = a.f64[1][i64];
+    v.x = float(X);
+    v.y = float(Y);
+    c.x = float(double(v.x) - X);
+    c.y = float(double(v.y) - Y);
+    v.z = __int_as_float(phi_quantize(a.f64[2][i64]));
+    v.w = __int_as_float(phi_quantize(a.f64[3][i64]));
+    reinterpret_cast<float4*>(a.A)[r] = v;
+    reinterpret_cast<float2*>(a.B)[r] = c;
+  }
+}
+
+__global__ void k_export3d(Conv3DArgs a) {
+  const long long n = (long long)a.Nx * a.Ny * a.Nz;
+  Step3DArgs g{};
+  g.Nx = a.Nx;
+  g.Ny = a.Ny;
+  g.Nz = a.Nz;
+  g.pitch = a.Nx + 2;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int x = int(t % a.Nx), y = int((t / a.Nx) % a.Ny), z = int(t / ((long long)a.Nx * a.Ny));
+    const long long r = ((long long)z * a.Ny + y) * a.pitch32 + x;
+    const float4 v = reinterpret_cast<const float4*>(a.A)[r];
+    const float2 c = reinterpret_cast<const float2*>(a.B)[r];
+    store64(a.f64[0], g, x, y, z, double(v.x) - double(c.x));
+    store64(a.f64[1], g, x, y, z, double(v.y) - double(c.y));
+    store64(a.f64[2], g, x, y, z, double(__float_as_int(v.z)) * kPhiInvScaleD);
+    store64(a.f64[3], g, x, y, z, double(__float_as_int(v.w)) * kPhiInvScaleD);
+  }
+}
+
+// z planes per segment: fill whole waves of resident CTAs, two extra planes
+// of gamma solves per segment
+int segment_planes(int Nx, int Ny, int Nz, int resident) {
+  const long long cols = (long long)((Nx + kCols - 1) / kCols) * ((Ny + kRowsOut - 1) / kRowsOut);
+  int best = Nz;
+  double best_score = 0.0;
+  for (int waves = 1; waves <= 256; waves++) {
+    const long long segs = (long long)waves * resident / cols;
+    if (segs < 1) continue;
+    const int planes = int((Nz + segs - 1) / segs);
+    if (planes < 16 && segs > 1) break;
+    const long long used = cols * ((Nz + planes - 1) / planes);
+    const long long slots = ((used + resident - 1) / resident) * (long long)resident;
+    const double score = double(used) / double(slots) / (1.0 + 2.0 / planes);
+    if (score > best_score) {
+      best_score = score;
+      best = planes;
+    }
+  }
+  return best;
+}
+
+int g_resident3[2] = {0, 0};
+
+template <bool F64>
+cudaError_t query3() {
+  int dev = 0, sms = 0, per = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_stream3d<F64>, 32 * kW, 0);
+  g_resident3[F64] = sms * (per > 0 ? per : 1);
+  return e;
+}
+
+}  // namespace
+
+cudaError_t prepare_step3d() {
+  cudaError_t e = query3<true>();
+  return e == cudaSuccess ? query3<false>() : e;
+}
+
+cudaError_t launch_step3d(Step3DArgs a, bool f64, cudaStream_t s) {
+  const int resident = g_resident3[f64] > 0 ? g_resident3[f64] : 152;
+  a.zrows = segment_planes(a.Nx, a.Ny, a.Nz, resident);
+  dim3 grid((a.Nx + kCols - 1) / kCols, (a.Ny + kRowsOut - 1) / kRowsOut,
+            (a.Nz + a.zrows - 1) / a.zrows);
+  if (f64)
+    k_stream3d<true><<<grid, 32 * kW, 0, s>>>(a);
+  else
+    k_stream3d<false><<<grid, 32 * kW, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_import3d(const Conv3DArgs& a, cudaStream_t s) {
+  k_import3d<<<1024, 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_export3d(const Conv3DArgs& a, cudaStream_t s) {
+  k_export3d<<<1024, 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace pfa

@@ -85,6 +85,14 @@ def load():
                                   ctypes.POINTER(ctypes.c_uint32), _i]),
         "pfa_summarize_fields_noalloc": (_i, [ctypes.c_void_p] * 4 + [_i, _i, ctypes.c_void_p,
                                                                       ctypes.c_void_p]),
+        "pfa3d_create": (_i, [ctypes.POINTER(ctypes.c_void_p), _i, _i, _i, _dp, _dp, _dp, _dp,
+                              _dp, _dp, _i]),
+        "pfa3d_run": (_i, [ctypes.c_void_p, _i]),
+        "pfa3d_run_timed": (_i, [ctypes.c_void_p, _i, _fp]),
+        "pfa3d_read": (_i, [ctypes.c_void_p, _dp, _dp, _dp, _dp]),
+        "pfa3d_upload": (_i, [ctypes.c_void_p, _dp, _dp, _dp, _dp]),
+        "pfa3d_summarize": (_i, [ctypes.c_void_p, _dp]),
+        "pfa3d_destroy": (_i, [ctypes.c_void_p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -261,6 +269,64 @@ class Grid2D:
         if self._live:
             self._live = False
             check(self.L.pfa_free_cuda(self.ref), "free_cuda")
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def params_vector(p):
+    """The 12-double parameter block of pfa3d_create (pfa_model_params layout)."""
+    return np.array(list(p["D_Cr"]) + list(p["D_Nb"]) + list(p["kappa"]) + list(p["omega"]) +
+                    list(p["Lmob"]) + [p["alpha"], p["dt"]], dtype=np.float64)
+
+
+class Grid3D:
+    """One 3D grid (7-point Laplacian), fields (nz, ny, nx) with the ghost ring."""
+
+    def __init__(self, fields, params, precision="fp64"):
+        L = load()
+        self.L = L
+        f = [np.ascontiguousarray(a, dtype=np.float64) for a in fields]
+        self.shape = f[0].shape
+        nz, ny, nx = self.shape
+        self.params = dict(params)
+        self._pv = params_vector(params)
+        self._d = np.array([params["dx"], params.get("dy", params["dx"]),
+                            params.get("dz", params["dx"])], dtype=np.float64)
+        self.h = ctypes.c_void_p()
+        check(L.pfa3d_create(ctypes.byref(self.h), nx, ny, nz, _ptr(self._pv), _ptr(self._d),
+                             *[_ptr(a) for a in f], PRECISIONS[precision]), "pfa3d_create")
+        self._live = True
+
+    def run(self, nsteps):
+        check(self.L.pfa3d_run(self.h, int(nsteps)), "pfa3d_run")
+
+    def run_timed(self, nsteps):
+        ms = ctypes.c_float()
+        check(self.L.pfa3d_run_timed(self.h, int(nsteps), ctypes.byref(ms)), "pfa3d_run_timed")
+        return ms.value
+
+    def read(self):
+        out = [np.empty(self.shape) for _ in range(4)]
+        check(self.L.pfa3d_read(self.h, *[_ptr(a) for a in out]), "pfa3d_read")
+        return out
+
+    def upload(self, fields):
+        f = [np.ascontiguousarray(a, dtype=np.float64) for a in fields]
+        check(self.L.pfa3d_upload(self.h, *[_ptr(a) for a in f]), "pfa3d_upload")
+
+    def summarize(self):
+        out = np.zeros(5)
+        check(self.L.pfa3d_summarize(self.h, _ptr(out)), "pfa3d_summarize")
+        return out
+
+    def close(self):
+        if self._live:
+            self._live = False
+            check(self.L.pfa3d_destroy(self.h), "pfa3d_destroy")
 
     def __del__(self):
         try:

@@ -1,0 +1,100 @@
+"""3D grids (7-point Laplacian) on the GPU against the oracle's 3D step.
+
+The reference is 2D only; the oracle extends its equations unchanged to
+three dimensions (oracle/step_impl.h, step3d), and the 3D kernels are held
+to the same tolerances as the 2D ones: FP64 within 1e-12 of the oracle,
+the FP32 form within 1e-5 absolute of FP64.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import field_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _params(pfa):
+    return pfa.model_params(dim=3)
+
+
+@pytest.mark.parametrize("shape", [(1, 1, 1), (7, 3, 5), (12, 14, 20), (40, 9, 33)])
+def test_fp64_3d_matches_oracle(pfa, orc, shape):
+    from pfa_gb300 import ic
+    nz, ny, nx = shape
+    f = ic.grid3d(nx, ny, nz, seed=nx + 7 * ny + 31 * nz, slab=max(1, nx // 3),
+                  n_particles=2 if min(shape) >= 9 else 0, radius=3.0)
+    p = _params(pfa)
+    want = orc.run3d(f, O.model_params(dim=3), 30)
+    g = pfa.Grid3D(f, p)
+    g.run(30)
+    got = g.read()
+    g.close()
+    # compare interior + faces (edges/corners of the ghost ring are not read)
+    err = [np.max(np.abs(a[1:-1, 1:-1, 1:-1] - b[1:-1, 1:-1, 1:-1])) / np.max(np.abs(b[1:-1, 1:-1, 1:-1]))
+           for a, b in zip(got, want)]
+    assert max(err) <= 1e-12, err
+    for a in got:  # zero-flux faces mirror the interior
+        assert np.array_equal(a[0, 1:-1, 1:-1], a[1, 1:-1, 1:-1])
+        assert np.array_equal(a[1:-1, 1:-1, -1], a[1:-1, 1:-1, -2])
+
+
+def test_3d_uniform_in_z_equals_2d(pfa):
+    from pfa_gb300 import ic
+    f2 = ic.grid2d(45, 37, seed=4, stripe_width=9, n_particles=2, radius=4.0)
+    f3 = [np.repeat(a[None, :, :], 6, axis=0) for a in f2]
+    p = _params(pfa)
+    g2 = pfa.Grid2D(f2, p)
+    g2.run(40)
+    g3 = pfa.Grid3D(f3, p)
+    g3.run(40)
+    a2, a3 = g2.read(), g3.read()
+    for x, y in zip(a3, a2):
+        for z in range(1, 7):
+            assert np.max(np.abs(x[z, 1:-1, 1:-1] - y[1:-1, 1:-1])) <= 1e-12 * np.max(np.abs(y))
+    g2.close()
+    g3.close()
+
+
+def test_fp32_3d_error_against_fp64(pfa):
+    from pfa_gb300 import ic
+    f = ic.grid3d(64, 48, 40, seed=9, slab=16, n_particles=4, radius=5.0)
+    p = _params(pfa)
+    a = pfa.Grid3D(f, p, precision="fp32")
+    b = pfa.Grid3D(f, p)
+    a.run(300)
+    b.run(300)
+    fa, fb = a.read(), b.read()
+    err = [float(np.max(np.abs(x[1:-1, 1:-1, 1:-1] - y[1:-1, 1:-1, 1:-1]))) for x, y in zip(fa, fb)]
+    print("3D fp32 max field error after 300 steps", err)
+    assert max(err) <= 1e-5, err
+    sa, sb = a.summarize(), b.summarize()
+    np.testing.assert_allclose(sa[:2], sb[:2], rtol=0, atol=1e-9)
+    a.close()
+    b.close()
+
+
+def test_3d_summary_matches_oracle(pfa, orc):
+    from pfa_gb300 import ic
+    f = ic.grid3d(30, 20, 10, seed=10, slab=8, n_particles=2, radius=3.0)
+    g = pfa.Grid3D(f, _params(pfa))
+    np.testing.assert_allclose(g.summarize(), orc.summarize(f), rtol=1e-13)
+    g.run(5)
+    np.testing.assert_allclose(g.summarize(), orc.summarize(g.read()), rtol=1e-13)
+    g.close()
+
+
+def test_3d_graph_replay_equals_single_steps(pfa):
+    from pfa_gb300 import ic
+    f = ic.grid3d(33, 18, 12, seed=11, slab=8, n_particles=2, radius=3.0)
+    p = _params(pfa)
+    for prec in ("fp64", "fp32"):
+        a = pfa.Grid3D(f, p, precision=prec)
+        a.run(23)
+        b = pfa.Grid3D(f, p, precision=prec)
+        for _ in range(23):
+            b.run(1)
+        for x, y in zip(a.read(), b.read()):
+            assert np.array_equal(x, y), prec
+        a.close()
+        b.close()
