@@ -50,7 +50,7 @@ def test_3d_uniform_in_z_equals_2d(pfa):
     g3.run(40)
     a2, a3 = g2.read(), g3.read()
     for x, y in zip(a3, a2):
-        for z in range(1, 7):
+        for z in range(1, x.shape[0] - 1):
             assert np.max(np.abs(x[z, 1:-1, 1:-1] - y[1:-1, 1:-1])) <= 1e-12 * np.max(np.abs(y))
     g2.close()
     g3.close()
