@@ -157,6 +157,176 @@ def run_reference(args, ws, rank):
     print(json.dumps(line))
 
 
+BATCH_COUNT = 64
+BATCH_WORKLOAD = (f"batch of {BATCH_COUNT} 2D grids, sides log-uniform in [128, 2048] (seed 3), "
+                  f"per-grid matrix / enrichment compositions from the alloy ranges, dx=5nm, "
+                  f"zero-flux, 5-point Laplacian, KKS-stable dt; one launch per time step over "
+                  f"all grids; one bench step = {STEPS_PER_BENCH_STEP} time steps")
+GRID3D_SIDE = 512
+GRID3D_WORKLOAD = (f"single 3D grid {GRID3D_SIDE}^3, dx=5nm, enriched slab 64 thick + 32 spheres "
+                   f"R=6 (seeded), zero-flux, 7-point Laplacian, KKS-stable dt; one bench step = "
+                   f"{STEPS_PER_BENCH_STEP} time steps")
+
+
+def _line(args, ws, metric_value, t, workload, config, **extra):
+    line = {"metric": METRIC, "value": metric_value, "unit": "cell-updates/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": dict({"workload": workload}, **config)}
+    line.update(extra)
+    return line
+
+
+def bench_batch(args, ws, rank, local, barrier, max_over_ranks, pl, ic):
+    """The many-grids workload: all grids resident in one batch arena."""
+    sides = ic.batch_sides(BATCH_COUNT, seed=3 + 100 * rank)
+    fields = [ic.batch_grid(s, seed=1000 + k) for k, s in enumerate(sides)]
+    cells = sum(s * s for s in sides)
+    params = pl.model_params()
+    arena = sum(pl.Batch.footprint(f[0].shape) for f in fields) + (1 << 20)
+    b = pl.Batch(params, arena)
+    slots = [b.add(f) for f in fields]
+    tuned_ms = b.tune(reps=5)
+    launch = b.launch()
+    b.run(args.warmup * STEPS_PER_BENCH_STEP)
+    b.sync()
+    barrier()
+    with ClockSampler(local) as clk:
+        ms = b.run_timed(args.steps * STEPS_PER_BENCH_STEP)
+    barrier()
+    t = max_over_ranks(ms / 1e3)
+    value = ws * cells * STEPS_PER_BENCH_STEP * args.steps / t
+    if args.only == "value":
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": "cell-updates/s",
+                              "ms_per_step": 1e3 * t / args.steps, "partial": "value only"}))
+        b.close()
+        return
+    kms = b.run_timed(400) / 400
+    peak, peak_kind = measured_peak_hbm()
+    achieved = 48 * cells / (kms / 1e3) / 1e9
+    # one-at-a-time FP64 loop over the same grids (the single-grid FP64 step)
+    n64 = 10
+    t64 = 0.0
+    for f in fields:
+        g = pl.Grid2D(f, params, precision="fp64")
+        g.run(2)
+        t64 += g.run_timed(n64) / 1e3
+        g.close()
+    fp64_value = cells * n64 / t64
+    # stated error on the three largest grids after 400 steps
+    big = sorted(range(len(sides)), key=lambda k: -sides[k])[:3]
+    eb = pl.Batch(params, arena)
+    es = {k: eb.add(fields[k]) for k in big}
+    eb.run(400)
+    err = [0.0] * 4
+    for k in big:
+        g = pl.Grid2D(fields[k], params, precision="fp64")
+        g.run(400)
+        for i, (x, y) in enumerate(zip(eb.read(es[k]), g.read())):
+            err[i] = max(err[i], float(np.max(np.abs(x[1:-1, 1:-1] - y[1:-1, 1:-1]))))
+        g.close()
+    eb.close()
+    b.close()
+    # e2e: every bench step adds all grids from host memory, runs, reads them back
+    import torch
+    host = [[torch.from_numpy(a).pin_memory().numpy() for a in f] for f in fields]
+    outs = [[torch.empty(a.shape, dtype=torch.float64, pin_memory=True).numpy() for a in f]
+            for f in fields]
+    be = pl.Batch(params, arena)
+    be.set_launch(launch["rows"], launch["persistent"])
+
+    def e2e_step():
+        ss = [be.add(h) for h in host]
+        be.run(STEPS_PER_BENCH_STEP)
+        for s, o in zip(ss, outs):
+            be.read(s, o)
+        for s in ss:
+            be.remove(s)
+
+    e2e_step()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    barrier()
+    te = max_over_ranks(time.perf_counter() - t0)
+    be.close()
+    io = sum(4 * f[0].size * 8 for f in fields)
+    if rank == 0:
+        line = _line(args, ws, value, t, BATCH_WORKLOAD,
+                     {"grids": BATCH_COUNT, "cells": cells, "precision": "fp32",
+                      "launch": launch, "tuned_ms_per_step": tuned_ms,
+                      "l2": "inputs larger than L2 (FP32 state 48 B/cell, 2.3 GB)",
+                      "parallelism": f"replicas x{ws}"},
+                     fp64={"value": fp64_value, "unit": "cell-updates/s",
+                           "how": "one grid at a time, single-grid FP64 step",
+                           "speedup_fp32_over_fp64": value / ws / fp64_value},
+                     max_field_error={"vs": "fp64 GPU step", "steps": 400,
+                                      "grids": [sides[k] for k in big],
+                                      "x_Cr": err[0], "x_Nb": err[1], "phi_delta": err[2],
+                                      "phi_laves": err[3]},
+                     roofline={"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                               "frac": achieved / peak, "traffic": profiled_traffic("batch_f32_64"),
+                               "kernel": "k_batch_f32", "bytes_per_cell": 48, "kernel_ms": kms,
+                               "peak_kind": peak_kind},
+                     cpu_baseline=None,
+                     e2e={"value": ws * cells * STEPS_PER_BENCH_STEP * args.steps / te,
+                          "unit": "cell-updates/s", "h2d_bytes_per_step": io,
+                          "d2h_bytes_per_step": io},
+                     gpu_launches=args.steps * STEPS_PER_BENCH_STEP,
+                     clocks=clk.summary())
+        print(json.dumps(line))
+
+
+def bench_grid3d(args, ws, rank, local, barrier, max_over_ranks, pl, ic):
+    """The 3D workload, FP32 form vs the FP64 step."""
+    n = args.side or GRID3D_SIDE
+    fields = ic.grid3d(n, n, n, seed=4 + rank, slab=64, n_particles=32, radius=6.0)
+    params = pl.model_params(dim=3)
+    cells = n ** 3
+    g = pl.Grid3D(fields, params, precision="fp32")
+    g.run(args.warmup * STEPS_PER_BENCH_STEP)
+    barrier()
+    with ClockSampler(local) as clk:
+        ms = g.run_timed(args.steps * STEPS_PER_BENCH_STEP)
+    barrier()
+    t = max_over_ranks(ms / 1e3)
+    value = ws * cells * STEPS_PER_BENCH_STEP * args.steps / t
+    if args.only == "value":
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": "cell-updates/s",
+                              "ms_per_step": 1e3 * t / args.steps, "partial": "value only"}))
+        g.close()
+        return
+    kms = g.run_timed(50) / 50
+    g.close()
+    g64 = pl.Grid3D(fields, params, precision="fp64")
+    g64.run(2)
+    ms64 = g64.run_timed(6) / 6
+    g64.close()
+    peak, peak_kind = measured_peak_hbm()
+    achieved = 48 * cells / (kms / 1e3) / 1e9
+    if rank == 0:
+        workload = GRID3D_WORKLOAD if n == GRID3D_SIDE else GRID3D_WORKLOAD.replace(
+            f"{GRID3D_SIDE}^3", f"{n}^3")
+        line = _line(args, ws, value, t, workload,
+                     {"nx": n, "ny": n, "nz": n, "precision": "fp32",
+                      "l2": "inputs larger than L2 (FP32 state 6.4 GB)",
+                      "parallelism": f"replicas x{ws}"},
+                     fp64={"value": cells / (ms64 / 1e3), "unit": "cell-updates/s",
+                           "ms_per_step": ms64,
+                           "speedup_fp32_over_fp64": value / ws / (cells / (ms64 / 1e3))},
+                     roofline={"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                               "frac": achieved / peak, "traffic": profiled_traffic("step3d_f32_512"),
+                               "kernel": "k_stream3d", "bytes_per_cell": 48, "kernel_ms": kms,
+                               "peak_kind": peak_kind},
+                     cpu_baseline=None,
+                     gpu_launches=args.steps * STEPS_PER_BENCH_STEP,
+                     clocks=clk.summary())
+        print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -164,6 +334,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp32k"])
+    ap.add_argument("--workload", default="grid4096", choices=["grid4096", "batch64", "grid3d512"],
+                    help="grid4096: the headline single-grid workload; batch64 / grid3d512: "
+                         "the many-grids and 3D workloads")
+    ap.add_argument("--side", type=int, default=0,
+                    help="grid3d512 only: another cube side (smaller profiler captures)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--only", default="all", choices=["all", "value"],
                     help="'value': only the device-resident timed run (for profiler captures)")
@@ -208,6 +383,13 @@ def main():
         t = torch.tensor([x], dtype=torch.float64, device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
+
+    if args.workload != "grid4096":
+        fn = bench_batch if args.workload == "batch64" else bench_grid3d
+        fn(args, ws, rank, local, barrier, max_over_ranks, pl, ic)
+        if dist is not None:
+            dist.destroy_process_group()
+        return
 
     # ---- device-resident FP32 precision form (headline value) ----
     g = pl.Grid2D(fields, params, precision=args.precision)
@@ -308,7 +490,7 @@ def main():
                                 "phi_delta": err[2], "phi_laves": err[3]},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
-                         "kernel": "k_step2d_f32", "bytes_per_cell": bytes_per_cell,
+                         "kernel": "k_stream_f32", "bytes_per_cell": bytes_per_cell,
                          "kernel_ms": kms, "peak_kind": peak_kind},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": io_bytes,

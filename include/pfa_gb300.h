@@ -21,6 +21,7 @@
 #ifndef PFA_GB300_H
 #define PFA_GB300_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -124,6 +125,37 @@ int pfa3d_upload(void* handle, const double* conc_Cr, const double* conc_Nb,
                  const double* phi_del, const double* phi_lav);
 int pfa3d_summarize(void* handle, double* out);
 int pfa3d_destroy(void* handle);
+
+/* ---- batches of 2D grids (continuous batching) ----
+ * No counterpart in the reference, which runs one grid per process
+ * (src/main.cpp:285-321).  A batch owns a device arena of arena_bytes and
+ * steps every member grid with one launch per time step (FP32 form,
+ * fixed-point phases, 5-point Laplacian); all members share params (the 12
+ * doubles of pfa3d_create) and dxy = dx, dy.  Grids join (pfa_batch_add:
+ * fields in the reference layout, ny x nx doubles with the ghost ring;
+ * PFA_ENOMEM, not printed, when the arena has no room) and leave
+ * (pfa_batch_remove) between runs; slot ids are reused.  A member advances
+ * bit-for-bit as it would alone.  pfa_batch_footprint gives the arena bytes a
+ * grid takes.  pfa_batch_tune times the launch shapes (rows per segment,
+ * persistent or one warp per unit) on the current members without advancing
+ * them and keeps the fastest; pfa_batch_set_launch fixes one. */
+size_t pfa_batch_footprint(int nx, int ny);
+int pfa_batch_create(void** handle, const double* params, const double* dxy, size_t arena_bytes);
+int pfa_batch_add(void* handle, int nx, int ny, const double* conc_Cr, const double* conc_Nb,
+                  const double* phi_del, const double* phi_lav, int* slot);
+int pfa_batch_remove(void* handle, int slot);
+int pfa_batch_read(void* handle, int slot, double* conc_Cr, double* conc_Nb, double* phi_del,
+                   double* phi_lav);
+int pfa_batch_run(void* handle, int nsteps);
+int pfa_batch_run_timed(void* handle, int nsteps, float* ms);
+int pfa_batch_sync(void* handle);
+int pfa_batch_summarize(void* handle, int slot, double* out);
+int pfa_batch_tune(void* handle, int reps, float* best_ms);
+int pfa_batch_set_launch(void* handle, int rows, int persistent, int ctas);
+int pfa_batch_get_launch(void* handle, int* rows, int* persistent, int* ctas, int* units);
+int pfa_batch_info(void* handle, int* grids, size_t* used_bytes, size_t* arena_bytes);
+void* pfa_batch_stream(void* handle);
+int pfa_batch_destroy(void* handle);
 
 /* ---- on-device FP64 field summary (src/alloy625.cpp:811-863) ---- */
 /* out[5] = mean x_Cr, mean x_Nb, f_gamma, f_delta, f_laves over the interior */

@@ -56,9 +56,34 @@ struct StageArgs {
   double mask9[9];
 };
 
+// A batch of 2D grids in the FP32 form (fixed-point phases) stepped by one
+// launch.  Per grid: record buffers of both parities; per unit of work: one
+// warp strip (30 columns) over a row segment of one grid.
+struct BatchGrid {
+  float4* A[2];   // {x_Cr, x_Nb, phi_del, phi_lav} records, parity 0 / 1
+  float2* B[2];   // Kahan compensations
+  int Nx, Ny, pitch, pad;
+};
+struct BatchUnit {
+  int grid, x0, y0, y1;
+};
+struct BatchArgs {
+  const BatchGrid* grid;
+  const BatchUnit* unit;
+  int* counter;   // unit counters of parity 0 / 1, then the unit count
+  int units;      // one-warp-per-unit mode: units of this launch
+  int parity;     // records are read from parity, written to parity ^ 1
+  int persistent;
+};
+
 cudaError_t launch_step2d_f64(const Step2DArgs& a, cudaStream_t s);
 cudaError_t launch_step2d_f32(const Step2DArgs& a, cudaStream_t s);
 cudaError_t prepare_step2d_f32();
+// ctas: CTAs of a persistent launch (b.persistent), else one warp per unit
+cudaError_t launch_batch_f32(const Step2DArgs& a, const BatchArgs& b, int ctas, cudaStream_t s);
+int batch_resident_ctas();   // CTAs of k_batch_f32 resident on the device at once
+int batch_warps_per_cta();
+int batch_strip_cols();
 cudaError_t launch_import_f32(const ConvArgs& a, cudaStream_t s);
 cudaError_t launch_export_f32(const ConvArgs& a, cudaStream_t s);
 

@@ -171,23 +171,20 @@ struct Stream {
   }
 };
 
+// One warp updates the strip of output columns x0 .. x0+29 over rows
+// y0 .. y1-1 of one grid (the unit of work of both the single-grid and the
+// batched kernels).  Whole warp; x0 < Nx.
 template <bool FIX>
-__global__ void __launch_bounds__(32 * kWarps, 8) k_stream_f32(Step2DArgs a) {
+__device__ __forceinline__ void stream_strip(const Step2DArgs& a, const float4* Ain,
+                                             const CompT<FIX>* Bin, float4* Aout,
+                                             CompT<FIX>* Bout, int Nx, int Ny, int P, int x0,
+                                             int y0, int y1) {
   const int lane = threadIdx.x & 31;
-  const int strip = blockIdx.x * kWarps + (threadIdx.x >> 5);
-  const int x0 = strip * kCols;  // first output column of the strip
-  if (x0 >= a.Nx) return;        // whole warp leaves together
-  const int y0 = blockIdx.y * a.rows;
-  const int y1 = min(y0 + a.rows, a.Ny);
   const int gx = x0 - 1 + lane;  // lanes 0 and 31 hold the neighbour columns
-  const int cx = min(max(gx, 0), a.Nx - 1);
+  const int cx = min(max(gx, 0), Nx - 1);
   const FastCoef& K = a.k;
-  const Stream<FIX> S{a,
-                      static_cast<const float4*>(a.in[0]) + cx,
-                      static_cast<const CompT<FIX>*>(a.in[1]) + cx,
-                      static_cast<float4*>(a.out[0]) + cx,
-                      static_cast<CompT<FIX>*>(a.out[1]) + cx,
-                      a.Ny, a.pitch, lane >= 1 && lane <= kCols && gx < a.Nx};
+  const Stream<FIX> S{a, Ain + cx, Bin + cx, Aout + cx, Bout + cx,
+                      Ny, P, lane >= 1 && lane <= kCols && gx < Nx};
   auto solve_raw = [&](const Raw<FIX>& r) {
     return solve(K, r.a.x, r.a.y, phf<FIX>(r.a.z), phf<FIX>(r.a.w));
   };
@@ -215,6 +212,43 @@ __global__ void __launch_bounds__(32 * kWarps, 8) k_stream_f32(Step2DArgs a) {
     n1 = n2;
     r0 = r1;
     r1 = r2;
+  }
+}
+
+template <bool FIX>
+__global__ void __launch_bounds__(32 * kWarps, 8) k_stream_f32(Step2DArgs a) {
+  const int strip = blockIdx.x * kWarps + (threadIdx.x >> 5);
+  const int x0 = strip * kCols;  // first output column of the strip
+  if (x0 >= a.Nx) return;        // whole warp leaves together
+  const int y0 = blockIdx.y * a.rows;
+  stream_strip<FIX>(a, static_cast<const float4*>(a.in[0]),
+                    static_cast<const CompT<FIX>*>(a.in[1]), static_cast<float4*>(a.out[0]),
+                    static_cast<CompT<FIX>*>(a.out[1]), a.Nx, a.Ny, a.pitch, x0, y0,
+                    min(y0 + a.rows, a.Ny));
+}
+
+// ---- many grids in one launch ----
+// Warps claim units (grid, strip, row segment) of the batch's unit table
+// through an atomic counter (counter[parity]) until the unit count in
+// counter[2] is reached, so a captured launch stays valid while the table's
+// contents change.  The launch also zeroes the other parity's counter for the
+// next step, which stream order runs after this one.  A persistent launch
+// has one CTA per resident slot; the other shape has one warp per unit (and
+// leaves the balancing to the block scheduler).  Unit indices come only from
+// the counter: ptxas keeps this form within 64 registers without spills.
+__global__ void __launch_bounds__(32 * kWarps, 8) k_batch_f32(Step2DArgs a, BatchArgs b) {
+  const int p = b.parity;
+  if (blockIdx.x == 0 && threadIdx.x == 0) b.counter[p ^ 1] = 0;
+  const int units = b.counter[2];
+  for (;;) {
+    int u = 0;
+    if ((threadIdx.x & 31) == 0) u = atomicAdd(b.counter + p, 1);
+    u = __shfl_sync(0xffffffffu, u, 0);
+    if (u >= units) return;
+    const BatchUnit w = b.unit[u];
+    const BatchGrid& g = b.grid[w.grid];
+    stream_strip<true>(a, g.A[p], g.B[p], g.A[p ^ 1], g.B[p ^ 1], g.Nx, g.Ny, g.pitch, w.x0,
+                       w.y0, w.y1);
   }
 }
 
@@ -301,16 +335,16 @@ int segment_rows(int Nx, int Ny, int resident) {
   return best;
 }
 
-int g_resident[2] = {0, 0};  // resident CTAs of the two variants
+int g_resident[3] = {0, 0, 0};  // resident CTAs: the two variants, the batch kernel
 
-template <bool FIX>
-cudaError_t query_resident() {
+template <typename K>
+cudaError_t query_resident(K kernel, int slot) {
   int dev = 0, sms = 0, per = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (e == cudaSuccess)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_stream_f32<FIX>, 32 * kWarps, 0);
-  g_resident[FIX] = sms * (per > 0 ? per : 1);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, 32 * kWarps, 0);
+  g_resident[slot] = sms * (per > 0 ? per : 1);
   return e;
 }
 
@@ -332,9 +366,22 @@ cudaError_t launch_step2d_f32(const Step2DArgs& a, cudaStream_t s) {
 
 // occupancy of the FP32 kernels on the current device (outside any capture)
 cudaError_t prepare_step2d_f32() {
-  cudaError_t e = query_resident<true>();
-  return e == cudaSuccess ? query_resident<false>() : e;
+  cudaError_t e = query_resident(k_stream_f32<false>, 0);
+  if (e == cudaSuccess) e = query_resident(k_stream_f32<true>, 1);
+  if (e == cudaSuccess) e = query_resident(k_batch_f32, 2);
+  return e;
 }
+
+cudaError_t launch_batch_f32(const Step2DArgs& a, const BatchArgs& b, int ctas, cudaStream_t s) {
+  const int grid = b.persistent ? ctas : (b.units + kWarps - 1) / kWarps;
+  if (grid <= 0) return cudaSuccess;
+  k_batch_f32<<<grid, 32 * kWarps, 0, s>>>(a, b);
+  return cudaGetLastError();
+}
+
+int batch_resident_ctas() { return g_resident[2] > 0 ? g_resident[2] : 152 * 8; }
+int batch_warps_per_cta() { return kWarps; }
+int batch_strip_cols() { return kCols; }
 
 cudaError_t launch_import_f32(const ConvArgs& a, cudaStream_t s) {
   dim3 block(32, 8);

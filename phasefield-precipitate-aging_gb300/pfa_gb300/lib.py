@@ -93,6 +93,23 @@ def load():
         "pfa3d_upload": (_i, [ctypes.c_void_p, _dp, _dp, _dp, _dp]),
         "pfa3d_summarize": (_i, [ctypes.c_void_p, _dp]),
         "pfa3d_destroy": (_i, [ctypes.c_void_p]),
+        "pfa_batch_footprint": (ctypes.c_size_t, [_i, _i]),
+        "pfa_batch_create": (_i, [ctypes.POINTER(ctypes.c_void_p), _dp, _dp, ctypes.c_size_t]),
+        "pfa_batch_add": (_i, [ctypes.c_void_p, _i, _i, _dp, _dp, _dp, _dp,
+                               ctypes.POINTER(_i)]),
+        "pfa_batch_remove": (_i, [ctypes.c_void_p, _i]),
+        "pfa_batch_read": (_i, [ctypes.c_void_p, _i, _dp, _dp, _dp, _dp]),
+        "pfa_batch_run": (_i, [ctypes.c_void_p, _i]),
+        "pfa_batch_run_timed": (_i, [ctypes.c_void_p, _i, _fp]),
+        "pfa_batch_sync": (_i, [ctypes.c_void_p]),
+        "pfa_batch_summarize": (_i, [ctypes.c_void_p, _i, _dp]),
+        "pfa_batch_tune": (_i, [ctypes.c_void_p, _i, _fp]),
+        "pfa_batch_set_launch": (_i, [ctypes.c_void_p, _i, _i, _i]),
+        "pfa_batch_get_launch": (_i, [ctypes.c_void_p] + [ctypes.POINTER(_i)] * 4),
+        "pfa_batch_info": (_i, [ctypes.c_void_p, ctypes.POINTER(_i),
+                                ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)]),
+        "pfa_batch_stream": (ctypes.c_void_p, [ctypes.c_void_p]),
+        "pfa_batch_destroy": (_i, [ctypes.c_void_p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -327,6 +344,103 @@ class Grid3D:
         if self._live:
             self._live = False
             check(self.L.pfa3d_destroy(self.h), "pfa3d_destroy")
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+ENOMEM = 5
+
+
+class Batch:
+    """Many 2D grids (FP32 form) stepped together by one launch per step.
+
+    ``add`` returns a slot id, or None when the arena has no room for the grid
+    (the admission refusal); ``remove`` frees the slot between runs."""
+
+    def __init__(self, params, arena_bytes):
+        L = load()
+        self.L = L
+        self.params = dict(params)
+        self._pv = params_vector(params)
+        self._d = np.array([params["dx"], params.get("dy", params["dx"])], dtype=np.float64)
+        self.h = ctypes.c_void_p()
+        check(L.pfa_batch_create(ctypes.byref(self.h), _ptr(self._pv), _ptr(self._d),
+                                 int(arena_bytes)), "pfa_batch_create")
+        self.shapes = {}
+        self._live = True
+
+    @staticmethod
+    def footprint(shape):
+        ny, nx = shape
+        return int(load().pfa_batch_footprint(nx, ny))
+
+    def add(self, fields):
+        f = [np.ascontiguousarray(a, dtype=np.float64) for a in fields]
+        ny, nx = f[0].shape
+        slot = _i()
+        rc = self.L.pfa_batch_add(self.h, nx, ny, *[_ptr(a) for a in f], ctypes.byref(slot))
+        if rc == ENOMEM:
+            return None
+        check(rc, "pfa_batch_add")
+        self.shapes[slot.value] = (ny, nx)
+        return slot.value
+
+    def remove(self, slot):
+        check(self.L.pfa_batch_remove(self.h, slot), "pfa_batch_remove")
+        self.shapes.pop(slot, None)
+
+    def read(self, slot, out=None):
+        out = out or [np.empty(self.shapes[slot]) for _ in range(4)]
+        check(self.L.pfa_batch_read(self.h, slot, *[_ptr(a) for a in out]), "pfa_batch_read")
+        return out
+
+    def run(self, nsteps):
+        check(self.L.pfa_batch_run(self.h, int(nsteps)), "pfa_batch_run")
+
+    def run_timed(self, nsteps):
+        ms = ctypes.c_float()
+        check(self.L.pfa_batch_run_timed(self.h, int(nsteps), ctypes.byref(ms)),
+              "pfa_batch_run_timed")
+        return ms.value
+
+    def sync(self):
+        check(self.L.pfa_batch_sync(self.h), "pfa_batch_sync")
+
+    def summarize(self, slot):
+        out = np.zeros(5)
+        check(self.L.pfa_batch_summarize(self.h, slot, _ptr(out)), "pfa_batch_summarize")
+        return out
+
+    def tune(self, reps=10):
+        ms = ctypes.c_float()
+        check(self.L.pfa_batch_tune(self.h, reps, ctypes.byref(ms)), "pfa_batch_tune")
+        return ms.value
+
+    def set_launch(self, rows, persistent, ctas=0):
+        check(self.L.pfa_batch_set_launch(self.h, rows, int(persistent), ctas),
+              "pfa_batch_set_launch")
+
+    def launch(self):
+        v = [_i() for _ in range(4)]
+        check(self.L.pfa_batch_get_launch(self.h, *[ctypes.byref(x) for x in v]),
+              "pfa_batch_get_launch")
+        return {"rows": v[0].value, "persistent": bool(v[1].value), "ctas": v[2].value,
+                "units": v[3].value}
+
+    def info(self):
+        n, used, cap = _i(), ctypes.c_size_t(), ctypes.c_size_t()
+        check(self.L.pfa_batch_info(self.h, ctypes.byref(n), ctypes.byref(used),
+                                    ctypes.byref(cap)), "pfa_batch_info")
+        return {"grids": n.value, "used_bytes": used.value, "arena_bytes": cap.value}
+
+    def close(self):
+        if self._live:
+            self._live = False
+            check(self.L.pfa_batch_destroy(self.h), "pfa_batch_destroy")
 
     def __del__(self):
         try:

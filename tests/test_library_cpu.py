@@ -12,7 +12,7 @@ from conftest import GOLDEN, ROOT
 
 def _declared_c_functions():
     src = open(os.path.join(ROOT, "include", "pfa_gb300.h")).read()
-    return sorted(set(re.findall(r"\b(pfa_[a-z0-9_]+)\s*\(", src)))
+    return sorted(set(re.findall(r"\b(pfa[0-9a-z]*_[a-z0-9_]+)\s*\(", src)))
 
 
 def _exported(path):
@@ -23,7 +23,8 @@ def _exported(path):
 
 def test_library_exports_c_abi(pfa):
     names = _declared_c_functions()
-    assert len(names) > 30
+    assert len(names) > 50
+    assert "pfa3d_create" in names and "pfa_batch_create" in names
     L = pfa.load()
     for n in names:
         assert hasattr(L, n), n
@@ -35,6 +36,17 @@ def test_library_exports_reference_cxx_abi(pfa):
     missing = [s for s in want if s not in have]
     assert not missing, missing
     assert len(want) == 14
+
+
+def test_batch_footprint_host_side(pfa):
+    """Arena bytes of one batched grid: records of 32-aligned rows, 48 bytes
+    per cell over both parities, rounded to 256 bytes (no GPU needed)."""
+    L = pfa.load()
+    for nx, ny in [(3, 3), (34, 66), (130, 130), (2050, 2050), (4098, 17)]:
+        pitch = (nx - 2 + 31) // 32 * 32
+        want = (pitch * (ny - 2) * 48 + 255) // 256 * 256
+        assert L.pfa_batch_footprint(nx, ny) == want
+    assert L.pfa_batch_footprint(2, 10) == 0
 
 
 def test_model_params_match_oracle(pfa):
