@@ -327,6 +327,86 @@ def bench_grid3d(args, ws, rank, local, barrier, max_over_ranks, pl, ic):
         print(json.dumps(line))
 
 
+SERVE_COUNT = 24
+SERVE_WORKLOAD = (f"serving trace of {SERVE_COUNT} requests (seed 5): Poisson arrivals 20/s, size "
+                  f"uniform over {{256^2, 1024^2, 4096^2, 128^3, 256^3}}, steps uniform in "
+                  f"[2000, 20000], compositions from the alloy ranges; FP32 form, continuous "
+                  f"batching (2D grids in one batch, 3D grids on their own streams), FIFO "
+                  f"admission by device footprint; one bench step = the whole trace")
+
+
+def bench_serve(args, ws, rank, local, barrier, max_over_ranks, pl, ic):
+    """Latency and aggregate throughput of the serving layer on a request trace."""
+    from pfa_gb300.serve import GpuBackend, Request, Server, fifo_latencies, latency_stats
+    args.steps = 1  # the whole trace is the one timed step
+    trace = ic.serve_trace(SERVE_COUNT, seed=5 + 100 * rank)
+    reqs = [Request(t["rid"], ic.serve_fields(t), t["steps"], t["arrival"]) for t in trace]
+    work = sum(r.cells * r.steps for r in reqs)
+    p2, p3 = pl.model_params(), pl.model_params(dim=3)
+    arena = 48 << 30
+    budget3 = 48 << 30
+
+    def serve_once(realtime=True):
+        be = GpuBackend(pl, p2, p3, arena, budget3)
+        srv = Server(be, tick_steps=STEPS_PER_BENCH_STEP)
+        done = srv.run_trace(reqs, realtime=realtime)
+        be.close()
+        return done, srv
+
+    # warm-up: the same trace scaled down to 300 steps per request
+    warm = [Request(r.rid, r.fields, 300, 0.0) for r in reqs[:8]]
+    for _ in range(max(1, args.warmup // 3)):
+        be = GpuBackend(pl, p2, p3, arena, budget3)
+        Server(be, tick_steps=STEPS_PER_BENCH_STEP).run_trace(warm, realtime=False)
+        be.close()
+    barrier()
+    with ClockSampler(local) as clk:
+        done, srv = serve_once()
+    barrier()
+    span = max(r.finished for r in done) - min(r.req.arrival for r in done)
+    t = max_over_ranks(span)
+    value = ws * work / t
+    stats = latency_stats(done)
+    # one-at-a-time FP64: each request's FP64 step time measured on a sample,
+    # queueing in arrival order computed from those service times
+    service = []
+    for r in reqs:
+        t0 = time.perf_counter()
+        if r.dim == 2:
+            g = pl.Grid2D(r.fields, p2, precision="fp64")
+        else:
+            g = pl.Grid3D(r.fields, p3, precision="fp64")
+        g.run(2)
+        sample = 10 if r.cells > 4e6 else 40
+        ms = g.run_timed(sample) / sample
+        g.read()
+        g.close()
+        setup = time.perf_counter() - t0 - 1e-3 * ms * (sample + 2)
+        service.append(max(0.0, setup) + 1e-3 * ms * r.steps)
+    arr = [r.arrival for r in reqs]
+    lat64 = fifo_latencies(arr, service)
+    span64 = max(a + l for a, l in zip(arr, lat64)) - min(arr)
+    if rank == 0:
+        line = _line(args, ws, value, t, SERVE_WORKLOAD,
+                     {"requests": SERVE_COUNT, "cell_updates": work, "precision": "fp32",
+                      "tick_steps": STEPS_PER_BENCH_STEP, "ticks": srv.ticks,
+                      "budget_bytes": {"2d_arena": arena, "3d": budget3},
+                      "l2": "inputs larger than L2",
+                      "parallelism": f"replicas x{ws}"},
+                     latency=dict(stats, unit="s", what="arrival to result read back"),
+                     fp64={"value": work / span64, "unit": "cell-updates/s",
+                           "how": "one request at a time in arrival order, FP64 step; service "
+                                  "times from measured per-request step times",
+                           "p50_s": float(np.percentile(lat64, 50)),
+                           "p99_s": float(np.percentile(lat64, 99))},
+                     cpu_baseline=None,
+                     e2e={"value": value, "unit": "cell-updates/s",
+                          "h2d_bytes_per_step": sum(4 * r.fields[0].size * 8 for r in reqs),
+                          "d2h_bytes_per_step": sum(4 * r.fields[0].size * 8 for r in reqs)},
+                     clocks=clk.summary())
+        print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -334,7 +414,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp32k"])
-    ap.add_argument("--workload", default="grid4096", choices=["grid4096", "batch64", "grid3d512"],
+    ap.add_argument("--workload", default="grid4096",
+                    choices=["grid4096", "batch64", "grid3d512", "serve"],
                     help="grid4096: the headline single-grid workload; batch64 / grid3d512: "
                          "the many-grids and 3D workloads")
     ap.add_argument("--side", type=int, default=0,
@@ -385,7 +466,7 @@ def main():
         return float(t.item())
 
     if args.workload != "grid4096":
-        fn = bench_batch if args.workload == "batch64" else bench_grid3d
+        fn = {"batch64": bench_batch, "grid3d512": bench_grid3d, "serve": bench_serve}[args.workload]
         fn(args, ws, rank, local, barrier, max_over_ranks, pl, ic)
         if dist is not None:
             dist.destroy_process_group()

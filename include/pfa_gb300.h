@@ -115,15 +115,20 @@ int pfa_last_nucleation_events(struct CudaData* dev, int64_t* cells, int32_t* ph
  * kappa[2], omega[2], Lmob[2], alpha, dt (12 doubles, the layout of
  * pfa_model_params' output); dxyz = dx, dy, dz; precision PFA_FP64 or
  * PFA_FP32.  The handle owns its device buffers and stream. */
+/* device bytes of the field buffers pfa3d_create allocates (host-side) */
+size_t pfa3d_footprint(int nx, int ny, int nz, int precision);
 int pfa3d_create(void** handle, int nx, int ny, int nz, const double* params, const double* dxyz,
                  const double* conc_Cr, const double* conc_Nb, const double* phi_del,
                  const double* phi_lav, int precision);
 int pfa3d_run(void* handle, int nsteps);
 int pfa3d_run_timed(void* handle, int nsteps, float* ms);
+int pfa3d_sync(void* handle);  /* wait for the handle's enqueued work */
 int pfa3d_read(void* handle, double* conc_Cr, double* conc_Nb, double* phi_del, double* phi_lav);
 int pfa3d_upload(void* handle, const double* conc_Cr, const double* conc_Nb,
                  const double* phi_del, const double* phi_lav);
 int pfa3d_summarize(void* handle, double* out);
+/* free energy as pfa_summarize_energy, dV = dx dy dz, gradients in 3D */
+int pfa3d_summarize_energy(void* handle, double Omega, double* energy);
 int pfa3d_destroy(void* handle);
 
 /* ---- batches of 2D grids (continuous batching) ----
@@ -176,6 +181,15 @@ int pfa_summarize(struct CudaData* dev, double* out);
 int pfa_summarize_fields_noalloc(const double* conc_Cr, const double* conc_Nb,
                                  const double* phi_del, const double* phi_lav, int nx, int ny,
                                  double* out, void* stream);
+
+/* ---- on-device FP64 free energy (summarize_energy, src/alloy625.cpp:865-919,
+ * with gibbs :752-786 and maskedgradient :788-807) ----
+ * *energy = sum over interior nodes of dV (g(x, phi) + sum_i kappa_i |grad phi_i|^2),
+ * dV = dx dy, Omega the three-phase coefficient (src/parameters.h:37);
+ * chem_nrg / grad_nrg (ny x nx, optional, NULL to skip) receive the per-node
+ * terms like the reference's host.chem_nrg / grad_nrg (ghost ring 0). */
+int pfa_summarize_energy(struct CudaData* dev, double dx, double dy, double Omega, double* energy,
+                         double* chem_nrg, double* grad_nrg);
 
 /* ---- model helpers ---- */
 /* out[13]: D_Cr[2], D_Nb[2], kappa[2], omega[2], Lmob[2], alpha, dt, rho(D J).

@@ -115,6 +115,10 @@ class Oracle:
         self._sum3d = getattr(L, P + "summarize3d")
         self._sum3d.restype = None
         self._sum3d.argtypes = [ctypes.POINTER(_dbl_p), i, i, i, _dbl_p]
+        self._energy2d = getattr(L, P + "energy2d")
+        self._energy2d.restype = ctypes.c_double
+        self._energy2d.argtypes = [ctypes.POINTER(_dbl_p), i, i, ctypes.c_double, ctypes.c_double,
+                                   _dbl_p, _dbl_p, ctypes.c_double, _dbl_p, _dbl_p]
 
     # ---- pointwise (vectorised by np.frompyfunc-free loops: small inputs only) ----
     def p(self, x):
@@ -181,6 +185,19 @@ class Oracle:
         events = [(ev[k].cell, ev[k].phase, ev[k].xcr, ev[k].xnb, ev[k].r_precip)
                   for k in range(min(n, max_events))]
         return a, events, n
+
+    def energy2d(self, fields, dx, dy, kappa, omega, Omega, maps=False):
+        """Total free energy (and the per-node chemical / gradient maps),
+        src/alloy625.cpp:752-807,865-919."""
+        arrs, pa = self._arr4(fields)
+        ny, nx = arrs[0].shape
+        k = np.ascontiguousarray(kappa, dtype=np.float64)
+        w = np.ascontiguousarray(omega, dtype=np.float64)
+        chem = np.zeros((ny, nx)) if maps else None
+        grad = np.zeros((ny, nx)) if maps else None
+        e = self._energy2d(pa, nx, ny, dx, dy, _ptr(k), _ptr(w), Omega,
+                           _ptr(chem) if maps else None, _ptr(grad) if maps else None)
+        return (e, chem, grad) if maps else e
 
     def summarize(self, fields):
         arrs, pa = self._arr4(fields)

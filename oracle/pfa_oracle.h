@@ -98,6 +98,11 @@ int orc_nucleation2d(double* f[4], int nx, int ny, const orc_nuc_params* np,
 void orc_summarize2d(const double* f[4], int nx, int ny, double out[5]);
 void orc_summarize3d(const double* f[4], int nx, int ny, int nz, double out[5]);
 
+/* ---- free energy (src/alloy625.cpp:752-807,865-919) ---- */
+double orc_energy2d(const double* f[4], int nx, int ny, double dx, double dy,
+                    const double kappa[2], const double omega[2], double Omega,
+                    double* chem, double* grad);
+
 #ifdef __cplusplus
 }
 #endif

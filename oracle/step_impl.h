@@ -417,3 +417,58 @@ void SFN(summarize3d)(const double* f[4], int nx, int ny, int nz, double out[5])
 {
 	SFN(summarize_range)(f, nx, ny, nz, 1, out);
 }
+
+/* Free energy of the grid, src/alloy625.cpp:752-786 (gibbs), :788-807
+ * (maskedgradient) and :865-919 (summarize_energy), 2D: per interior node
+ *   chem = dV * ( pGam g_gam(x^gam) + pDel g_del(x^del) + pLav g_lav(x^lav)
+ *                 + sum_i omega_i phi_i^2 (1 - phi_i)^2
+ *                 + 2 Omega phi_del^2 phi_lav^2 )
+ *   grad = dV * sum_i kappa_i |grad phi_i|^2, central differences
+ *          (phi(x+1) - phi(x-1)) / (2 dx) reading the ghost ring at the edges,
+ * dV = dx dy.  chem / grad (nx*ny, optional) receive the per-node values at
+ * the node's index (ghost ring untouched); returns the sum over the nodes of
+ * chem + grad, accumulated in row-major order. */
+double SFN(energy2d)(const double* f[4], int nx, int ny, double dx, double dy,
+                     const double kappa[2], const double omega[2], double Omega,
+                     double* chem, double* grad)
+{
+	const double dV = dx * dy;
+	const double wx = 1.0 / (2.0 * dx), wy = 1.0 / (2.0 * dy);
+	double energy = 0.0;
+	for (int y = 1; y < ny - 1; y++)
+		for (int x = 1; x < nx - 1; x++) {
+			const size_t i = (size_t)y * nx + x;
+			const double xCr = f[0][i], xNb = f[1][i];
+			const double phi[2] = {f[2][i], f[3][i]};
+			const double pDel = E_P(phi[0]);
+			const double pLav = E_P(phi[1]);
+			const double pGam = 1.0 - pDel - pLav;
+			const double gCr = E_FICT_GAM_CR(xCr, xNb, pDel, pGam, pLav);
+			const double gNb = E_FICT_GAM_NB(xCr, xNb, pDel, pGam, pLav);
+			const double dCr = E_FICT_DEL_CR(xCr, xNb, pDel, pGam, pLav);
+			const double dNb = E_FICT_DEL_NB(xCr, xNb, pDel, pGam, pLav);
+			const double lCr = E_FICT_LAV_CR(xCr, xNb, pDel, pGam, pLav);
+			const double lNb = E_FICT_LAV_NB(xCr, xNb, pDel, pGam, pLav);
+			const double sq[2] = {phi[0] * phi[0], phi[1] * phi[1]};
+			double g = pGam * E_G_GAM(gCr, gNb);
+			g += pDel * E_G_DEL(dCr, dNb);
+			g += pLav * E_G_LAV(lCr, lNb);
+			for (int k = 0; k < 2; k++) {
+				const double u = 1.0 - phi[k];
+				g += omega[k] * sq[k] * (u * u);
+			}
+			g += 2.0 * Omega * sq[0] * sq[1];
+			double ge = 0.0;
+			for (int k = 0; k < 2; k++) {
+				const double* p = f[2 + k];
+				const double gx = wx * (p[i + 1] - p[i - 1]);
+				const double gy = wy * (p[i + nx] - p[i - nx]);
+				ge += kappa[k] * (gx * gx + gy * gy);
+			}
+			const double c = g * dV, e = ge * dV;
+			if (chem) chem[i] = c;
+			if (grad) grad[i] = e;
+			energy += c + e;
+		}
+	return energy;
+}

@@ -97,6 +97,7 @@ struct State {
   unsigned long long* call_dev = nullptr;
   double* sum_partial = nullptr;
   double* sum_out = nullptr;
+  double* nrg_map[2] = {};  // per-node chemical / gradient energy (on request)
   std::vector<GraphEntry> graphs;
 };
 
@@ -624,6 +625,8 @@ static int free_core(CudaData* dev) {
   cudaFree(s->call_dev);
   cudaFree(s->sum_partial);
   cudaFree(s->sum_out);
+  cudaFree(s->nrg_map[0]);
+  cudaFree(s->nrg_map[1]);
   cudaStream_t st[4] = {dev->str_A, dev->str_B, dev->str_C, dev->str_D};
   for (auto x : st)
     if (x) cudaStreamDestroy(x);
@@ -1052,6 +1055,49 @@ int pfa_summarize(struct CudaData* dev, double* out) {
   a.out = s->sum_out;
   CK(launch_summarize(a, s->st));
   CK(cudaMemcpyAsync(out, s->sum_out, 5 * sizeof(double), cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  return 0;
+}
+
+int pfa_summarize_energy(struct CudaData* dev, double dx, double dy, double Omega, double* energy,
+                         double* chem_nrg, double* grad_nrg) {
+  State* s = lookup(dev);
+  if (!s) return fail(PFA_ESTATE, "pfa_summarize_energy: unknown CudaData");
+  if (!energy || !(dx > 0.0) || !(dy > 0.0))
+    return fail(PFA_EINVAL, "pfa_summarize_energy: needs energy and dx, dy > 0");
+  if (int r = f32_export(dev, s)) return r;
+  const size_t n = size_t(s->nx) * s->ny;
+  double* want[2] = {chem_nrg, grad_nrg};
+  for (int k = 0; k < 2; k++)
+    if (want[k] && !s->nrg_map[k]) {
+      if (alloc_field(&s->nrg_map[k], n)) return PFA_ECUDA;
+      CK(cudaMemsetAsync(s->nrg_map[k], 0, n * sizeof(double), s->st));
+    }
+  EnergyArgs a{};
+  a.f[0] = dev->conc_Cr_old;
+  a.f[1] = dev->conc_Nb_old;
+  a.f[2] = dev->phi_del_old;
+  a.f[3] = dev->phi_lav_old;
+  a.Nx = s->Nx;
+  a.Ny = s->Ny;
+  a.Nz = 1;
+  a.dxyz[0] = dx;
+  a.dxyz[1] = dy;
+  a.dxyz[2] = 1.0;
+  for (int k = 0; k < 2; k++) {
+    a.kappa[k] = s->m.kappa[k];
+    a.omega[k] = s->m.omega[k];
+  }
+  a.Omega = Omega;
+  a.chem = chem_nrg ? s->nrg_map[0] : nullptr;
+  a.grad = grad_nrg ? s->nrg_map[1] : nullptr;
+  a.partial = s->sum_partial;
+  a.out = s->sum_out;
+  CK(launch_energy(a, s->st));
+  CK(cudaMemcpyAsync(energy, s->sum_out, sizeof(double), cudaMemcpyDeviceToHost, s->st));
+  for (int k = 0; k < 2; k++)
+    if (want[k])
+      CK(cudaMemcpyAsync(want[k], s->nrg_map[k], n * sizeof(double), cudaMemcpyDeviceToHost, s->st));
   CK(cudaStreamSynchronize(s->st));
   return 0;
 }

@@ -33,6 +33,7 @@ struct Grid3D {
   float* A[2] = {};
   float* B[2] = {};
   int pitch32 = 0;
+  double dxyz[3] = {};
   int cur = 0;
   bool f32_live = false;
   double* sum_partial = nullptr;
@@ -178,6 +179,14 @@ using namespace pfa;
 
 extern "C" {
 
+size_t pfa3d_footprint(int nx, int ny, int nz, int precision) {
+  if (nx < 3 || ny < 3 || nz < 3) return 0;
+  const size_t ghost = size_t(nx) * ny * nz;
+  if (precision == PFA_FP64) return 2 * 4 * ghost * sizeof(double);
+  const size_t recs = size_t((nx - 2 + 31) / 32 * 32) * (ny - 2) * (nz - 2);
+  return 4 * ghost * sizeof(double) + 2 * recs * (16 + 8);
+}
+
 int pfa3d_create(void** handle, int nx, int ny, int nz, const double* params, const double* dxyz,
                  const double* conc_Cr, const double* conc_Nb, const double* phi_del,
                  const double* phi_lav, int precision) {
@@ -201,7 +210,10 @@ int pfa3d_create(void** handle, int nx, int ny, int nz, const double* params, co
   }
   g->m.alpha = params[10];
   g->m.dt = params[11];
-  for (int i = 0; i < 3; i++) g->m.idx2[i] = 1.0 / (dxyz[i] * dxyz[i]);
+  for (int i = 0; i < 3; i++) {
+    g->dxyz[i] = dxyz[i];
+    g->m.idx2[i] = 1.0 / (dxyz[i] * dxyz[i]);
+  }
   model_fast_coef(&g->fk);
   static bool ready = false;
   if (!ready) {
@@ -258,6 +270,13 @@ int pfa3d_run_timed(void* handle, int nsteps, float* ms) {
   return r;
 }
 
+int pfa3d_sync(void* handle) {
+  Grid3D* g = static_cast<Grid3D*>(handle);
+  if (!g) return err(PFA_ESTATE, "pfa3d_sync: null handle");
+  CK3(cudaStreamSynchronize(g->st));
+  return 0;
+}
+
 int pfa3d_read(void* handle, double* conc_Cr, double* conc_Nb, double* phi_del, double* phi_lav) {
   Grid3D* g = static_cast<Grid3D*>(handle);
   if (!g) return err(PFA_ESTATE, "pfa3d_read: null handle");
@@ -311,6 +330,30 @@ int pfa3d_summarize(void* handle, double* out) {
   a.out = g->sum_out;
   CK3(launch_summarize(a, g->st));
   CK3(cudaMemcpyAsync(out, g->sum_out, 5 * sizeof(double), cudaMemcpyDeviceToHost, g->st));
+  CK3(cudaStreamSynchronize(g->st));
+  return 0;
+}
+
+int pfa3d_summarize_energy(void* handle, double Omega, double* energy) {
+  Grid3D* g = static_cast<Grid3D*>(handle);
+  if (!g || !energy) return err(PFA_EINVAL, "pfa3d_summarize_energy: null argument");
+  if (int r = sync_f64(g)) return r;
+  EnergyArgs a{};
+  for (int k = 0; k < 4; k++) a.f[k] = g->f64[0][k];
+  a.Nx = g->Nx;
+  a.Ny = g->Ny;
+  a.Nz = g->Nz;
+  a.is3d = 1;
+  for (int i = 0; i < 3; i++) a.dxyz[i] = g->dxyz[i];
+  for (int k = 0; k < 2; k++) {
+    a.kappa[k] = g->m.kappa[k];
+    a.omega[k] = g->m.omega[k];
+  }
+  a.Omega = Omega;
+  a.partial = g->sum_partial;
+  a.out = g->sum_out;
+  CK3(launch_energy(a, g->st));
+  CK3(cudaMemcpyAsync(energy, g->sum_out, sizeof(double), cudaMemcpyDeviceToHost, g->st));
   CK3(cudaStreamSynchronize(g->st));
   return 0;
 }

@@ -22,4 +22,18 @@ struct SumArgs {
 
 cudaError_t launch_summarize(const SumArgs& a, cudaStream_t s);
 
+// Free energy of FP64 fields in the ghost-ring layout (pfa_energy.cu).
+struct EnergyArgs {
+  const double* f[4];
+  int Nx, Ny, Nz, is3d;
+  double dxyz[3];
+  double kappa[2], omega[2], Omega;
+  double* chem;       // per-node chemical energy (ghost-ring layout) or nullptr
+  double* grad;       // per-node gradient energy or nullptr
+  double* partial;    // scratch: kSumBlocks doubles
+  double* out;        // 1 double (device)
+};
+
+cudaError_t launch_energy(const EnergyArgs& a, cudaStream_t s);
+
 }  // namespace pfa

@@ -167,3 +167,35 @@ def batch_grid(side, seed):
     e = (rng.uniform(*ENRICH_RANGE[0]), rng.uniform(*ENRICH_RANGE[1]))
     return grid2d(side, side, seed + 7, matrix=m, enrich=e,
                   stripe_width=max(4, min(64, side // 4)), n_particles=4)
+
+
+# request sizes of the serving workload: (dimension, side)
+SERVE_SIZES = ((2, 256), (2, 1024), (2, 4096), (3, 128), (3, 256))
+
+
+def serve_trace(count=24, seed=5, rate=20.0, steps=(2000, 20000)):
+    """Seeded request trace: Poisson arrivals at `rate` per second, sizes
+    uniform over SERVE_SIZES, step counts uniform in `steps` (inclusive)."""
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, count))
+    out = []
+    for k in range(count):
+        dim, side = SERVE_SIZES[int(rng.integers(len(SERVE_SIZES)))]
+        out.append({"rid": k, "dim": dim, "side": side, "arrival": float(arrivals[k]),
+                    "steps": int(rng.integers(steps[0], steps[1] + 1)),
+                    "seed": seed * 1000 + k})
+    return out
+
+
+def serve_fields(item):
+    """Initial condition of one trace request: compositions drawn from the
+    matrix and enrichment ranges, a stripe (2D) or slab (3D), particles."""
+    rng = np.random.default_rng(item["seed"])
+    m = (rng.uniform(*MATRIX_RANGE[0]), rng.uniform(*MATRIX_RANGE[1]))
+    e = (rng.uniform(*ENRICH_RANGE[0]), rng.uniform(*ENRICH_RANGE[1]))
+    s = item["side"]
+    if item["dim"] == 2:
+        return grid2d(s, s, item["seed"] + 7, matrix=m, enrich=e,
+                      stripe_width=max(4, min(64, s // 4)), n_particles=4)
+    return grid3d(s, s, s, item["seed"] + 7, matrix=m, enrich=e, slab=max(4, s // 8),
+                  n_particles=8, radius=6.0)

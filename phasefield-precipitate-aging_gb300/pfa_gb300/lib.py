@@ -93,6 +93,10 @@ def load():
         "pfa3d_upload": (_i, [ctypes.c_void_p, _dp, _dp, _dp, _dp]),
         "pfa3d_summarize": (_i, [ctypes.c_void_p, _dp]),
         "pfa3d_destroy": (_i, [ctypes.c_void_p]),
+        "pfa3d_footprint": (ctypes.c_size_t, [_i, _i, _i, _i]),
+        "pfa3d_sync": (_i, [ctypes.c_void_p]),
+        "pfa3d_summarize_energy": (_i, [ctypes.c_void_p, _d, _dp]),
+        "pfa_summarize_energy": (_i, [P, _d, _d, _d, _dp, _dp, _dp]),
         "pfa_batch_footprint": (ctypes.c_size_t, [_i, _i]),
         "pfa_batch_create": (_i, [ctypes.POINTER(ctypes.c_void_p), _dp, _dp, ctypes.c_size_t]),
         "pfa_batch_add": (_i, [ctypes.c_void_p, _i, _i, _dp, _dp, _dp, _dp,
@@ -279,6 +283,18 @@ class Grid2D:
         check(self.L.pfa_summarize(self.ref, _ptr(out)), "summarize")
         return out
 
+    def energy(self, alpha=None, maps=False):
+        """Total free energy (and the per-node chemical / gradient maps)."""
+        alpha = self.params["alpha"] if alpha is None else alpha
+        e = ctypes.c_double()
+        chem = np.zeros((self.ny, self.nx)) if maps else None
+        grad = np.zeros((self.ny, self.nx)) if maps else None
+        check(self.L.pfa_summarize_energy(self.ref, self.params["dx"],
+                                          self.params.get("dy", self.params["dx"]), alpha,
+                                          ctypes.byref(e), _ptr(chem) if maps else None,
+                                          _ptr(grad) if maps else None), "pfa_summarize_energy")
+        return (e.value, chem, grad) if maps else e.value
+
     def sync(self):
         check(self.L.pfa_sync(self.ref), "sync")
 
@@ -318,6 +334,11 @@ class Grid3D:
                              *[_ptr(a) for a in f], PRECISIONS[precision]), "pfa3d_create")
         self._live = True
 
+    @staticmethod
+    def footprint(shape, precision="fp32"):
+        nz, ny, nx = shape
+        return int(load().pfa3d_footprint(nx, ny, nz, PRECISIONS[precision]))
+
     def run(self, nsteps):
         check(self.L.pfa3d_run(self.h, int(nsteps)), "pfa3d_run")
 
@@ -325,6 +346,16 @@ class Grid3D:
         ms = ctypes.c_float()
         check(self.L.pfa3d_run_timed(self.h, int(nsteps), ctypes.byref(ms)), "pfa3d_run_timed")
         return ms.value
+
+    def sync(self):
+        check(self.L.pfa3d_sync(self.h), "pfa3d_sync")
+
+    def energy(self, alpha=None):
+        e = ctypes.c_double()
+        alpha = self.params["alpha"] if alpha is None else alpha
+        check(self.L.pfa3d_summarize_energy(self.h, alpha, ctypes.byref(e)),
+              "pfa3d_summarize_energy")
+        return e.value
 
     def read(self):
         out = [np.empty(self.shape) for _ in range(4)]

@@ -126,6 +126,20 @@ def summary(ref):
                         summary=ref.summarize(f))
 
 
+def free_energy(ref):
+    """summarize_energy (src/alloy625.cpp:865-919) on a grid with particles,
+    so that both the chemical and the gradient terms are exercised."""
+    prm = O.model_params()
+    f = ic.grid2d(40, 31, seed=32, stripe_width=10, n_particles=2, radius=4.0)
+    e, chem, grad = ref.energy2d(f, prm.dx, prm.dx, list(prm.kappa), list(prm.omega), 1.07e11,
+                                 maps=True)
+    np.savez_compressed(os.path.join(HERE, "energy.npz"),
+                        **{f"ic_{n}": f[j] for j, n in enumerate(("cr", "nb", "pd", "pl"))},
+                        energy=np.array([e]), chem=chem, grad=grad,
+                        params=np.array([prm.dx, prm.dx, prm.kappa[0], prm.kappa[1],
+                                         prm.omega[0], prm.omega[1], 1.07e11]))
+
+
 def abi_symbols(refdir):
     """Mangled names the reference's caller links against: compile a stub
     that calls every host entry point through the reference's own headers."""
@@ -158,16 +172,18 @@ def abi_symbols(refdir):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--only", nargs="*", help="write only these sets (e.g. energy summary)")
     args = ap.parse_args()
     subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "ref", f"REF={args.ref}"],
                    check=True)
     ref = O.load_ref()
     rng = np.random.default_rng(20261203)
-    energies(ref, rng)
-    steps(ref)
-    nucleation(ref)
-    summary(ref)
-    abi_symbols(args.ref)
+    sets = {"energies": lambda: energies(ref, rng), "steps": lambda: steps(ref),
+            "nucleation": lambda: nucleation(ref), "summary": lambda: summary(ref),
+            "energy": lambda: free_energy(ref), "abi": lambda: abi_symbols(args.ref)}
+    for name, fn in sets.items():
+        if not args.only or name in args.only:
+            fn()
     print("golden vectors written to", HERE)
 
 

@@ -80,6 +80,17 @@ def test_summary_matches_reference(orc):
     np.testing.assert_allclose(s, g["summary"], rtol=1e-14, atol=0)
 
 
+def test_free_energy_matches_reference(orc):
+    g = golden("energy.npz")
+    dx, dy, k0, k1, w0, w1, Om = g["params"]
+    e, chem, grad = orc.energy2d(fields_of(g, "ic"), dx, dy, [k0, k1], [w0, w1], Om, maps=True)
+    np.testing.assert_allclose(e, g["energy"][0], rtol=1e-13, atol=0)
+    np.testing.assert_allclose(chem, g["chem"], rtol=1e-13, atol=1e-13 * np.abs(g["chem"]).max())
+    np.testing.assert_allclose(grad, g["grad"], rtol=1e-13, atol=1e-13 * np.abs(g["grad"]).max())
+    # both terms are present where the particles are
+    assert np.abs(g["grad"]).max() > 0.01 * np.abs(g["chem"]).max()
+
+
 def test_philox_known_answers():
     # Known-answer vectors of Philox4x32-10 published with the Random123
     # library (Salmon et al., SC'11).
