@@ -279,6 +279,52 @@ def bench_batch(args, ws, rank, local, barrier, max_over_ranks, pl, ic):
         print(json.dumps(line))
 
 
+def bench_error(args, ws, rank, local, barrier, max_over_ranks, pl, ic):
+    """Stated error at the configurations' full step counts: the FP32 form
+    against the FP64 step on the 4096^2 grid (10000 steps, nucleation every
+    100 steps with the same seed in both) and the 512^3 grid (2000 steps).
+    Prints one JSON line; `value` is the FP32 rate of the 2D run."""
+    if rank != 0:
+        return
+    out = {}
+    p2 = pl.model_params()
+    f2 = ic.config2(n=N_SIDE)
+    n2 = args.steps if args.steps > 10 else 10000
+    runs = {}
+    for prec in ("fp32", "fp64"):
+        g = pl.Grid2D(f2, p2, precision=prec)
+        g.set_nucleation(seed=42, geometry=pl.NUC_REFERENCE_GEOMETRY, interval=100,
+                         sigma=NUC["sigma"], unit_a=NUC["unit_a"], d=(p2["dx"],) * 3,
+                         dt_nuc=100 * p2["dt"])
+        ms = g.run_timed(n2)
+        runs[prec] = (g.read(), ms)
+        g.close()
+    err = [float(np.max(np.abs(a[1:-1, 1:-1] - b[1:-1, 1:-1])))
+           for a, b in zip(runs["fp32"][0], runs["fp64"][0])]
+    out["grid4096"] = {"steps": n2, "x_Cr": err[0], "x_Nb": err[1], "phi_delta": err[2],
+                       "phi_laves": err[3], "fp32_ms": runs["fp32"][1],
+                       "fp64_ms": runs["fp64"][1]}
+    side = args.side or GRID3D_SIDE
+    n3 = 2000
+    p3 = pl.model_params(dim=3)
+    f3 = ic.grid3d(side, side, side, seed=4, slab=64, n_particles=32, radius=6.0)
+    res3 = {}
+    for prec in ("fp32", "fp64"):
+        g = pl.Grid3D(f3, p3, precision=prec)
+        res3[prec] = (g.run_timed(n3), g.read())
+        g.close()
+    err3 = [float(np.max(np.abs(a[1:-1, 1:-1, 1:-1] - b[1:-1, 1:-1, 1:-1])))
+            for a, b in zip(res3["fp32"][1], res3["fp64"][1])]
+    out["grid3d"] = {"side": side, "steps": n3, "x_Cr": err3[0], "x_Nb": err3[1],
+                     "phi_delta": err3[2], "phi_laves": err3[3], "fp32_ms": res3["fp32"][0],
+                     "fp64_ms": res3["fp64"][0]}
+    value = N_SIDE * N_SIDE * n2 / (runs["fp32"][1] / 1e3)
+    args.steps = 1
+    print(json.dumps(_line(args, ws, value, runs["fp32"][1] / 1e3,
+                           "stated-error study: FP32 form vs FP64 at full step counts",
+                           {"bound": 1e-5}, max_field_error=out)))
+
+
 def bench_grid3d(args, ws, rank, local, barrier, max_over_ranks, pl, ic):
     """The 3D workload, FP32 form vs the FP64 step."""
     n = args.side or GRID3D_SIDE
@@ -415,7 +461,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp32k"])
     ap.add_argument("--workload", default="grid4096",
-                    choices=["grid4096", "batch64", "grid3d512", "serve"],
+                    choices=["grid4096", "batch64", "grid3d512", "serve", "error"],
                     help="grid4096: the headline single-grid workload; batch64 / grid3d512: "
                          "the many-grids and 3D workloads")
     ap.add_argument("--side", type=int, default=0,
@@ -466,7 +512,8 @@ def main():
         return float(t.item())
 
     if args.workload != "grid4096":
-        fn = {"batch64": bench_batch, "grid3d512": bench_grid3d, "serve": bench_serve}[args.workload]
+        fn = {"batch64": bench_batch, "grid3d512": bench_grid3d, "serve": bench_serve,
+              "error": bench_error}[args.workload]
         fn(args, ws, rank, local, barrier, max_over_ranks, pl, ic)
         if dist is not None:
             dist.destroy_process_group()

@@ -52,7 +52,6 @@ void pfa_clear_error(void);
 /* ---- device selection (cudaSetDevice for this library's runtime) ---- */
 int pfa_set_device(int device);
 int pfa_device_count(void);
-
 /* ---- configuration of one CudaData (library-side table) ---- */
 int pfa_set_mode(struct CudaData* dev, int mode);
 int pfa_set_precision(struct CudaData* dev, int precision);
