@@ -40,6 +40,9 @@ enum {
 };
 
 enum { PFA_MODE_FUSED = 0, PFA_MODE_COMPAT = 1 };
+/* PFA_FP32: FP32 arithmetic, every field Kahan-compensated with the
+ * compensations packed as 16-bit counts (48 bytes per cell update);
+ * PFA_FP32_KPHI: the same with FP32 compensations (64 bytes per cell). */
 enum { PFA_FP64 = 0, PFA_FP32 = 1, PFA_FP32_KPHI = 2 };
 enum { PFA_NUC_REFERENCE_GEOMETRY = 0, PFA_NUC_FIXED_GEOMETRY = 1 };
 
@@ -134,7 +137,7 @@ int pfa3d_destroy(void* handle);
  * No counterpart in the reference, which runs one grid per process
  * (src/main.cpp:285-321).  A batch owns a device arena of arena_bytes and
  * steps every member grid with one launch per time step (FP32 form,
- * fixed-point phases, 5-point Laplacian); all members share params (the 12
+ * packed compensations, 5-point Laplacian); all members share params (the 12
  * doubles of pfa3d_create) and dxy = dx, dy.  Grids join (pfa_batch_add:
  * fields in the reference layout, ny x nx doubles with the ghost ring;
  * PFA_ENOMEM, not printed, when the arena has no room) and leave

@@ -79,8 +79,7 @@ struct State {
   int pitch32 = 0;      // records per row
   float* f32mem = nullptr;
   float* recA[2] = {};  // {x_Cr, x_Nb, phi_del, phi_lav} records, ping-pong
-  float* recB[2] = {};  // Kahan compensation records
-  int bstride = 2;      // floats per B record (4 with compensated phases)
+  float* recB[2] = {};  // Kahan compensation records (packed counts or FP32)
   int cur = 0;
   bool f32_live = false;
   // nucleation
@@ -140,7 +139,6 @@ static int ensure_fict(CudaData* dev, State* s) {
 // either precision variant fits), Ny rows of pitch32 records (a multiple of
 // 32), interior only; every array starts on a 256-byte boundary.
 static int ensure_f32(State* s) {
-  s->bstride = s->precision == PFA_FP32_KPHI ? 4 : 2;
   if (s->f32mem) return 0;
   s->pitch32 = ((s->Nx + 31) / 32) * 32;
   const size_t per = ((size_t(s->pitch32) * s->Ny * 4 + 63) / 64) * 64;  // floats per array
@@ -162,12 +160,11 @@ static ConvArgs conv_args(CudaData* dev, State* s) {
   const bool kphi = s->precision == PFA_FP32_KPHI;
   c.A = s->recA[s->cur];
   c.B = s->recB[s->cur];
-  c.bstride = s->bstride;
+  c.pack = !kphi;
   c.Nx = s->Nx;
   c.Ny = s->Ny;
   c.pitch64 = s->nx;
   c.pitch32 = s->pitch32;
-  c.phi_fix = !kphi;
   return c;
 }
 
@@ -236,7 +233,7 @@ static int fused_step(CudaData* dev, State* s, double alpha, double dt) {
   a.out[0] = s->recA[n];
   a.out[1] = s->recB[n];
   a.pitch = s->pitch32;
-  a.kahan_phi = s->precision == PFA_FP32_KPHI;
+  a.full_comp = s->precision == PFA_FP32_KPHI;
   CK(launch_step2d_f32(a, s->st));
   s->cur = n;
   return 0;
@@ -254,19 +251,16 @@ static int nucleate(CudaData* dev, State* s, double sig_d, double sig_l, double 
     a.f[3] = dev->phi_lav_new;
     a.pitch = s->nx;
     a.is_f32 = 0;
-    a.stride = a.cstride = 1;
+    a.stride = 1;
   } else {
     if (int r = f32_import(dev, s)) return r;
-    for (int k = 0; k < 4; k++) {
-      a.f[k] = s->recA[s->cur] + k;
-      a.comp[k] = k < s->bstride ? s->recB[s->cur] + k : nullptr;
-    }
+    for (int k = 0; k < 4; k++) a.f[k] = s->recA[s->cur] + k;
+    a.comp = s->recB[s->cur];
+    a.pack = s->precision == PFA_FP32;
     a.stride = 4;
-    a.cstride = s->bstride;
     a.pitch = s->pitch32;
     a.is_f32 = 1;
     a.compact = 1;
-    a.phi_fix = s->precision == PFA_FP32;
   }
   a.Nx = s->Nx;
   a.Ny = s->Ny;
@@ -1032,13 +1026,11 @@ int pfa_summarize(struct CudaData* dev, double* out) {
   SumArgs a{};
   if (s->precision != PFA_FP64 && s->f32_live) {
     for (int k = 0; k < 4; k++) a.f[k] = s->recA[s->cur] + k;
-    a.c[0] = s->recB[s->cur];
-    a.c[1] = s->recB[s->cur] + 1;
+    a.comp = s->recB[s->cur];
+    a.pack = s->precision == PFA_FP32;
     a.stride = 4;
-    a.cstride = s->bstride;
     a.is_f32 = 1;
     a.compact = 1;
-    a.phi_fix = s->precision == PFA_FP32;
     a.pitch = s->pitch32;
   } else {
     a.f[0] = dev->conc_Cr_old;
@@ -1047,7 +1039,7 @@ int pfa_summarize(struct CudaData* dev, double* out) {
     a.f[3] = dev->phi_lav_old;
     a.pitch = s->nx;
   }
-  if (a.stride == 0) a.stride = a.cstride = 1;
+  if (a.stride == 0) a.stride = 1;
   a.Nx = s->Nx;
   a.Ny = s->Ny;
   a.Nz = 1;

@@ -2,7 +2,7 @@
 //
 // The reference steps one grid per process (src/main.cpp:285-321).  A batch
 // holds any number of 2D grids of different sizes that share one parameter
-// set, in the FP32 precision form (fixed-point phases), and advances all of
+// set, in the FP32 precision form (packed compensations), and advances all of
 // them with one launch per time step: the grids' warp strips x row segments
 // form one table of units of work that a persistent kernel drains through an
 // atomic counter (or that a one-warp-per-unit launch covers).  Multi-step runs
@@ -102,8 +102,8 @@ BatchGrid grid_entry(const Batch* b, const Slot& s) {
   char* base = b->arena + s.off;
   g.A[0] = reinterpret_cast<float4*>(base);
   g.A[1] = reinterpret_cast<float4*>(base + recs * 16);
-  g.B[0] = reinterpret_cast<float2*>(base + recs * 32);
-  g.B[1] = reinterpret_cast<float2*>(base + recs * 40);
+  g.B[0] = reinterpret_cast<uint2*>(base + recs * 32);
+  g.B[1] = reinterpret_cast<uint2*>(base + recs * 40);
   g.Nx = s.Nx;
   g.Ny = s.Ny;
   g.pitch = s.pitch;
@@ -286,13 +286,12 @@ ConvArgs conv(Batch* b, const Slot& s) {
   ConvArgs c{};
   for (int k = 0; k < 4; k++) c.f64[k] = b->stage[k];
   c.A = reinterpret_cast<float*>(g.A[b->cur]);
-  c.B = reinterpret_cast<float*>(g.B[b->cur]);
-  c.bstride = 2;
+  c.B = g.B[b->cur];
+  c.pack = 1;
   c.Nx = s.Nx;
   c.Ny = s.Ny;
   c.pitch64 = s.Nx + 2;
   c.pitch32 = s.pitch;
-  c.phi_fix = 1;
   return c;
 }
 
@@ -533,15 +532,12 @@ int pfa_batch_summarize(void* handle, int slot, double* out) {
   const BatchGrid g = grid_entry(b, *s);
   SumArgs a{};
   const float* A = reinterpret_cast<const float*>(g.A[b->cur]);
-  const float* B = reinterpret_cast<const float*>(g.B[b->cur]);
   for (int k = 0; k < 4; k++) a.f[k] = A + k;
-  a.c[0] = B;
-  a.c[1] = B + 1;
+  a.comp = g.B[b->cur];
+  a.pack = 1;
   a.stride = 4;
-  a.cstride = 2;
   a.is_f32 = 1;
   a.compact = 1;
-  a.phi_fix = 1;
   a.pitch = s->pitch;
   a.Nx = s->Nx;
   a.Ny = s->Ny;

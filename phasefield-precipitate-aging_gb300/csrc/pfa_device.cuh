@@ -94,31 +94,31 @@ __device__ __forceinline__ float quad2(const float* c, float a, float b) {
   return fmaf(a, fmaf(c[3], a, fmaf(c[4], b, c[1])), fmaf(b, fmaf(c[5], b, c[2]), c[0]));
 }
 
-// ---- fixed-point phase fields of the FP32 form: phi = q 2^-29 ----
-// Resolution 1.9e-9 everywhere on [-1.99, 1.99] (FP32 has 6e-8 near
-// phi = 1), so Allen-Cahn increments far below FP32's half-ulp still move
-// the field; q is saturated so that the difference of two values fits int32.
-constexpr float kPhiScale = 536870912.0f;  // 2^29
-constexpr float kPhiInvScale = 1.0f / 536870912.0f;
-constexpr double kPhiInvScaleD = 1.0 / 536870912.0;
-constexpr int kPhiQMax = 1068373114;  // floor(1.99 * 2^29)
+// ---- FP32 form: values in FP32, Kahan compensations c (value = hi - c) ----
+// Packed compensation record: four 16-bit counts, c = count 2^-40 for the
+// compositions and count 2^-39 for the phases.  A compensation is at most
+// half an ulp of its value -- below 2^-25 for |x| < 1 and 2^-24 for
+// |phi| < 2 -- so the counts keep 2^-40 (2^-39) of resolution, and a field
+// loses at most half of that per step where the full FP32 compensation
+// would keep it.
+constexpr float kCqX = 1099511627776.0f;  // 2^40
+constexpr float kCqP = 549755813888.0f;   // 2^39
+constexpr float kCqXi = 1.0f / 1099511627776.0f;
+constexpr float kCqPi = 1.0f / 549755813888.0f;
 
-__device__ __forceinline__ float phi_of(int q) { return float(q) * kPhiInvScale; }
-
-__device__ __forceinline__ int phi_sat(long long q) {
-  return int(q > kPhiQMax ? kPhiQMax : (q < -kPhiQMax ? -kPhiQMax : q));
+__device__ __forceinline__ float4 cq_unpack(uint2 w) {
+  const int a = int(w.x), b = int(w.y);
+  return make_float4(float((a << 16) >> 16) * kCqXi, float(a >> 16) * kCqXi,
+                     float((b << 16) >> 16) * kCqPi, float(b >> 16) * kCqPi);
 }
 
-// q + round(inc 2^29), saturated (the increment is clamped first so its
-// integer form cannot overflow)
-__device__ __forceinline__ int phi_add(int q, float inc) {
-  const float c = fminf(fmaxf(inc, -3.9f), 3.9f);
-  return phi_sat((long long)q + __float2int_rn(c * kPhiScale));
+__device__ __forceinline__ unsigned cq_count(float c, float scale) {
+  return unsigned(max(-32767, min(32767, __float2int_rn(c * scale)))) & 0xffffu;
 }
 
-__device__ __forceinline__ int phi_quantize(double v) {
-  const double c = fmin(fmax(v, -1.99), 1.99);
-  return phi_sat(__double2ll_rn(c * 536870912.0));
+__device__ __forceinline__ uint2 cq_pack(float cx, float cy, float cd, float cl) {
+  return make_uint2(cq_count(cx, kCqX) | (cq_count(cy, kCqX) << 16),
+                    cq_count(cd, kCqP) | (cq_count(cl, kCqP) << 16));
 }
 
 // 1 - p(x) = p(1 - x): the gamma fraction without cancellation near a pure
@@ -127,24 +127,68 @@ __device__ __forceinline__ float p_gamma32(float phd, float phl, float pD, float
   return pD >= pL ? p32(1.0f - phd) - pL : p32(1.0f - phl) - pD;
 }
 
-// x^gamma (Cr, Nb) from (X, Y, pD, pG, pL), three-variable form.
-__device__ __forceinline__ void fict_gam32(const FastCoef& k, float X, float Y, float pD, float pG,
-                                           float pL, float& gcr, float& gnb) {
-  const float m0 = pD * pD, m1 = pD * pG, m2 = pD * pL, m3 = pG * pG, m4 = pG * pL, m5 = pL * pL;
-  const float* d = k.den;
-  const float den = fmaf(d[0], m0, fmaf(d[1], m1, fmaf(d[2], m2, fmaf(d[3], m3, fmaf(d[4], m4, d[5] * m5)))));
-  const float r = __frcp_rn(den);
-  float n[2];
+// Phases below this (both fields) leave p(phi) < 1e-14: x^gamma = X to FP64
+// precision.
+constexpr float kBulkPhi = 1e-5f;
+
+// u = x^gamma - xe_gamma in pure gamma: X - xe_gamma, X = hi - c.
+__device__ __forceinline__ void gamma_bulk32(const FastCoef& K, float X, float Y, float cx,
+                                             float cy, float& u1, float& u2) {
+  u1 = (X - K.xe_hi[0][0]) - (cx + K.xe_lo[0][0]);
+  u2 = (Y - K.xe_hi[0][1]) - (cy + K.xe_lo[0][1]);
+}
+
+// u = x^gamma - xe_gamma of one cell in the equilibrium-referenced form
+// (FastCoef): u = d + (A d_Cr + B d_Nb) / den, d = X - X*(p).  X* is
+// expanded about the phase with the largest p (the pivot m):
+//   X* = xe_m + sum_{i != m} p_i xe_i - (sum_{i != m} p_i) xe_m,
+// and d = (hi - xe_m,hi) - (c + xe_m,lo + that sum), so the leading
+// difference is exact where X is near the pivot's composition and every
+// other term is small there (approximate reciprocal: 2 ulp).
+__device__ __forceinline__ void gamma_u32(const FastCoef& K, float X, float Y, float cx, float cy,
+                                          float phd, float phl, float& u1, float& u2) {
+  const float pD = p32(phd), pL = p32(phl);
+  const float pG = p_gamma32(phd, phl, pD, pL);
+  const int piv = (pG >= pD && pG >= pL) ? 0 : (pD >= pL ? 1 : 2);
+  const float t0 = piv == 0 ? 0.0f : pG, t1 = piv == 1 ? 0.0f : pD, t2 = piv == 2 ? 0.0f : pL;
+  const float s = t0 + t1 + t2;
+  const float xv[2] = {X, Y}, cv[2] = {cx, cy};
+  float dv[2];
+#pragma unroll
+  for (int k = 0; k < 2; k++) {
+    const float xh = piv == 0 ? K.xe_hi[0][k] : (piv == 1 ? K.xe_hi[1][k] : K.xe_hi[2][k]);
+    const float xl = piv == 0 ? K.xe_lo[0][k] : (piv == 1 ? K.xe_lo[1][k] : K.xe_lo[2][k]);
+    const float mix =
+        fmaf(t0, K.xe_hi[0][k], fmaf(t1, K.xe_hi[1][k], fmaf(t2, K.xe_hi[2][k], -s * xh)));
+    dv[k] = (xv[k] - xh) - (cv[k] + xl + mix);
+  }
+  const float m[5] = {pD * pD, pD * pG, pD * pL, pG * pL, pL * pL};
+  const float* d = K.den;
+  const float den = fmaf(d[0], m[0], fmaf(d[1], m[1], fmaf(d[2], m[2], fmaf(d[3], pG * pG, fmaf(d[4], m[3], d[5] * m[4])))));
+  const float r = __fdividef(1.0f, den);
+  float u[2];
 #pragma unroll
   for (int c = 0; c < 2; c++) {
-    const float* a = k.num[c];
-    const float lx = fmaf(a[0], pD, fmaf(a[1], pG, a[2] * pL));
-    const float ly = fmaf(a[3], pD, fmaf(a[4], pG, a[5] * pL));
-    const float q = fmaf(a[6], m0, fmaf(a[7], m1, fmaf(a[8], m2, fmaf(a[9], m3, fmaf(a[10], m4, a[11] * m5)))));
-    n[c] = fmaf(X, lx, fmaf(Y, ly, q));
+    float a = 0.0f, b = 0.0f;
+#pragma unroll
+    for (int j = 0; j < 5; j++) {
+      a = fmaf(K.dev[c][j][0], m[j], a);
+      b = fmaf(K.dev[c][j][1], m[j], b);
+    }
+    u[c] = fmaf(fmaf(a, dv[0], b * dv[1]), r, dv[c]);
   }
-  gcr = n[0] * r;
-  gnb = n[1] * r;
+  u1 = u[0];
+  u2 = u[1];
+}
+
+// dF/dphi_i without the Laplacian term: -p'(phi) dP + 2 omega phi (phi-1)(2 phi-1)
+// + 2 alpha phi phi_j^2, Horner forms
+__device__ __forceinline__ float dF_local32(float ph, float pj, float dP, float om2,
+                                            float alpha2) {
+  const float t = fmaf(-ph, ph, ph);  // phi (1 - phi)
+  const float pp = 30.0f * t * t;     // p'(phi)
+  const float well = ph * fmaf(ph, fmaf(2.0f * om2, ph, -3.0f * om2), om2);
+  return fmaf(-pp, dP, fmaf(alpha2 * ph, pj * pj, well));
 }
 
 }  // namespace dev

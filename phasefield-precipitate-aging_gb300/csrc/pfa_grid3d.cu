@@ -308,18 +308,16 @@ int pfa3d_summarize(void* handle, double* out) {
   SumArgs a{};
   if (g->precision == PFA_FP32 && g->f32_live) {
     for (int k = 0; k < 4; k++) a.f[k] = g->A[g->cur] + k;
-    a.c[0] = g->B[g->cur];
-    a.c[1] = g->B[g->cur] + 1;
+    a.comp = g->B[g->cur];
+    a.pack = 1;
     a.stride = 4;
-    a.cstride = 2;
     a.is_f32 = 1;
     a.compact = 1;
-    a.phi_fix = 1;
     a.pitch = g->pitch32;
   } else {
     if (int r = sync_f64(g)) return r;
     for (int k = 0; k < 4; k++) a.f[k] = g->f64[0][k];
-    a.stride = a.cstride = 1;
+    a.stride = 1;
     a.pitch = g->Nx + 2;
   }
   a.is3d = 1;

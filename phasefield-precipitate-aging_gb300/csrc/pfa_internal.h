@@ -28,11 +28,25 @@ struct ModelConst {
 //    with the scale folded into l, m, q;  x^gamma_k = num_k / den.
 //  * grand-potential difference of phase i as a quadratic in
 //      u = x^gamma - xe_gamma:  c0 + u1 (c1 + c11 u1 + c12 u2) + u2 (c2 + c22 u2)
+//  * equilibrium-referenced form of the same solve.  The system is linear in
+//    X, and the mixture X*(p) = sum_i p_i xe_i of the phases' equilibrium
+//    compositions (a common tangent of the paraboloids) gives x^gamma =
+//    xe_gamma for every p.  Hence, with d = X - X*(p),
+//      u = x^gamma - xe_gamma = d + (A(p) d_Cr + B(p) d_Nb) / den,
+//    A_k, B_k = sums over the monomials that contain pD or pL (pD^2, pD pG,
+//    pD pL, pG pL, pL^2) of the quadratic forms of (l_k - den e_k) and m_k
+//    (linear terms written as quadratics with pD + pG + pL = 1; the pG^2
+//    coefficients vanish).  Inside a precipitate d is small even where the
+//    KKS amplification A/den is large, so FP32 keeps u accurate; the plain
+//    num / den form loses it to cancellation in num.
 struct FastCoef {
   float den[6];        // d
   float num[2][12];    // per comp: l0 l1 l2 m0 m1 m2 q0..q5
   float dP[2][6];      // per phase (delta, laves): c0 c1 c2 c11 c12 c22
-  float xe_gam[2];
+  float xe_gam[2];     // xe_gamma rounded to FP32
+  float dev[2][5][2];  // per comp, per monomial (pD^2 pD pG pD pL pG pL pL^2): A B
+  float xe_hi[3][2];   // equilibrium compositions (gamma, delta, laves), FP32 part
+  float xe_lo[3][2];   // and their remainders
 };
 
 void model_fast_coef(FastCoef* out);

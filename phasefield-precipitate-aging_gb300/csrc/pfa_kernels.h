@@ -17,8 +17,8 @@ struct Step2DArgs {
   int Nx, Ny, pitch;    // interior size and row pitch (elements)
   int write_halo;       // also write the mirrored ghost ring
   int nine;             // 3x3 mask has non-zero corners
-  int kahan_phi;        // FP32 form: FP32 phases with Kahan compensation
-                        // (otherwise 32-bit fixed-point phases)
+  int full_comp;        // FP32 form: compensations as FP32 (16-byte B records)
+                        // instead of packed 16-bit counts (8-byte B records)
   ModelConst m;
   double mask9[9];      // full 3x3 mask, row-major (rows y-1..y+1)
   FastCoef k;
@@ -33,15 +33,14 @@ struct Step2DArgs {
 
 // Layout conversion between FP64 reference fields (ghost ring, pitch64) and
 // the FP32 form's records (interior only, rows of pitch32 records):
-// A = {x_Cr, x_Nb, phi_del, phi_lav} per cell, B = Kahan compensations
-// (bstride = 2: {c_Cr, c_Nb}; 4: also the phases).
+// A = {x_Cr, x_Nb, phi_del, phi_lav} per cell, B = the four Kahan
+// compensations, packed 16-bit counts (pack) or FP32.
 struct ConvArgs {
   double* f64[4];
-  float* A;        // phases hold int32 fixed-point bits when phi_fix
-  float* B;
-  int bstride;
+  float* A;
+  void* B;
+  int pack;
   int Nx, Ny, pitch64, pitch32;
-  int phi_fix;
 };
 
 // Arguments of the reference's per-stage kernels (compat mode).
@@ -56,12 +55,12 @@ struct StageArgs {
   double mask9[9];
 };
 
-// A batch of 2D grids in the FP32 form (fixed-point phases) stepped by one
+// A batch of 2D grids in the FP32 form (packed compensations) stepped by one
 // launch.  Per grid: record buffers of both parities; per unit of work: one
 // warp strip (30 columns) over a row segment of one grid.
 struct BatchGrid {
   float4* A[2];   // {x_Cr, x_Nb, phi_del, phi_lav} records, parity 0 / 1
-  float2* B[2];   // Kahan compensations
+  uint2* B[2];    // packed Kahan compensations
   int Nx, Ny, pitch, pad;
 };
 struct BatchUnit {
@@ -89,7 +88,8 @@ cudaError_t launch_export_f32(const ConvArgs& a, cudaStream_t s);
 
 // Arguments of one 3D step (pfa_step3d.cu).  F64: in/out = four ghost-ring
 // arrays ((Nz+2) x (Ny+2) x pitch, pitch = Nx + 2); FP32 form: in[0]/out[0]
-// = float4 A records, in[1]/out[1] = float2 B records, Nz x Ny x pitch.
+// = float4 A records, in[1]/out[1] = packed compensation records (uint2),
+// Nz x Ny x pitch.
 struct Step3DArgs {
   const void* in[4];
   void* out[4];
@@ -103,7 +103,7 @@ struct Step3DArgs {
 struct Conv3DArgs {
   double* f64[4];  // ghost-ring layout
   float* A;        // float4 records
-  float* B;        // float2 records
+  void* B;         // packed compensation records (uint2)
   int Nx, Ny, Nz, pitch32;
 };
 

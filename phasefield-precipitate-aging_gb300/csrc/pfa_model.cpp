@@ -131,6 +131,38 @@ void model_fast_coef(FastCoef* o) {
   }
   o->xe_gam[0] = float(kXe[0][0]);
   o->xe_gam[1] = float(kXe[0][1]);
+  for (int ph = 0; ph < 3; ph++)
+    for (int c = 0; c < 2; c++) {
+      o->xe_hi[ph][c] = float(kXe[ph][c]);
+      o->xe_lo[ph][c] = float(kXe[ph][c] - double(o->xe_hi[ph][c]));
+    }
+  // equilibrium-referenced form (FastCoef::dev): quadratic coefficients of
+  // l . [pD pG pL] on the monomials pD^2, pD pG, pD pL, pG^2, pG pL, pL^2
+  auto homog = [](const double l[3], double q[6]) {
+    q[0] = l[0];
+    q[1] = l[0] + l[1];
+    q[2] = l[0] + l[2];
+    q[3] = l[1];
+    q[4] = l[1] + l[2];
+    q[5] = l[2];
+  };
+  static const int kMono[5] = {0, 1, 2, 4, 5};  // all but pG^2
+  for (int c = 0; c < 2; c++) {
+    const FictRow& r = kFict[0][c];
+    double lx[3], ly[3], qx[6], qy[6];
+    for (int k = 0; k < 3; k++) {
+      lx[k] = r.scale * r.l[k];
+      ly[k] = r.scale * r.m[k];
+    }
+    homog(lx, qx);
+    homog(ly, qy);
+    for (int j = 0; j < 6; j++) (c == 0 ? qx : qy)[j] -= kDen[j];  // - X_c den
+    for (int t = 0; t < 5; t++) {
+      const int j = kMono[t];
+      o->dev[c][t][0] = float(qx[j]);
+      o->dev[c][t][1] = float(qy[j]);
+    }
+  }
 }
 
 }  // namespace pfa

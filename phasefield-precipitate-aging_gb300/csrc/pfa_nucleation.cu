@@ -67,20 +67,35 @@ __device__ __forceinline__ size_t stor(const NucArgs& a, int xx, int yy) {
   return size_t(yy) * a.pitch + xx;
 }
 
-// a phase field as stored (FP64, FP32 or the FP32 form's fixed point), exact
-template <class T>
-__device__ __forceinline__ double ldphi(const NucArgs& a, int k, size_t cell) {
-  const size_t i = cell * a.stride;
-  if (a.phi_fix) return double(static_cast<const int*>(a.f[k])[i]) * kPhiInvScaleD;
-  return ld<T>(a.f[k], i);
+// Kahan compensation of field k at a cell of the FP32 form (value = f - c)
+__device__ __forceinline__ float comp_get(const NucArgs& a, size_t cell, int k) {
+  if (!a.comp) return 0.0f;
+  float4 c;
+  if (a.pack)
+    c = cq_unpack(static_cast<const uint2*>(a.comp)[cell]);
+  else
+    c = static_cast<const float4*>(a.comp)[cell];
+  return k == 0 ? c.x : (k == 1 ? c.y : (k == 2 ? c.z : c.w));
 }
 
-// the same, rounded to FP32 without touching the FP64 pipe in the FP32 form
+__device__ __forceinline__ void comp_set(const NucArgs& a, size_t cell, int k, float c) {
+  if (!a.comp) return;
+  if (a.pack)
+    static_cast<short*>(a.comp)[4 * cell + k] = short(cq_count(c, k < 2 ? kCqX : kCqP));
+  else
+    static_cast<float*>(a.comp)[4 * cell + k] = c;
+}
+
+// a field's value as stored (FP64, or the FP32 form's hi - c), exact
+template <class T>
+__device__ __forceinline__ double ldval(const NucArgs& a, int k, size_t cell) {
+  return ld<T>(a.f[k], cell * a.stride) - double(comp_get(a, cell, k));
+}
+
+// a phase field rounded to FP32 without touching the FP64 pipe in the FP32 form
 template <class T>
 __device__ __forceinline__ float ldphi_f(const NucArgs& a, int k, size_t cell) {
-  const size_t i = cell * a.stride;
-  if (a.phi_fix) return phi_of(static_cast<const int*>(a.f[k])[i]);
-  return float(static_cast<const T*>(a.f[k])[i]);
+  return float(static_cast<const T*>(a.f[k])[cell * a.stride]);
 }
 
 // composition-dependent diffusivities D_CrCr, D_NbNb (thermo/parabola625.c:1860-1894)
@@ -163,7 +178,7 @@ __device__ __forceinline__ bool clear_at(const NucArgs& a, size_t s) {
   if (q - err > 1e-10f) return false;
   if (q + err < 1e-10f) return true;
   // the reference takes max(phi_pre, sum), which skips a NaN sum
-  return !(p64(ldphi<T>(a, 2, s)) + p64(ldphi<T>(a, 3, s)) >= 1e-10);
+  return !(p64(ldval<T>(a, 2, s)) + p64(ldval<T>(a, 3, s)) >= 1e-10);
 }
 
 template <class T>
@@ -230,7 +245,7 @@ __global__ void __launch_bounds__(256) k_nuc_decide(NucArgs a) {
         }
       }
       if (need) {
-        const double X = double(Xs), Y = double(Ys);
+        const double X = ldval<T>(a, 0, s), Y = ldval<T>(a, 1, s);
         const double u[2] = {u53(w.x, w.y), u53(w.z, w.w)};
         const double dG = g64<0>(X, Y);
         double dcc, dnn;
@@ -278,11 +293,11 @@ __global__ void __launch_bounds__(256) k_nuc_decide(NucArgs a) {
   }
 }
 
-// store v at cell s of field f (and reset its compensation: value = hi - c)
+// store v at cell s of field k (and its compensation: value = hi - c)
 template <class T>
-__device__ __forceinline__ void put(const NucArgs& a, void* f, float* c, size_t s, double v) {
-  static_cast<T*>(f)[s * a.stride] = T(v);
-  if (c) c[s * a.cstride] = float(double(T(v)) - v);
+__device__ __forceinline__ void put(const NucArgs& a, int k, size_t s, double v) {
+  static_cast<T*>(a.f[k])[s * a.stride] = T(v);
+  comp_set(a, s, k, float(double(T(v)) - v));
 }
 
 // embed_OPC_kernel, src/discretization.cu:1046-1077, painted cooperatively
@@ -303,10 +318,6 @@ __device__ void paint(const NucArgs& a, const NucEvent& e, int ph) {
   const int w = hi - lo;
   if (w <= 0) return;
   const long long n = (long long)w * w;
-  void* phi = a.f[2 + ph];
-  float* cphi = a.comp[2 + ph];
-  float* ccr = a.comp[0];
-  float* cnb = a.comp[1];
   for (long long t = threadIdx.x; t < n; t += blockDim.x) {
     const int i = lo + int(t / w), j = lo + int(t % w);
     const long long idn = (long long)nxr * (y + j) + (x + i);
@@ -317,15 +328,12 @@ __device__ void paint(const NucArgs& a, const NucEvent& e, int ph) {
     const size_t s = stor(a, xx, yy);
     const double r = sqrt(double(i * i + j * j));
     if (r <= R) {
-      put<T>(a, a.f[0], ccr, s, parCr);
-      put<T>(a, a.f[1], cnb, s, parNb);
-      if (a.phi_fix)
-        static_cast<int*>(phi)[s * a.stride] = phi_quantize(1.0);
-      else
-        put<T>(a, phi, cphi, s, 1.0);
+      put<T>(a, 0, s, parCr);
+      put<T>(a, 1, s, parNb);
+      put<T>(a, 2 + ph, s, 1.0);
     } else {
-      if (r <= RdCr) put<T>(a, a.f[0], ccr, s, xgCr);
-      if (r <= RdNb) put<T>(a, a.f[1], cnb, s, xgNb);
+      if (r <= RdCr) put<T>(a, 0, s, xgCr);
+      if (r <= RdNb) put<T>(a, 1, s, xgNb);
     }
   }
 }

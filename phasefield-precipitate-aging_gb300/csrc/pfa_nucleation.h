@@ -22,13 +22,13 @@ struct NucEvent {
 
 struct NucArgs {
   void* f[4];          // x_Cr, x_Nb, phi_del, phi_lav (halo layout, row pitch `pitch`)
-  float* comp[4];      // FP32 form: compensation arrays (reset where painted), or nullptr
+  void* comp;          // FP32 form: compensation records (value = f - c; set where
+                       // painted), packed 16-bit counts (pack) or float4; else nullptr
+  int pack;
   int is_f32;
-  int phi_fix;         // phases in 32-bit fixed point (FP32 form)
   int compact;         // FP32 form layout: interior rows only (ghost cells read
                        // as their mirrored interior cell, never painted)
   int stride;          // elements between consecutive cells of f[k] (4 for FP32 records)
-  int cstride;         // elements between consecutive cells of comp[k]
   int Nx, Ny, pitch;
   double sigma[2];
   double dx;           // kernel spacing (the reference passes dx * nx here)

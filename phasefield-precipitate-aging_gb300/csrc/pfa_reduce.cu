@@ -39,20 +39,19 @@ __global__ void __launch_bounds__(kThreads) k_sum_partial(SumArgs a) {
     const size_t cell = a.compact
                             ? (size_t(z) * a.Ny + y) * a.pitch + x
                             : (size_t(a.is3d ? z + 1 : 0) * (a.Ny + 2) + (y + 1)) * a.pitch + (x + 1);
-    const size_t i = cell * a.stride, ic = cell * a.cstride;
-    const T* f0 = static_cast<const T*>(a.f[0]);
-    const T* f1 = static_cast<const T*>(a.f[1]);
-    double xcr = double(f0[i]), xnb = double(f1[i]);
-    if (a.c[0]) xcr -= double(a.c[0][ic]);
-    if (a.c[1]) xnb -= double(a.c[1][ic]);
-    double phd, phl;
-    if (a.phi_fix) {
-      phd = double(static_cast<const int*>(a.f[2])[i]) * kPhiInvScaleD;
-      phl = double(static_cast<const int*>(a.f[3])[i]) * kPhiInvScaleD;
-    } else {
-      phd = double(static_cast<const T*>(a.f[2])[i]);
-      phl = double(static_cast<const T*>(a.f[3])[i]);
+    const size_t i = cell * a.stride;
+    double v[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) v[k] = double(static_cast<const T*>(a.f[k])[i]);
+    if (a.comp) {  // FP32 form: value = f - c
+      const float4 c = a.pack ? cq_unpack(static_cast<const uint2*>(a.comp)[cell])
+                              : static_cast<const float4*>(a.comp)[cell];
+      v[0] -= double(c.x);
+      v[1] -= double(c.y);
+      v[2] -= double(c.z);
+      v[3] -= double(c.w);
     }
+    const double xcr = v[0], xnb = v[1], phd = v[2], phl = v[3];
     const double pd = p64(phd), pl = p64(phl);
     acc.add(0, xcr);
     acc.add(1, xnb);

@@ -9,12 +9,11 @@ constexpr int kSumBlocks = 256;  // fixed partial-sum count (deterministic order
 
 struct SumArgs {
   const void* f[4];   // fields in the halo layout
-  const float* c[2];  // FP32 form: compensation of x_Cr, x_Nb (value = f - c), or nullptr
+  const void* comp;   // FP32 form: compensation records (value = f - c), or nullptr
+  int pack;           // comp holds packed 16-bit counts (else float4)
   int is_f32, is3d;
-  int phi_fix;        // phases in the FP32 form's 32-bit fixed point
   int compact;        // interior-only rows (FP32 form) instead of the ghost-ring layout
   int stride;         // elements between consecutive cells of f (4 for FP32 records)
-  int cstride;        // elements between consecutive cells of c
   int Nx, Ny, Nz, pitch;
   double* partial;    // scratch: kSumBlocks * 5 doubles
   double* out;        // 5 doubles (device)

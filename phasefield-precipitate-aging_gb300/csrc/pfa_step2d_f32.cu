@@ -1,9 +1,13 @@
 // pfa_step2d_f32.cu -- the FP32 precision form of the 2D step (sm_103a).
 //
 // Same step as the FP64 kernel (src/main.cpp:289-305 fused), arithmetic in
-// FP32, x_Cr / x_Nb Kahan-compensated, phases in 32-bit fixed point (or FP32
-// + Kahan).  At 48 bytes per cell the HBM budget leaves ~250 instructions per
-// cell, so the kernel is organised for instruction economy:
+// FP32 with every field Kahan-compensated (value = hi - c).  The gamma
+// solve is the equilibrium-referenced form (pfa_device.cuh, gamma_u32),
+// which keeps FP32 accurate inside precipitates where the plain num / den
+// form loses it to cancellation; rows whose phases are all below 1e-5 skip
+// the solve (x^gamma = X there).  At 48 bytes per cell the HBM budget leaves
+// ~250 instructions per cell, so the kernel is organised for instruction
+// economy:
 //  * each warp owns a strip of 30 output columns (lanes 1..30; lanes 0 and
 //    31 carry the neighbour columns) and streams down a segment of rows; the
 //    three rows a 5-point Laplacian needs live in registers, rotated by a
@@ -11,15 +15,14 @@
 //    through shared memory;
 //  * left / right neighbours come from __shfl_up / __shfl_down;
 //  * the state is stored as two records per cell -- A = {x_Cr, x_Nb, phi_del,
-//    phi_lav} (16 bytes) and B = Kahan compensations {c_Cr, c_Nb} (8 bytes,
-//    or 16 with compensated phases) -- so a row costs one 128-bit and one
-//    64-bit load and store and a single address per lane; records of the row
-//    after next are loaded one iteration ahead.
+//    phi_lav} (16 bytes) and B = the four compensations, packed into 16-bit
+//    counts (8 bytes, PACK) or as FP32 (16 bytes) -- so a row costs one
+//    128-bit and one 64-bit (128-bit) load and store and a single address per
+//    lane; records of the row after next are loaded one iteration ahead.
 //
 // Record layout: Ny rows of `pitch` records (pitch a multiple of 32), interior
 // cell (x, y) at record y * pitch + x, no ghost ring; zero-flux edges come
 // from clamped indexing (the mirror the reference's halo fill produces).
-// Fixed-point phases (FIX) keep their int32 bits in the float slots.
 #include <cstdint>
 #include <type_traits>
 
@@ -35,96 +38,66 @@ namespace {
 constexpr int kWarps = 4;  // warps (strips) per CTA
 constexpr int kCols = 30;  // output columns per warp; lanes 0 and 31 are halo
 
-// The values a neighbour needs: gamma compositions and the phases (FP32).
+// The values a neighbour needs: the gamma compositions as deviations
+// u = x^gamma - xe_gamma (the variable of the grand-potential difference;
+// their Laplacian is that of x^gamma) and the phases.
 struct Nb {
-  float gcr, gnb, pd, pl;
+  float u1, u2, pd, pl;
 };
 
-// Compensation record: {c_Cr, c_Nb} or {c_Cr, c_Nb, c_del, c_lav}.
-template <bool FIX>
-using CompT = typename std::conditional<FIX, float2, float4>::type;
+// Compensation record: packed 16-bit counts or four FP32 values.
+template <bool PACK>
+using CompT = typename std::conditional<PACK, uint2, float4>::type;
 
-template <bool FIX>
+template <bool PACK>
 struct Raw {
-  float4 a;      // x_Cr, x_Nb, phi_del, phi_lav (int bits when FIX)
-  CompT<FIX> c;  // Kahan compensations
+  float4 a;       // x_Cr, x_Nb, phi_del, phi_lav
+  CompT<PACK> c;  // Kahan compensations
 };
 
-template <bool FIX>
-__device__ __forceinline__ float phf(float bits) {
-  if constexpr (FIX)
-    return phi_of(__float_as_int(bits));
+template <bool PACK>
+__device__ __forceinline__ float4 comps(const CompT<PACK>& c) {
+  if constexpr (PACK)
+    return cq_unpack(c);
   else
-    return bits;
+    return c;
 }
 
-// gamma solve of one cell (approximate reciprocal: 2 ulp is far inside the
-// form's error budget)
-__device__ __forceinline__ Nb solve(const FastCoef& K, float X, float Y, float phd, float phl) {
-  const float pD = p32(phd), pL = p32(phl);
-  const float pG = p_gamma32(phd, phl, pD, pL);
-  const float m0 = pD * pD, m1 = pD * pG, m2 = pD * pL, m3 = pG * pG, m4 = pG * pL, m5 = pL * pL;
-  const float* d = K.den;
-  const float den = fmaf(d[0], m0, fmaf(d[1], m1, fmaf(d[2], m2, fmaf(d[3], m3, fmaf(d[4], m4, d[5] * m5)))));
-  const float r = __fdividef(1.0f, den);
-  float n[2];
-#pragma unroll
-  for (int c = 0; c < 2; c++) {
-    const float* a = K.num[c];
-    const float lx = fmaf(a[0], pD, fmaf(a[1], pG, a[2] * pL));
-    const float ly = fmaf(a[3], pD, fmaf(a[4], pG, a[5] * pL));
-    const float q = fmaf(a[6], m0, fmaf(a[7], m1, fmaf(a[8], m2, fmaf(a[9], m3, fmaf(a[10], m4, a[11] * m5)))));
-    n[c] = fmaf(X, lx, fmaf(Y, ly, q));
-  }
-  return Nb{n[0] * r, n[1] * r, phd, phl};
+// the composition compensations only (what the gamma solve needs)
+template <bool PACK>
+__device__ __forceinline__ float2 comps_x(const CompT<PACK>& c) {
+  if constexpr (PACK)
+    return make_float2(float((int(c.x) << 16) >> 16) * kCqXi, float(int(c.x) >> 16) * kCqXi);
+  else
+    return make_float2(c.x, c.y);
 }
 
-__device__ __forceinline__ int add_sat(int a, int b) {
-  int r;
-  asm("add.sat.s32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
-  return r;
-}
-
-// q + round(inc 2^29) with saturation; |q| stays <= kPhiQMax so that two
-// values differ by less than 2^31
-__device__ __forceinline__ int phi_step(int q, float inc) {
-  const int d = __float2int_rn(inc * kPhiScale);  // saturates on overflow
-  return max(-kPhiQMax, min(kPhiQMax, add_sat(q, d)));
-}
-
-// dF/dphi_i without the Laplacian term: -p'(phi) dP + 2 omega phi (phi-1)(2 phi-1)
-// + 2 alpha phi phi_j^2, Horner forms
-__device__ __forceinline__ float dF_local(float ph, float pj, float dP, float om2, float alpha2) {
-  const float t = fmaf(-ph, ph, ph);  // phi (1 - phi)
-  const float pp = 30.0f * t * t;     // p'(phi)
-  const float well = ph * fmaf(ph, fmaf(2.0f * om2, ph, -3.0f * om2), om2);
-  return fmaf(-pp, dP, fmaf(alpha2 * ph, pj * pj, well));
-}
-
-template <bool FIX>
+template <bool PACK>
 struct Stream {
   const Step2DArgs& a;
   const float4* A;        // this lane's column, row 0
-  const CompT<FIX>* B;
+  const CompT<PACK>* B;
   float4* Ao;
-  CompT<FIX>* Bo;
+  CompT<PACK>* Bo;
   int Ny, P;
   bool out;  // this lane writes its column
 
   __device__ __forceinline__ int row(int y) const { return min(max(y, 0), Ny - 1) * P; }
 
-  __device__ __forceinline__ Raw<FIX> load(int off) const { return Raw<FIX>{__ldg(A + off), __ldg(B + off)}; }
+  __device__ __forceinline__ Raw<PACK> load(int off) const {
+    return Raw<PACK>{__ldg(A + off), __ldg(B + off)};
+  }
 
   // update row y from its window (up, c, dn); rc = raw centre record
   __device__ __forceinline__ void update(int y, const Nb& up, const Nb& c, const Nb& dn,
-                                         const Raw<FIX>& rc) const {
+                                         const Raw<PACK>& rc) const {
     Nb w, e;
-    w.gcr = __shfl_up_sync(0xffffffffu, c.gcr, 1);
-    w.gnb = __shfl_up_sync(0xffffffffu, c.gnb, 1);
+    w.u1 = __shfl_up_sync(0xffffffffu, c.u1, 1);
+    w.u2 = __shfl_up_sync(0xffffffffu, c.u2, 1);
     w.pd = __shfl_up_sync(0xffffffffu, c.pd, 1);
     w.pl = __shfl_up_sync(0xffffffffu, c.pl, 1);
-    e.gcr = __shfl_down_sync(0xffffffffu, c.gcr, 1);
-    e.gnb = __shfl_down_sync(0xffffffffu, c.gnb, 1);
+    e.u1 = __shfl_down_sync(0xffffffffu, c.u1, 1);
+    e.u2 = __shfl_down_sync(0xffffffffu, c.u2, 1);
     e.pd = __shfl_down_sync(0xffffffffu, c.pd, 1);
     e.pl = __shfl_down_sync(0xffffffffu, c.pl, 1);
     const float idx2 = a.idx2f[0], idy2 = a.idx2f[1];
@@ -133,40 +106,31 @@ struct Stream {
       const float sy = (vn - vc) + (vs - vc);
       return fmaf(sx, idx2, sy * idy2);
     };
-    const float lapCr = lap(w.gcr, e.gcr, up.gcr, dn.gcr, c.gcr);
-    const float lapNb = lap(w.gnb, e.gnb, up.gnb, dn.gnb, c.gnb);
+    const float lapCr = lap(w.u1, e.u1, up.u1, dn.u1, c.u1);
+    const float lapNb = lap(w.u2, e.u2, up.u2, dn.u2, c.u2);
     const float lapD = lap(w.pd, e.pd, up.pd, dn.pd, c.pd);
     const float lapL = lap(w.pl, e.pl, up.pl, dn.pl, c.pl);
-    // Cahn-Hilliard, Kahan-compensated
+    const float4 cc = comps<PACK>(rc.c);
+    // Cahn-Hilliard
     const float X = rc.a.x, Y = rc.a.y;
-    const float ycr = fmaf(a.dtD[0][0], lapCr, a.dtD[0][1] * lapNb) - rc.c.x, tcr = X + ycr;
-    const float ynb = fmaf(a.dtD[1][0], lapCr, a.dtD[1][1] * lapNb) - rc.c.y, tnb = Y + ynb;
+    const float ycr = fmaf(a.dtD[0][0], lapCr, a.dtD[0][1] * lapNb) - cc.x, tcr = X + ycr;
+    const float ynb = fmaf(a.dtD[1][0], lapCr, a.dtD[1][1] * lapNb) - cc.y, tnb = Y + ynb;
     // Allen-Cahn
     const FastCoef& K = a.k;
-    const float u1 = c.gcr - K.xe_gam[0], u2 = c.gnb - K.xe_gam[1];
-    const float dFd = fmaf(-a.kap[0], lapD, dF_local(c.pd, c.pl, quad2(K.dP[0], u1, u2), a.om2[0], a.alpha2));
-    const float dFl = fmaf(-a.kap[1], lapL, dF_local(c.pl, c.pd, quad2(K.dP[1], u1, u2), a.om2[1], a.alpha2));
+    const float phd = c.pd, phl = c.pl;
+    const float dFd = fmaf(-a.kap[0], lapD, dF_local32(phd, phl, quad2(K.dP[0], c.u1, c.u2), a.om2[0], a.alpha2));
+    const float dFl = fmaf(-a.kap[1], lapL, dF_local32(phl, phd, quad2(K.dP[1], c.u1, c.u2), a.om2[1], a.alpha2));
+    const float yd = fmaf(-a.dtL[0], dFd, -cc.z), td = phd + yd;
+    const float yl = fmaf(-a.dtL[1], dFl, -cc.w), tl = phl + yl;
     if (out) {
       const int i = y * P;
-      float4 o;
-      CompT<FIX> oc;
-      o.x = tcr;
-      o.y = tnb;
-      oc.x = (tcr - X) - ycr;
-      oc.y = (tnb - Y) - ynb;
-      if constexpr (FIX) {
-        o.z = __int_as_float(phi_step(__float_as_int(rc.a.z), -a.dtL[0] * dFd));
-        o.w = __int_as_float(phi_step(__float_as_int(rc.a.w), -a.dtL[1] * dFl));
-      } else {
-        const float yd = fmaf(-a.dtL[0], dFd, -rc.c.z), td = c.pd + yd;
-        const float yl = fmaf(-a.dtL[1], dFl, -rc.c.w), tl = c.pl + yl;
-        o.z = td;
-        o.w = tl;
-        oc.z = (td - c.pd) - yd;
-        oc.w = (tl - c.pl) - yl;
-      }
-      Ao[i] = o;
-      Bo[i] = oc;
+      Ao[i] = make_float4(tcr, tnb, td, tl);
+      const float ox = (tcr - X) - ycr, oy = (tnb - Y) - ynb;
+      const float od = (td - phd) - yd, ol = (tl - phl) - yl;
+      if constexpr (PACK)
+        Bo[i] = cq_pack(ox, oy, od, ol);
+      else
+        Bo[i] = make_float4(ox, oy, od, ol);
     }
   }
 };
@@ -174,22 +138,31 @@ struct Stream {
 // One warp updates the strip of output columns x0 .. x0+29 over rows
 // y0 .. y1-1 of one grid (the unit of work of both the single-grid and the
 // batched kernels).  Whole warp; x0 < Nx.
-template <bool FIX>
+template <bool PACK>
 __device__ __forceinline__ void stream_strip(const Step2DArgs& a, const float4* Ain,
-                                             const CompT<FIX>* Bin, float4* Aout,
-                                             CompT<FIX>* Bout, int Nx, int Ny, int P, int x0,
+                                             const CompT<PACK>* Bin, float4* Aout,
+                                             CompT<PACK>* Bout, int Nx, int Ny, int P, int x0,
                                              int y0, int y1) {
   const int lane = threadIdx.x & 31;
   const int gx = x0 - 1 + lane;  // lanes 0 and 31 hold the neighbour columns
   const int cx = min(max(gx, 0), Nx - 1);
   const FastCoef& K = a.k;
-  const Stream<FIX> S{a, Ain + cx, Bin + cx, Aout + cx, Bout + cx,
-                      Ny, P, lane >= 1 && lane <= kCols && gx < Nx};
-  auto solve_raw = [&](const Raw<FIX>& r) {
-    return solve(K, r.a.x, r.a.y, phf<FIX>(r.a.z), phf<FIX>(r.a.w));
+  const Stream<PACK> S{a, Ain + cx, Bin + cx, Aout + cx, Bout + cx,
+                       Ny, P, lane >= 1 && lane <= kCols && gx < Nx};
+  auto solve_raw = [&](const Raw<PACK>& r) {
+    const float2 cxy = comps_x<PACK>(r.c);
+    Nb n;
+    n.pd = r.a.z;
+    n.pl = r.a.w;
+    // warp-uniform choice: a row of pure gamma needs no solve
+    if (__all_sync(0xffffffffu, fmaxf(fabsf(r.a.z), fabsf(r.a.w)) < kBulkPhi))
+      gamma_bulk32(K, r.a.x, r.a.y, cxy.x, cxy.y, n.u1, n.u2);
+    else
+      gamma_u32(K, r.a.x, r.a.y, cxy.x, cxy.y, r.a.z, r.a.w, n.u1, n.u2);
+    return n;
   };
   // window rows y-1, y, y+1 and raw records of rows y, y+1, y+2
-  Raw<FIX> r0 = S.load(S.row(y0)), r1 = S.load(S.row(y0 + 1)), r2;
+  Raw<PACK> r0 = S.load(S.row(y0)), r1 = S.load(S.row(y0 + 1)), r2;
   Nb n0 = solve_raw(S.load(S.row(y0 - 1))), n1 = solve_raw(r0), n2;
   // three rows per iteration with rotated roles: no register moves
   int y = y0;
@@ -215,16 +188,16 @@ __device__ __forceinline__ void stream_strip(const Step2DArgs& a, const float4* 
   }
 }
 
-template <bool FIX>
+template <bool PACK>
 __global__ void __launch_bounds__(32 * kWarps, 8) k_stream_f32(Step2DArgs a) {
   const int strip = blockIdx.x * kWarps + (threadIdx.x >> 5);
   const int x0 = strip * kCols;  // first output column of the strip
   if (x0 >= a.Nx) return;        // whole warp leaves together
   const int y0 = blockIdx.y * a.rows;
-  stream_strip<FIX>(a, static_cast<const float4*>(a.in[0]),
-                    static_cast<const CompT<FIX>*>(a.in[1]), static_cast<float4*>(a.out[0]),
-                    static_cast<CompT<FIX>*>(a.out[1]), a.Nx, a.Ny, a.pitch, x0, y0,
-                    min(y0 + a.rows, a.Ny));
+  stream_strip<PACK>(a, static_cast<const float4*>(a.in[0]),
+                     static_cast<const CompT<PACK>*>(a.in[1]), static_cast<float4*>(a.out[0]),
+                     static_cast<CompT<PACK>*>(a.out[1]), a.Nx, a.Ny, a.pitch, x0, y0,
+                     min(y0 + a.rows, a.Ny));
 }
 
 // ---- many grids in one launch ----
@@ -259,20 +232,18 @@ __global__ void k_import_records(ConvArgs a) {
   if (gx >= a.Nx || gy >= a.Ny) return;
   const size_t i64 = size_t(gy + 1) * a.pitch64 + gx + 1;
   const size_t r = size_t(gy) * a.pitch32 + gx;
-  float* A = a.A + 4 * r;
-  float* B = a.B + size_t(a.bstride) * r;
+  float hi[4], c[4];
 #pragma unroll
   for (int k = 0; k < 4; k++) {
     const double v = a.f64[k][i64];
-    if (k >= 2 && a.phi_fix) {
-      A[k] = __int_as_float(phi_quantize(v));
-      continue;
-    }
-    const float hi = float(v);
-    A[k] = hi;
-    // compensation c holds -(low part): value = hi - c
-    if (k < a.bstride) B[k] = float(double(hi) - v);
+    hi[k] = float(v);
+    c[k] = float(double(hi[k]) - v);  // value = hi - c
   }
+  reinterpret_cast<float4*>(a.A)[r] = make_float4(hi[0], hi[1], hi[2], hi[3]);
+  if (a.pack)
+    static_cast<uint2*>(a.B)[r] = cq_pack(c[0], c[1], c[2], c[3]);
+  else
+    static_cast<float4*>(a.B)[r] = make_float4(c[0], c[1], c[2], c[3]);
 }
 
 __global__ void k_export_records(ConvArgs a) {
@@ -280,34 +251,30 @@ __global__ void k_export_records(ConvArgs a) {
   const int gy = blockIdx.y * blockDim.y + threadIdx.y;
   if (gx >= a.Nx || gy >= a.Ny) return;
   const size_t r = size_t(gy) * a.pitch32 + gx;
-  const float* A = a.A + 4 * r;
-  const float* B = a.B + size_t(a.bstride) * r;
+  const float4 v = reinterpret_cast<const float4*>(a.A)[r];
+  const float4 c = a.pack ? cq_unpack(static_cast<const uint2*>(a.B)[r])
+                          : static_cast<const float4*>(a.B)[r];
+  const double val[4] = {double(v.x) - double(c.x), double(v.y) - double(c.y),
+                         double(v.z) - double(c.z), double(v.w) - double(c.w)};
   const size_t row = size_t(gy + 1) * a.pitch64;
 #pragma unroll
   for (int k = 0; k < 4; k++) {
-    double v;
-    if (k >= 2 && a.phi_fix) {
-      v = double(__float_as_int(A[k])) * kPhiInvScaleD;
-    } else {
-      v = double(A[k]);
-      if (k < a.bstride) v -= double(B[k]);
-    }
     double* f = a.f64[k];
-    f[row + gx + 1] = v;
+    f[row + gx + 1] = val[k];
     // ghost ring = mirror of the interior; corners take the diagonal cell
     const bool l = gx == 0, rr = gx == a.Nx - 1, b = gy == 0, t = gy == a.Ny - 1;
-    if (l) f[row] = v;
-    if (rr) f[row + a.Nx + 1] = v;
+    if (l) f[row] = val[k];
+    if (rr) f[row + a.Nx + 1] = val[k];
     if (b) {
-      f[gx + 1] = v;
-      if (l) f[0] = v;
-      if (rr) f[a.Nx + 1] = v;
+      f[gx + 1] = val[k];
+      if (l) f[0] = val[k];
+      if (rr) f[a.Nx + 1] = val[k];
     }
     if (t) {
       const size_t top = size_t(a.Ny + 1) * a.pitch64;
-      f[top + gx + 1] = v;
-      if (l) f[top] = v;
-      if (rr) f[top + a.Nx + 1] = v;
+      f[top + gx + 1] = val[k];
+      if (l) f[top] = val[k];
+      if (rr) f[top + a.Nx + 1] = val[k];
     }
   }
 }
@@ -335,7 +302,7 @@ int segment_rows(int Nx, int Ny, int resident) {
   return best;
 }
 
-int g_resident[3] = {0, 0, 0};  // resident CTAs: the two variants, the batch kernel
+int g_resident[3] = {0, 0, 0};  // resident CTAs: FP32 / packed variants, the batch kernel
 
 template <typename K>
 cudaError_t query_resident(K kernel, int slot) {
@@ -348,20 +315,20 @@ cudaError_t query_resident(K kernel, int slot) {
   return e;
 }
 
-template <bool FIX>
+template <bool PACK>
 cudaError_t launch_stream(Step2DArgs a, cudaStream_t s) {
-  const int resident = g_resident[FIX] > 0 ? g_resident[FIX] : 152 * 8;
+  const int resident = g_resident[PACK] > 0 ? g_resident[PACK] : 152 * 8;
   a.rows = segment_rows(a.Nx, a.Ny, resident);
   const int strips = (a.Nx + kCols - 1) / kCols;
   dim3 grid((strips + kWarps - 1) / kWarps, (a.Ny + a.rows - 1) / a.rows);
-  k_stream_f32<FIX><<<grid, 32 * kWarps, 0, s>>>(a);
+  k_stream_f32<PACK><<<grid, 32 * kWarps, 0, s>>>(a);
   return cudaGetLastError();
 }
 
 }  // namespace
 
 cudaError_t launch_step2d_f32(const Step2DArgs& a, cudaStream_t s) {
-  return a.kahan_phi ? launch_stream<false>(a, s) : launch_stream<true>(a, s);
+  return a.full_comp ? launch_stream<false>(a, s) : launch_stream<true>(a, s);
 }
 
 // occupancy of the FP32 kernels on the current device (outside any capture)

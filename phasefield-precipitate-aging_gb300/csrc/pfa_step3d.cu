@@ -5,9 +5,10 @@
 // fill.  One kernel template serves both forms:
 //   F64: plain FP64, the reference's formulas, ghost-ring layout
 //        ((Nz+2) planes of (Ny+2) rows of Nx+2 doubles, one array per field);
-//   F32: the precision form (FP32 arithmetic, Kahan-compensated x_Cr, x_Nb,
-//        fixed-point phases) on interior-only records (pfa_step2d_f32.cu):
-//        A = float4 {x_Cr, x_Nb, phi_del, phi_lav}, B = float2 {c_Cr, c_Nb}.
+//   F32: the precision form (FP32 arithmetic, every field Kahan-compensated,
+//        the equilibrium-referenced gamma solve) on interior-only records
+//        (pfa_step2d_f32.cu): A = float4 {x_Cr, x_Nb, phi_del, phi_lav},
+//        B = the four compensations as packed 16-bit counts (uint2).
 // A CTA of 16 warps covers 30 x-columns (lanes 1..30) by 14 y-rows (warps
 // 1..14) and streams along z; lanes 0 / 31 and warps 0 / 15 carry the
 // neighbour columns and rows.  x-neighbours come from shuffles, y-neighbours
@@ -35,22 +36,12 @@ struct Nb3 {
   R gcr, gnb, pd, pl;
 };
 
+// F64: gcr / gnb are x^gamma; F32: the deviations u = x^gamma - xe_gamma
 template <class R>
 struct Raw3 {
-  R x, y, pd, pl;  // F32: pd / pl hold the fixed-point bits
-  float cx, cy;    // F32: Kahan compensations
+  R x, y, pd, pl;
+  uint2 cq;  // F32: packed Kahan compensations
 };
-
-__device__ __forceinline__ int add_sat3(int a, int b) {
-  int r;
-  asm("add.sat.s32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
-  return r;
-}
-
-__device__ __forceinline__ int phi_step3(int q, float inc) {
-  const int d = __float2int_rn(inc * kPhiScale);
-  return max(-kPhiQMax, min(kPhiQMax, add_sat3(q, d)));
-}
 
 // FP64 store of the interior cell (x, y, z) and of every ghost cell whose
 // nearest interior cell it is (the six-face fill; edges and corners take the
@@ -92,54 +83,37 @@ struct S3 {
       r.y = __ldg(static_cast<const double*>(a.in[1]) + i);
       r.pd = __ldg(static_cast<const double*>(a.in[2]) + i);
       r.pl = __ldg(static_cast<const double*>(a.in[3]) + i);
-      r.cx = r.cy = 0.f;
+      r.cq = make_uint2(0u, 0u);
     } else {
       const float4 v = __ldg(static_cast<const float4*>(a.in[0]) + i);
-      const float2 c = __ldg(static_cast<const float2*>(a.in[1]) + i);
       r.x = v.x;
       r.y = v.y;
       r.pd = v.z;
       r.pl = v.w;
-      r.cx = c.x;
-      r.cy = c.y;
+      r.cq = __ldg(static_cast<const uint2*>(a.in[1]) + i);
     }
     return r;
   }
 
-  __device__ __forceinline__ R ph(R bits) const {
-    if constexpr (F64)
-      return bits;
-    else
-      return phi_of(__float_as_int(bits));
-  }
-
-  // gamma solve of one cell
+  // gamma solve of one cell (F32: warp-uniform bulk / equilibrium-referenced
+  // forms, pfa_device.cuh)
   __device__ __forceinline__ Nb3<R> solve(const Raw3<R>& r) const {
-    const R d = ph(r.pd), l = ph(r.pl);
     if constexpr (F64) {
-      const double pD = p64(d), pL = p64(l), pG = 1.0 - pD - pL;
+      const double pD = p64(r.pd), pL = p64(r.pl), pG = 1.0 - pD - pL;
       Poly64 m;
       poly64(pD, pG, pL, m);
-      return Nb3<R>{fict64<0, 0>(r.x, r.y, m), fict64<0, 1>(r.x, r.y, m), d, l};
+      return Nb3<R>{fict64<0, 0>(r.x, r.y, m), fict64<0, 1>(r.x, r.y, m), r.pd, r.pl};
     } else {
-      const FastCoef& K = a.k;
-      const float pD = p32(d), pL = p32(l), pG = p_gamma32(d, l, pD, pL);
-      const float m0 = pD * pD, m1 = pD * pG, m2 = pD * pL, m3 = pG * pG, m4 = pG * pL, m5 = pL * pL;
-      const float* q = K.den;
-      const float den =
-          fmaf(q[0], m0, fmaf(q[1], m1, fmaf(q[2], m2, fmaf(q[3], m3, fmaf(q[4], m4, q[5] * m5)))));
-      const float rr = __fdividef(1.0f, den);
-      float n[2];
-#pragma unroll
-      for (int c = 0; c < 2; c++) {
-        const float* k = K.num[c];
-        const float lx = fmaf(k[0], pD, fmaf(k[1], pG, k[2] * pL));
-        const float ly = fmaf(k[3], pD, fmaf(k[4], pG, k[5] * pL));
-        const float qq =
-            fmaf(k[6], m0, fmaf(k[7], m1, fmaf(k[8], m2, fmaf(k[9], m3, fmaf(k[10], m4, k[11] * m5)))));
-        n[c] = fmaf(r.x, lx, fmaf(r.y, ly, qq));
-      }
-      return Nb3<R>{n[0] * rr, n[1] * rr, d, l};
+      const float cx = float((int(r.cq.x) << 16) >> 16) * kCqXi;
+      const float cy = float(int(r.cq.x) >> 16) * kCqXi;
+      Nb3<R> n;
+      n.pd = r.pd;
+      n.pl = r.pl;
+      if (__all_sync(0xffffffffu, fmaxf(fabsf(r.pd), fabsf(r.pl)) < kBulkPhi))
+        gamma_bulk32(a.k, r.x, r.y, cx, cy, n.gcr, n.gnb);
+      else
+        gamma_u32(a.k, r.x, r.y, cx, cy, r.pd, r.pl, n.gcr, n.gnb);
+      return n;
     }
   }
 
@@ -213,27 +187,20 @@ struct S3 {
       const float lapNb = lap(up.gnb, s.gnb, wv.gnb, c.gnb, e.gnb, n.gnb, dn.gnb);
       const float lapD = lap(up.pd, s.pd, wv.pd, c.pd, e.pd, n.pd, dn.pd);
       const float lapL = lap(up.pl, s.pl, wv.pl, c.pl, e.pl, n.pl, dn.pl);
-      const float X = rc.x, Y = rc.y;
-      const float ycr = fmaf(a.dtD[0][0], lapCr, a.dtD[0][1] * lapNb) - rc.cx, tcr = X + ycr;
-      const float ynb = fmaf(a.dtD[1][0], lapCr, a.dtD[1][1] * lapNb) - rc.cy, tnb = Y + ynb;
+      const float4 cc = cq_unpack(rc.cq);
+      const float X = rc.x, Y = rc.y, pd = rc.pd, pl = rc.pl;
+      const float ycr = fmaf(a.dtD[0][0], lapCr, a.dtD[0][1] * lapNb) - cc.x, tcr = X + ycr;
+      const float ynb = fmaf(a.dtD[1][0], lapCr, a.dtD[1][1] * lapNb) - cc.y, tnb = Y + ynb;
       const FastCoef& K = a.k;
-      const float u1 = c.gcr - K.xe_gam[0], u2 = c.gnb - K.xe_gam[1];
-      auto dF = [&](float p, float q, float dP, float om2) {
-        const float t = fmaf(-p, p, p);
-        const float pp = 30.0f * t * t;
-        const float well = p * fmaf(p, fmaf(2.0f * om2, p, -3.0f * om2), om2);
-        return fmaf(-pp, dP, fmaf(a.alpha2 * p, q * q, well));
-      };
-      const float dFd = fmaf(-a.kap[0], lapD, dF(c.pd, c.pl, quad2(K.dP[0], u1, u2), a.om2[0]));
-      const float dFl = fmaf(-a.kap[1], lapL, dF(c.pl, c.pd, quad2(K.dP[1], u1, u2), a.om2[1]));
+      const float u1 = c.gcr, u2 = c.gnb;
+      const float dFd = fmaf(-a.kap[0], lapD, dF_local32(pd, pl, quad2(K.dP[0], u1, u2), a.om2[0], a.alpha2));
+      const float dFl = fmaf(-a.kap[1], lapL, dF_local32(pl, pd, quad2(K.dP[1], u1, u2), a.om2[1], a.alpha2));
+      const float yd = fmaf(-a.dtL[0], dFd, -cc.z), td = pd + yd;
+      const float yl = fmaf(-a.dtL[1], dFl, -cc.w), tl = pl + yl;
       const long long i = cell(z);
-      float4 o;
-      o.x = tcr;
-      o.y = tnb;
-      o.z = __int_as_float(phi_step3(__float_as_int(rc.pd), -a.dtL[0] * dFd));
-      o.w = __int_as_float(phi_step3(__float_as_int(rc.pl), -a.dtL[1] * dFl));
-      static_cast<float4*>(a.out[0])[i] = o;
-      static_cast<float2*>(a.out[1])[i] = make_float2((tcr - X) - ycr, (tnb - Y) - ynb);
+      static_cast<float4*>(a.out[0])[i] = make_float4(tcr, tnb, td, tl);
+      static_cast<uint2*>(a.out[1])[i] =
+          cq_pack((tcr - X) - ycr, (tnb - Y) - ynb, (td - pd) - yd, (tl - pl) - yl);
     }
   }
 };
@@ -282,17 +249,15 @@ __global__ void k_import3d(Conv3DArgs a) {
     const int x = int(t % a.Nx), y = int((t / a.Nx) % a.Ny), z = int(t / ((long long)a.Nx * a.Ny));
     const long long i64 = ((long long)(z + 1) * (a.Ny + 2) + (y + 1)) * (a.Nx + 2) + (x + 1);
     const long long r = ((long long)z * a.Ny + y) * a.pitch32 + x;
-    float4 v;
-    float2 c;
-    const double X = a.f64[0][i64], Y = a.f64[1][i64];
-    v.x = float(X);
-    v.y = float(Y);
-    c.x = float(double(v.x) - X);
-    c.y = float(double(v.y) - Y);
-    v.z = __int_as_float(phi_quantize(a.f64[2][i64]));
-    v.w = __int_as_float(phi_quantize(a.f64[3][i64]));
-    reinterpret_cast<float4*>(a.A)[r] = v;
-    reinterpret_cast<float2*>(a.B)[r] = c;
+    float hi[4], c[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const double v = a.f64[k][i64];
+      hi[k] = float(v);
+      c[k] = float(double(hi[k]) - v);  // value = hi - c
+    }
+    reinterpret_cast<float4*>(a.A)[r] = make_float4(hi[0], hi[1], hi[2], hi[3]);
+    static_cast<uint2*>(a.B)[r] = cq_pack(c[0], c[1], c[2], c[3]);
   }
 }
 
@@ -308,11 +273,11 @@ __global__ void k_export3d(Conv3DArgs a) {
     const int x = int(t % a.Nx), y = int((t / a.Nx) % a.Ny), z = int(t / ((long long)a.Nx * a.Ny));
     const long long r = ((long long)z * a.Ny + y) * a.pitch32 + x;
     const float4 v = reinterpret_cast<const float4*>(a.A)[r];
-    const float2 c = reinterpret_cast<const float2*>(a.B)[r];
+    const float4 c = cq_unpack(static_cast<const uint2*>(a.B)[r]);
     store64(a.f64[0], g, x, y, z, double(v.x) - double(c.x));
     store64(a.f64[1], g, x, y, z, double(v.y) - double(c.y));
-    store64(a.f64[2], g, x, y, z, double(__float_as_int(v.z)) * kPhiInvScaleD);
-    store64(a.f64[3], g, x, y, z, double(__float_as_int(v.w)) * kPhiInvScaleD);
+    store64(a.f64[2], g, x, y, z, double(v.z) - double(c.z));
+    store64(a.f64[3], g, x, y, z, double(v.w) - double(c.w));
   }
 }
 
