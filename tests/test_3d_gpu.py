@@ -67,7 +67,7 @@ def test_fp32_3d_error_against_fp64(pfa):
     fa, fb = a.read(), b.read()
     err = [float(np.max(np.abs(x[1:-1, 1:-1, 1:-1] - y[1:-1, 1:-1, 1:-1]))) for x, y in zip(fa, fb)]
     print("3D fp32 max field error after 300 steps", err)
-    assert max(err) <= 1e-5, err
+    assert max(err) <= 5e-7, err  # stated bound 1e-5; the form holds far less
     sa, sb = a.summarize(), b.summarize()
     np.testing.assert_allclose(sa[:2], sb[:2], rtol=0, atol=1e-9)
     a.close()

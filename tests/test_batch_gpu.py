@@ -152,7 +152,7 @@ def test_fp32_batch_error_against_fp64(pfa):
         err = [float(np.max(np.abs(x[1:-1, 1:-1] - y[1:-1, 1:-1])))
                for x, y in zip(b.read(s), g.read())]
         g.close()
-        assert max(err) <= 1e-5, err
+        assert max(err) <= 5e-7, err  # stated bound 1e-5; the form holds far less
     b.close()
 
 

@@ -14,7 +14,8 @@ from conftest import field_err, fields_of, golden, interior
 pytestmark = pytest.mark.gpu
 
 FP64_TOL = 1e-12
-FP32_TOL = 1e-5
+FP32_TOL = 1e-5          # the stated bound: max |FP32 - FP64| per field
+FP32_TOL_1000 = 2e-7     # what the form holds after 1000 steps (measured ~4e-8)
 
 
 def _params(pfa):
@@ -147,8 +148,48 @@ def test_fp32_error_against_fp64(pfa, orc, precision):
     got = grid.read()
     err = [float(np.max(np.abs(interior(a) - interior(b)))) for a, b in zip(got, want)]
     print(precision, "max field error", err)
-    assert max(err) <= FP32_TOL, err
+    assert max(err) <= FP32_TOL_1000, err
     grid.close()
+
+
+def test_fp32_long_run_error(pfa):
+    """Error growth over a long run on a grid with precipitates and stripes:
+    the form's error comes from systematic FP32 rounding, so it is checked at
+    the step counts the workloads run (4000 steps here; 10 000 in the bench's
+    stated-error workload)."""
+    from pfa_gb300 import ic
+    f = ic.grid2d(256, 192, seed=21, stripes=[40, 150], stripe_width=32, n_particles=6,
+                  radius=7.0)
+    p = _params(pfa)
+    a = pfa.Grid2D(f, p, precision="fp32")
+    b = pfa.Grid2D(f, p)
+    for steps in (1000, 3000):
+        a.run(steps)
+        b.run(steps)
+    err = [float(np.max(np.abs(interior(x) - interior(y)))) for x, y in zip(a.read(), b.read())]
+    print("fp32 max field error after 4000 steps", err)
+    assert max(err) <= 1e-6, err
+    a.close()
+    b.close()
+
+
+def test_fp32_import_export_roundtrip(pfa):
+    """FP64 fields -> FP32 form (values + packed compensations) -> FP64: the
+    compensations carry each value to 2^-40 (compositions) / 2^-39 (phases)."""
+    from pfa_gb300 import ic
+    f = ic.grid2d(70, 52, seed=15, stripe_width=10, n_particles=2, radius=5.0)
+    for prec, tol in (("fp32", (2.0 ** -40, 2.0 ** -40, 2.0 ** -39, 2.0 ** -39)),
+                      ("fp32k", (1e-15,) * 4)):
+        p = _params(pfa)
+        g = pfa.Grid2D(f, p, precision=prec)
+        # a nucleation call with the physical parameters (no event is
+        # possible) imports the fields into the FP32 records and paints nothing
+        g.nucleate(dt_nuc=100 * p["dt"])
+        assert g.events() == []
+        got = g.read()
+        for k, (x, y) in enumerate(zip(got, f)):
+            assert float(np.max(np.abs(interior(x) - interior(y)))) <= tol[k], (prec, k)
+        g.close()
 
 
 def test_read_upload_roundtrip_and_summary(pfa, orc):
