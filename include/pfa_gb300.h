@@ -131,6 +131,18 @@ int pfa3d_upload(void* handle, const double* conc_Cr, const double* conc_Nb,
 int pfa3d_summarize(void* handle, double* out);
 /* free energy as pfa_summarize_energy, dV = dx dy dz, gradients in 3D */
 int pfa3d_summarize_energy(void* handle, double Omega, double* energy);
+/* Philox nucleation on a 3D grid after every step whose index k has
+ * k % interval == 0 (interval 0: off), the 2D call's physics with spheres
+ * (neighbourhood ball, spherical nucleus and depletion shells); dx, dy, dz
+ * and dt_nuc are the nucleation kernel's own (dV = dx dy dz, radii in cells
+ * of dx).  Resets the step and call counters.  No counterpart in the
+ * reference (2D only). */
+int pfa3d_set_nucleation(void* handle, uint64_t seed, int interval, double sigma_del,
+                         double sigma_lav, double unit_a, double dx, double dy, double dz,
+                         double dt_nuc);
+/* events of the last nucleation call, (cell, phase) in ascending cell order,
+ * cell = (z ny + y) nx + x in the ghost-ring layout; returns the count */
+int pfa3d_last_nucleation_events(void* handle, int64_t* cells, int32_t* phases, int cap);
 int pfa3d_destroy(void* handle);
 
 /* ---- batches of 2D grids (continuous batching) ----

@@ -186,6 +186,22 @@ class Oracle:
                   for k in range(min(n, max_events))]
         return a, events, n
 
+    def nucleation3d(self, fields, nuc, seed, call, max_events=1 << 16):
+        """3D form of nucleation2d (spheres)."""
+        a = [np.array(f, dtype=np.float64, copy=True) for f in fields]
+        nz, ny, nx = a[0].shape
+        pa = (_dbl_p * 4)(*[_ptr(x) for x in a])
+        ev = (OrcNucEvent * max_events)()
+        fn = getattr(self.lib, self.prefix + "nucleation3d")
+        fn.restype = ctypes.c_int
+        fn.argtypes = [ctypes.POINTER(_dbl_p), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                       ctypes.POINTER(OrcNucParams), ctypes.c_uint64, ctypes.c_uint64,
+                       ctypes.POINTER(OrcNucEvent), ctypes.c_int]
+        n = fn(pa, nx, ny, nz, ctypes.byref(nuc), seed, call, ev, max_events)
+        events = [(ev[k].cell, ev[k].phase, ev[k].xcr, ev[k].xnb, ev[k].r_precip)
+                  for k in range(min(n, max_events))]
+        return a, events, n
+
     def energy2d(self, fields, dx, dy, kappa, omega, Omega, maps=False):
         """Total free energy (and the per-node chemical / gradient maps),
         src/alloy625.cpp:752-807,865-919."""

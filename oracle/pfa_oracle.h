@@ -93,6 +93,10 @@ void orc_step3d(double* old_f[4], double* new_f[4], int nx, int ny, int nz,
 int orc_nucleation2d(double* f[4], int nx, int ny, const orc_nuc_params* np,
                      uint64_t seed, uint64_t call_index,
                      orc_nuc_event* events, int max_events);
+/* 3D form (spheres; cell = (z ny + y) nx + x in the ghost-ring layout) */
+int orc_nucleation3d(double* f[4], int nx, int ny, int nz, const orc_nuc_params* np,
+                     uint64_t seed, uint64_t call_index,
+                     orc_nuc_event* events, int max_events);
 
 /* ---- reductions (src/alloy625.cpp:811-863) ---- */
 void orc_summarize2d(const double* f[4], int nx, int ny, double out[5]);

@@ -333,6 +333,33 @@ static int SFN(nuc_decide)(double* const* f, int nx, int ny, int x, int y,
 
 /* Two-phase nucleation: every interior cell decides on the same snapshot,
  * then events are painted in ascending cell order, delta before laves. */
+/* The events of one call in canonical order -- ascending cell, delta before
+ * laves -- each with the composition of its cell on the snapshot every
+ * decision was taken from (an earlier nucleus painted over a later one's
+ * centre does not change the later one's depletion shells); terminated by
+ * an entry with phase -1.  Caller frees. */
+static orc_nuc_event* SFN(collect_events)(double* const* f, const unsigned char* mask,
+                                          const double* rad, size_t n)
+{
+	size_t m = 0;
+	for (size_t i = 0; i < n; i++)
+		m += (mask[i] & 1) + ((mask[i] >> 1) & 1);
+	orc_nuc_event* ev = (orc_nuc_event*)calloc(m + 1, sizeof(orc_nuc_event));
+	size_t k = 0;
+	for (size_t i = 0; i < n; i++)
+		for (int ph = 0; ph < 2; ph++)
+			if (mask[i] & (1 << ph)) {
+				ev[k].cell = (int64_t)i;
+				ev[k].phase = ph;
+				ev[k].xcr = f[0][i];
+				ev[k].xnb = f[1][i];
+				ev[k].r_precip = rad[2 * i + ph];
+				k++;
+			}
+	ev[m].phase = -1;
+	return ev;
+}
+
 int SFN(nucleation2d)(double* f[4], int nx, int ny, const orc_nuc_params* np,
                       uint64_t seed, uint64_t call, orc_nuc_event* events, int max_events)
 {
@@ -347,31 +374,21 @@ int SFN(nucleation2d)(double* f[4], int nx, int ny, const orc_nuc_params* np,
 			mask[i] = (unsigned char)SFN(nuc_decide)(f, nx, ny, x, y, np, seed, call,
 			                                           &rad[2 * i], &rad[2 * i + 1]);
 		}
+	orc_nuc_event* ev = SFN(collect_events)(f, mask, rad, n);
 	int count = 0;
-	for (size_t i = 0; i < n; i++) {
-		if (!mask[i])
-			continue;
-		const int x = (int)(i % nx), yy = (int)(i / nx);
-		const double xCr = f[0][i], xNb = f[1][i];
-		for (int ph = 0; ph < 2; ph++) {
-			if (!(mask[i] & (1 << ph)))
-				continue;
-			const double rp = rad[2 * i + ph];
-			if (count < max_events && events) {
-				events[count].cell = (int64_t)i;
-				events[count].phase = ph;
-				events[count].pad = 0;
-				events[count].xcr = xCr;
-				events[count].xnb = xNb;
-				events[count].r_precip = rp;
-			}
-			count++;
-			if (ph == 0)
-				SFN(embed)(f[0], f[1], f[2], nx, ny, x, yy, xCr, xNb, E_XE_DEL_CR, E_XE_DEL_NB, rp);
-			else
-				SFN(embed)(f[0], f[1], f[3], nx, ny, x, yy, xCr, xNb, E_XE_LAV_CR, E_XE_LAV_NB, rp);
-		}
+	for (; ev && ev[count].phase >= 0; count++) {
+		const orc_nuc_event* e = &ev[count];
+		const int x = (int)(e->cell % nx), yy = (int)(e->cell / nx);
+		if (e->phase == 0)
+			SFN(embed)(f[0], f[1], f[2], nx, ny, x, yy, e->xcr, e->xnb, E_XE_DEL_CR, E_XE_DEL_NB,
+			           e->r_precip);
+		else
+			SFN(embed)(f[0], f[1], f[3], nx, ny, x, yy, e->xcr, e->xnb, E_XE_LAV_CR, E_XE_LAV_NB,
+			           e->r_precip);
+		if (count < max_events && events)
+			events[count] = *e;
 	}
+	free(ev);
 	free(mask);
 	free(rad);
 	return count;
@@ -471,4 +488,126 @@ double SFN(energy2d)(const double* f[4], int nx, int ny, double dx, double dy,
 			energy += c + e;
 		}
 	return energy;
+}
+
+/* ---- 3D nucleation (no counterpart in the reference, which is 2D only) ----
+ * The 2D semantics above with spheres: the neighbourhood scan covers
+ * i^2 + j^2 + k^2 < R^2 and the nucleus and its depletion shells are
+ * spheres; offsets that leave the array along any axis are skipped (the 2D
+ * reference's row wrap-around is a property of its linear indexing that a
+ * 3D extension does not inherit).  Cell index: (z ny + y) nx + x in the
+ * ghost-ring layout. */
+static void SFN(embed3d)(double* cr, double* nb, double* phi, int nx, int ny, int nz,
+                         int x, int y, int z, double xCr, double xNb,
+                         double par_Cr, double par_Nb, double R_precip)
+{
+	const double R_dep_Cr = R_precip * sqrt((par_Cr - xCr) / (xCr - E_XE_GAM_CR));
+	const double R_dep_Nb = R_precip * sqrt((par_Nb - xNb) / (xNb - E_XE_GAM_NB));
+	for (int k = (int)(-R_precip); k < R_precip; k++)
+		for (int j = (int)(-R_precip); j < R_precip; j++)
+			for (int i = (int)(-R_precip); i < R_precip; i++) {
+				const int xx = x + i, yy = y + j, zz = z + k;
+				if (xx < 0 || xx >= nx || yy < 0 || yy >= ny || zz < 0 || zz >= nz)
+					continue;
+				const size_t idn = ((size_t)zz * ny + yy) * nx + xx;
+				const double r = sqrt((double)(i * i + j * j + k * k));
+				if (r <= R_precip) {
+					cr[idn] = par_Cr;
+					nb[idn] = par_Nb;
+					phi[idn] = 1.;
+				} else {
+					if (r <= R_dep_Cr)
+						cr[idn] = E_XE_GAM_CR;
+					if (r <= R_dep_Nb)
+						nb[idn] = E_XE_GAM_NB;
+				}
+			}
+}
+
+static int SFN(nuc_decide3d)(double* const* f, int nx, int ny, int nz, int x, int y, int z,
+                             const orc_nuc_params* np, uint64_t seed, uint64_t call,
+                             double* rd, double* rl)
+{
+	const double dV = np->dx * np->dy * np->dz;
+	const double Vatom = 0.25 * np->unit_a * np->unit_a * np->unit_a;
+	const double n_gam = dV / Vatom;
+	const double R = 1.75e-9 / np->dx;
+	double phi_pre = 0.;
+	for (int k = (int)(-R); k < R; k++)
+		for (int j = (int)(-R); j < R; j++)
+			for (int i = (int)(-R); i < R; i++) {
+				const int xx = x + i, yy = y + j, zz = z + k;
+				if (xx < 0 || xx >= nx || yy < 0 || yy >= ny || zz < 0 || zz >= nz)
+					continue;
+				if (i * i + j * j + k * k < R * R) {
+					const size_t idn = ((size_t)zz * ny + yy) * nx + xx;
+					phi_pre = fmax(phi_pre, E_P(f[2][idn]) + E_P(f[3][idn]));
+				}
+			}
+	if (!(phi_pre < 1e-10))
+		return 0;
+	const long long idx = ((long long)z * ny + y) * nx + x;
+	const double xCr = f[0][idx];
+	const double xNb = f[1][idx];
+	uint32_t ctr[4] = {(uint32_t)idx, (uint32_t)((uint64_t)idx >> 32),
+	                   (uint32_t)call, (uint32_t)(call >> 32)};
+	uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+	uint32_t w[4];
+	orc_philox4x32_10(ctr, key, w);
+	const double u[2] = {orc_u53(w[0], w[1]), orc_u53(w[2], w[3])};
+	const double dG = E_G_GAM(xCr, xNb);
+	const double dCrCr = E_D_CRCR(xCr, xNb);
+	const double dNbNb = E_D_NBNB(xCr, xNb);
+	int mask = 0;
+	for (int ph = 0; ph < 2; ph++) {
+		double Rstar = 0., P = 0.;
+		E_NUC_PROB(xCr, xNb, dG, dCrCr, dNbNb, np->sigma[ph], Vatom, n_gam, dV, np->dt, &Rstar, &P);
+		if (Rstar > 0.) {
+			const double rp = Rstar / np->dx;
+			if (P - u[ph] > 0) {
+				mask |= 1 << ph;
+				if (ph == 0)
+					*rd = rp;
+				else
+					*rl = rp;
+			}
+		}
+	}
+	return mask;
+}
+
+int SFN(nucleation3d)(double* f[4], int nx, int ny, int nz, const orc_nuc_params* np,
+                      uint64_t seed, uint64_t call, orc_nuc_event* events, int max_events)
+{
+	const size_t n = (size_t)nx * ny * nz;
+	unsigned char* mask = (unsigned char*)calloc(n, 1);
+	double* rad = (double*)calloc(2 * n, sizeof(double));
+	int z;
+	#pragma omp parallel for schedule(dynamic, 1)
+	for (z = 1; z < nz - 1; z++)
+		for (int y = 1; y < ny - 1; y++)
+			for (int x = 1; x < nx - 1; x++) {
+				const size_t i = ((size_t)z * ny + y) * nx + x;
+				mask[i] = (unsigned char)SFN(nuc_decide3d)(f, nx, ny, nz, x, y, z, np, seed, call,
+				                                             &rad[2 * i], &rad[2 * i + 1]);
+			}
+	orc_nuc_event* ev = SFN(collect_events)(f, mask, rad, n);
+	int count = 0;
+	for (; ev && ev[count].phase >= 0; count++) {
+		const orc_nuc_event* e = &ev[count];
+		const int x = (int)(e->cell % nx), y = (int)((e->cell / nx) % ny);
+		const int zz = (int)(e->cell / ((int64_t)nx * ny));
+		if (e->phase == 0)
+			SFN(embed3d)(f[0], f[1], f[2], nx, ny, nz, x, y, zz, e->xcr, e->xnb, E_XE_DEL_CR,
+			             E_XE_DEL_NB, e->r_precip);
+		else
+			SFN(embed3d)(f[0], f[1], f[3], nx, ny, nz, x, y, zz, e->xcr, e->xnb, E_XE_LAV_CR,
+			             E_XE_LAV_NB, e->r_precip);
+		if (count < max_events && events)
+			events[count] = *e;
+	}
+	free(ev);
+	free(mask);
+	free(rad);
+	return count;
 }

@@ -270,46 +270,8 @@ static int nucleate(CudaData* dev, State* s, double sig_d, double sig_l, double 
   // dx * nx and dy * ny; the fixed geometry passes the spacing itself.
   const double kdx = s->geometry == PFA_NUC_REFERENCE_GEOMETRY ? dx * s->nx : dx;
   const double kdy = s->geometry == PFA_NUC_REFERENCE_GEOMETRY ? dy * s->ny : dy;
-  const bool ok = std::isfinite(kdx) && std::isfinite(kdy) && std::isfinite(dz) &&
-                  std::isfinite(dt) && std::isfinite(unit_a) && kdx > 0 && kdy > 0 && dz > 0 &&
-                  dt > 0 && unit_a > 0 && std::isfinite(sig_d) && std::isfinite(sig_l);
-  if (!ok) return fail(PFA_EINVAL, "nucleation: spacing, time and lattice must be finite and > 0");
-  if (!(1.75e-9 / kdx <= kNucMaxScan))
-    return fail(PFA_EINVAL, "nucleation: neighbourhood scan radius 1.75 nm / dx exceeds 64 cells");
-  a.dx = kdx;
-  a.dV = kdx * kdy * dz;
-  a.Vatom = 0.25 * unit_a * unit_a * unit_a;
-  a.n_gam = a.dV / a.Vatom;
-  a.dt = dt;
-  a.R_scan = 1.75e-9 / kdx;
-  a.ln_dtdV = std::log(dt * a.dV);
-  a.ln_ngam = std::log(a.n_gam);
-  // the reference's loop `for (int i = -R; i < R; i++)` with the test
-  // i*i + j*j < R*R, in integers: lo = (int)(-R), hi = first int >= R,
-  // r2 = largest int < R*R
-  {
-    const double R = a.R_scan;
-    a.scan_lo = int(-R);
-    int hi = a.scan_lo;
-    while (double(hi) < R) hi++;
-    a.scan_hi = hi;
-    const double R2 = R * R;
-    long long m = (long long)std::floor(R2);
-    if (double(m) >= R2) m--;  // strictly below R^2
-    a.scan_r2 = int(m);
-  }
-  // constants of the FP32 screening bound (pfa_nucleation.cu, ln_z_bound):
-  // ln z <= lnC1 + max e - C2 / (dG^2 max dc)
-  for (int ph = 0; ph < 2; ph++) {
-    const double sg = a.sigma[ph], s3 = sg * sg * sg;
-    const double a4 = std::pow(kLatticeConst, 4);
-    const double lnDpre = std::log(3.0 * 1.5e-20 * 2.5e6);            // |D| prefactor bound
-    const double lnG = std::log(16.0 * kPi * s3 / 3.0);                  // G* dG^2
-    const double lnZ = std::log(a.Vatom / (8.0 * kPi * std::sqrt(kKT * s3)));  // Zeldovich / dG^2
-    a.lnC1[ph] = float(std::log(3.0) + lnG - std::log(sg) - std::log(a4) + lnDpre + lnZ +
-                       a.ln_ngam + std::log(2.0) + a.ln_dtdV);
-    a.C2[ph] = float(16.0 * kPi * s3 / (3.0 * kKT));
-  }
+  if (const char* msg = nucleation_constants(a, kdx, kdy, dz, dt, unit_a))
+    return fail(PFA_EINVAL, msg);
   a.seed = s->seed;
   a.call_ptr = s->call_dev;
   a.events = s->ev;

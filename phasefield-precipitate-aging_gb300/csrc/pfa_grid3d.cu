@@ -14,13 +14,14 @@
 #include "pfa_gb300.h"
 #include "pfa_internal.h"
 #include "pfa_kernels.h"
+#include "pfa_nucleation.h"
 #include "pfa_reduce.h"
 
 namespace pfa {
 namespace {
 
 struct Graph {
-  int len;
+  int len, nuc_first, cur;
   cudaGraphExec_t exec;
 };
 
@@ -39,6 +40,15 @@ struct Grid3D {
   double* sum_partial = nullptr;
   double* sum_out = nullptr;
   std::vector<Graph> graphs;
+  // nucleation after every step whose index k has k % nuc_interval == 0
+  uint64_t seed = 42;
+  int nuc_interval = 0;
+  double nuc_sigma[2] = {0.13, 0.13}, nuc_unit_a = 0.352e-9, nuc_d[3] = {}, nuc_dt = 0.0;
+  uint64_t step_counter = 0;
+  NucEvent* ev = nullptr;
+  unsigned* ev_count = nullptr;
+  int* ev_status = nullptr;
+  unsigned long long* call_dev = nullptr;  // Philox call counter
 };
 
 int err(int code, const char* what) {
@@ -140,36 +150,118 @@ int sync_f64(Grid3D* g) {
   return 0;
 }
 
+// Nucleation on the state after a step (3D form of pfa_nucleation.cu).
+int nucleate(Grid3D* g) {
+  NucArgs a{};
+  const int c = g->cur;
+  if (g->precision == PFA_FP64) {
+    for (int k = 0; k < 4; k++) a.f[k] = g->f64[c][k];
+    a.pitch = g->Nx + 2;
+    a.stride = 1;
+  } else {
+    for (int k = 0; k < 4; k++) a.f[k] = g->A[c] + k;
+    a.comp = g->B[c];
+    a.pack = 1;
+    a.stride = 4;
+    a.pitch = g->pitch32;
+    a.is_f32 = 1;
+    a.compact = 1;
+  }
+  a.Nx = g->Nx;
+  a.Ny = g->Ny;
+  a.Nz = g->Nz;
+  a.is3d = 1;
+  a.sigma[0] = g->nuc_sigma[0];
+  a.sigma[1] = g->nuc_sigma[1];
+  if (const char* msg =
+          nucleation_constants(a, g->nuc_d[0], g->nuc_d[1], g->nuc_d[2], g->nuc_dt, g->nuc_unit_a))
+    return err(PFA_EINVAL, msg);
+  a.seed = g->seed;
+  a.call_ptr = g->call_dev;
+  a.events = g->ev;
+  a.count = g->ev_count;
+  a.status = g->ev_status;
+  a.cap = kNucCap;
+  CK3(launch_nucleation(a, g->st));
+  return 0;
+}
+
+// len steps, with a nucleation call after the first when nuc_first
+int chunk(Grid3D* g, int len, bool nuc_first) {
+  for (int k = 0; k < len; k++) {
+    if (int r = step(g)) return r;
+    if (k == 0 && nuc_first)
+      if (int r = nucleate(g)) return r;
+  }
+  return 0;
+}
+
+// an even number of steps from a captured graph (the ping-pong ends where
+// it started)
+int graph_chunk(Grid3D* g, int len, bool nuc_first) {
+  cudaGraphExec_t exec = nullptr;
+  for (auto& e : g->graphs)
+    if (e.len == len && e.nuc_first == int(nuc_first) && e.cur == g->cur) exec = e.exec;
+  if (!exec) {
+    const int cur0 = g->cur;
+    cudaGraph_t graph;
+    CK3(cudaStreamBeginCapture(g->st, cudaStreamCaptureModeThreadLocal));
+    const int r = chunk(g, len, nuc_first);
+    const cudaError_t e = cudaStreamEndCapture(g->st, &graph);
+    if (r) return r;
+    if (e != cudaSuccess) return cuda_err(e, "cudaStreamEndCapture");
+    CK3(cudaGraphInstantiate(&exec, graph, 0));
+    cudaGraphDestroy(graph);
+    if (g->graphs.size() >= 8) {
+      cudaGraphExecDestroy(g->graphs.front().exec);
+      g->graphs.erase(g->graphs.begin());
+    }
+    g->graphs.push_back({len, int(nuc_first), cur0, exec});
+    g->cur = cur0;
+  }
+  CK3(cudaGraphLaunch(exec, g->st));
+  return 0;
+}
+
+int check_status(Grid3D* g) {
+  int st = 0;
+  CK3(cudaMemcpyAsync(&st, g->ev_status, sizeof(int), cudaMemcpyDeviceToHost, g->st));
+  CK3(cudaStreamSynchronize(g->st));
+  if (st) {
+    CK3(cudaMemsetAsync(g->ev_status, 0, sizeof(int), g->st));
+    if (st == 2) return err(PFA_EINVAL, "nucleation: a nucleus radius exceeded 256 cells (not painted)");
+    return err(PFA_EOVERFLOW, "nucleation: more events than the event buffer holds");
+  }
+  return 0;
+}
+
 int run(Grid3D* g, int nsteps) {
   if (int r = ensure_live(g)) return r;
   while (nsteps > 0) {
-    if (nsteps == 1) {
-      if (int r = step(g)) return r;
-      nsteps = 0;
-      break;
+    int len;
+    bool nuc_first = false;
+    if (g->nuc_interval > 0) {
+      const int phase = int(g->step_counter % uint64_t(g->nuc_interval));
+      nuc_first = phase == 0;
+      len = std::min(nsteps, g->nuc_interval - phase);
+    } else {
+      len = std::min(nsteps, 100);
     }
-    const int len = std::min(nsteps - nsteps % 2, 100);
-    cudaGraphExec_t exec = nullptr;
-    for (auto& e : g->graphs)
-      if (e.len == len) exec = e.exec;
-    if (!exec) {
-      const int cur0 = g->cur;
-      cudaGraph_t graph;
-      CK3(cudaStreamBeginCapture(g->st, cudaStreamCaptureModeThreadLocal));
-      int r = 0;
-      for (int k = 0; k < len && !r; k++) r = step(g);
-      const cudaError_t e = cudaStreamEndCapture(g->st, &graph);
-      if (r) return r;
-      if (e != cudaSuccess) return cuda_err(e, "cudaStreamEndCapture");
-      CK3(cudaGraphInstantiate(&exec, graph, 0));
-      cudaGraphDestroy(graph);
-      g->graphs.push_back({len, exec});
-      g->cur = cur0;  // an even count returns the ping-pong to where it was
+    if (len % 2) {
+      // one step outside the graphs, so that they see an even count
+      if (int r = chunk(g, 1, nuc_first)) return r;
+      g->step_counter += 1;
+      nsteps -= 1;
+      len -= 1;
+      nuc_first = false;
     }
-    CK3(cudaGraphLaunch(exec, g->st));
-    nsteps -= len;
+    if (len > 0) {
+      if (int r = graph_chunk(g, len, nuc_first)) return r;
+      g->step_counter += uint64_t(len);
+      nsteps -= len;
+    }
   }
-  return 0;
+  return g->nuc_interval > 0 ? check_status(g) : 0;
 }
 
 }  // namespace
@@ -218,6 +310,7 @@ int pfa3d_create(void** handle, int nx, int ny, int nz, const double* params, co
   static bool ready = false;
   if (!ready) {
     CK3(prepare_step3d());
+    CK3(nucleation_setup());
     ready = true;
   }
   CK3(cudaStreamCreateWithFlags(&g->st, cudaStreamNonBlocking));
@@ -240,8 +333,74 @@ int pfa3d_create(void** handle, int nx, int ny, int nz, const double* params, co
   }
   CK3(cudaMalloc(reinterpret_cast<void**>(&g->sum_partial), sizeof(double) * kSumBlocks * 5));
   CK3(cudaMalloc(reinterpret_cast<void**>(&g->sum_out), sizeof(double) * 5));
+  CK3(cudaMalloc(reinterpret_cast<void**>(&g->ev), sizeof(NucEvent) * kNucCap));
+  CK3(cudaMalloc(reinterpret_cast<void**>(&g->ev_count), sizeof(unsigned)));
+  CK3(cudaMalloc(reinterpret_cast<void**>(&g->ev_status), sizeof(int)));
+  CK3(cudaMalloc(reinterpret_cast<void**>(&g->call_dev), sizeof(unsigned long long)));
+  CK3(cudaMemsetAsync(g->ev_count, 0, sizeof(unsigned), g->st));
+  CK3(cudaMemsetAsync(g->ev_status, 0, sizeof(int), g->st));
+  CK3(cudaMemsetAsync(g->call_dev, 0, sizeof(unsigned long long), g->st));
   CK3(cudaStreamSynchronize(g->st));
   return 0;
+}
+
+int pfa3d_set_nucleation(void* handle, uint64_t seed, int interval, double sigma_del,
+                         double sigma_lav, double unit_a, double dx, double dy, double dz,
+                         double dt_nuc) {
+  Grid3D* g = static_cast<Grid3D*>(handle);
+  if (!g) return err(PFA_ESTATE, "pfa3d_set_nucleation: null handle");
+  if (interval < 0) return err(PFA_EINVAL, "pfa3d_set_nucleation: negative interval");
+  NucArgs a{};
+  a.sigma[0] = sigma_del;
+  a.sigma[1] = sigma_lav;
+  a.is3d = 1;
+  a.Nz = g->Nz;
+  if (interval > 0)
+    if (const char* msg = nucleation_constants(a, dx, dy, dz, dt_nuc, unit_a))
+      return err(PFA_EINVAL, msg);
+  CK3(cudaStreamSynchronize(g->st));
+  for (auto& e : g->graphs) cudaGraphExecDestroy(e.exec);
+  g->graphs.clear();
+  g->seed = seed;
+  g->nuc_interval = interval;
+  g->nuc_sigma[0] = sigma_del;
+  g->nuc_sigma[1] = sigma_lav;
+  g->nuc_unit_a = unit_a;
+  g->nuc_d[0] = dx;
+  g->nuc_d[1] = dy;
+  g->nuc_d[2] = dz;
+  g->nuc_dt = dt_nuc;
+  g->step_counter = 0;
+  CK3(cudaMemsetAsync(g->call_dev, 0, sizeof(unsigned long long), g->st));
+  CK3(cudaMemsetAsync(g->ev_count, 0, sizeof(unsigned), g->st));
+  CK3(cudaStreamSynchronize(g->st));
+  return 0;
+}
+
+int pfa3d_last_nucleation_events(void* handle, int64_t* cells, int32_t* phases, int cap) {
+  Grid3D* g = static_cast<Grid3D*>(handle);
+  if (!g) return err(PFA_ESTATE, "pfa3d_last_nucleation_events: null handle");
+  unsigned n = 0;
+  CK3(cudaMemcpyAsync(&n, g->ev_count, sizeof(unsigned), cudaMemcpyDeviceToHost, g->st));
+  CK3(cudaStreamSynchronize(g->st));
+  if (n > unsigned(kNucCap)) return err(PFA_EOVERFLOW, "nucleation event buffer overflowed");
+  std::vector<NucEvent> ev(n);
+  if (n) {
+    CK3(cudaMemcpyAsync(ev.data(), g->ev, n * sizeof(NucEvent), cudaMemcpyDeviceToHost, g->st));
+    CK3(cudaStreamSynchronize(g->st));
+  }
+  std::sort(ev.begin(), ev.end(), [](const NucEvent& a, const NucEvent& b) { return a.cell < b.cell; });
+  int k = 0;
+  for (const auto& e : ev)
+    for (int ph = 0; ph < 2; ph++)
+      if (e.mask & (1 << ph)) {
+        if (k < cap) {
+          if (cells) cells[k] = e.cell;
+          if (phases) phases[k] = ph;
+        }
+        k++;
+      }
+  return k;
 }
 
 int pfa3d_run(void* handle, int nsteps) {
@@ -368,6 +527,10 @@ int pfa3d_destroy(void* handle) {
   }
   cudaFree(g->sum_partial);
   cudaFree(g->sum_out);
+  cudaFree(g->ev);
+  cudaFree(g->ev_count);
+  cudaFree(g->ev_status);
+  cudaFree(g->call_dev);
   if (g->st) cudaStreamDestroy(g->st);
   delete g;
   return 0;

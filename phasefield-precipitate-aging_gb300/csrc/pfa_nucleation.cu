@@ -16,6 +16,7 @@
 // an event: if dt dV (J_Cr + J_Nb) < 1e-17 the FP64 P_nuc is 0 or 2^-53 and
 // no draw u >= 2^-53 can fall below it, so skipping such cells changes no
 // decision.
+#include <cmath>
 #include <cstdint>
 
 #include "pfa_device.cuh"
@@ -57,14 +58,16 @@ __device__ __forceinline__ double ld(const void* p, size_t i) {
   return double(static_cast<const T*>(p)[i]);
 }
 
-// Storage index of reference cell (xx, yy) (ghost-ring coordinates).  The
-// FP32 form stores the interior only: a ghost cell reads its mirror.
-__device__ __forceinline__ size_t stor(const NucArgs& a, int xx, int yy) {
+// Storage index of reference cell (xx, yy, zz) (ghost-ring coordinates; zz
+// = 0 in 2D).  The FP32 form stores the interior only: a ghost cell reads its
+// mirror.
+__device__ __forceinline__ size_t stor(const NucArgs& a, int xx, int yy, int zz = 0) {
   if (a.compact) {
     const int cx = min(max(xx - 1, 0), a.Nx - 1), cy = min(max(yy - 1, 0), a.Ny - 1);
-    return size_t(cy) * a.pitch + cx;
+    const int cz = a.is3d ? min(max(zz - 1, 0), a.Nz - 1) : 0;
+    return (size_t(cz) * a.Ny + cy) * a.pitch + cx;
   }
-  return size_t(yy) * a.pitch + xx;
+  return (size_t(zz) * (a.Ny + 2) + yy) * a.pitch + xx;
 }
 
 // Kahan compensation of field k at a cell of the FP32 form (value = f - c)
@@ -189,31 +192,45 @@ __global__ void __launch_bounds__(256) k_nuc_decide(NucArgs a) {
   bool ev = false;
   NucEvent e;
   if (gx < a.Nx && gy < a.Ny) {
-    const int x = gx + 1, y = gy + 1;
-    const long long idx = (long long)nxr * y + x;
+    const int x = gx + 1, y = gy + 1, z = a.is3d ? int(blockIdx.z) + 1 : 0;
+    const long long idx = ((long long)z * nyr + y) * nxr + x;
     bool clear = true;
-    // neighbourhood scan of src/discretization.cu:1104-1117 with the
-    // reference's double-valued bounds turned into integers on the host
-    // (i from (int)(-R) while i < R, i^2 + j^2 < R^2); the reference
-    // bounds-checks the linear index nx (y + j) + (x + i), so offsets past a
-    // row end wrap onto the next row -- reproduced by normalising (xx, yy)
-    for (int i = a.scan_lo; i < a.scan_hi && clear; i++)
-      for (int j = a.scan_lo; j < a.scan_hi && clear; j++) {
-        if (i * i + j * j > a.scan_r2) continue;
-        int xx = x + i, yy = y + j;
-        while (xx < 0) {
-          xx += nxr;
-          yy--;
+    if (a.is3d) {
+      // the same scan over a ball; offsets that leave the array along any
+      // axis are skipped (no counterpart in the reference)
+      const int nzr = a.Nz + 2;
+      for (int k = a.scan_lo; k < a.scan_hi && clear; k++)
+        for (int j = a.scan_lo; j < a.scan_hi && clear; j++)
+          for (int i = a.scan_lo; i < a.scan_hi && clear; i++) {
+            if (i * i + j * j + k * k > a.scan_r2) continue;
+            const int xx = x + i, yy = y + j, zz = z + k;
+            if (xx < 0 || xx >= nxr || yy < 0 || yy >= nyr || zz < 0 || zz >= nzr) continue;
+            clear = clear_at<T>(a, stor(a, xx, yy, zz));
+          }
+    } else {
+      // neighbourhood scan of src/discretization.cu:1104-1117 with the
+      // reference's double-valued bounds turned into integers on the host
+      // (i from (int)(-R) while i < R, i^2 + j^2 < R^2); the reference
+      // bounds-checks the linear index nx (y + j) + (x + i), so offsets past
+      // a row end wrap onto the next row -- reproduced by normalising (xx, yy)
+      for (int i = a.scan_lo; i < a.scan_hi && clear; i++)
+        for (int j = a.scan_lo; j < a.scan_hi && clear; j++) {
+          if (i * i + j * j > a.scan_r2) continue;
+          int xx = x + i, yy = y + j;
+          while (xx < 0) {
+            xx += nxr;
+            yy--;
+          }
+          while (xx >= nxr) {
+            xx -= nxr;
+            yy++;
+          }
+          if (yy < 0 || yy >= nyr) continue;
+          clear = clear_at<T>(a, stor(a, xx, yy));
         }
-        while (xx >= nxr) {
-          xx -= nxr;
-          yy++;
-        }
-        if (yy < 0 || yy >= nyr) continue;
-        clear = clear_at<T>(a, stor(a, xx, yy));
-      }
+    }
     if (clear) {
-      const size_t s = stor(a, x, y);
+      const size_t s = stor(a, x, y, z);
       const T Xs = static_cast<const T*>(a.f[0])[s * a.stride];
       const T Ys = static_cast<const T*>(a.f[1])[s * a.stride];
       // Screen in FP32 on the bound z_up of z = dt dV (J_Cr + J_Nb), which
@@ -317,6 +334,34 @@ __device__ void paint(const NucArgs& a, const NucEvent& e, int ph) {
   while (double(hi) < R) hi++;  // loop bound of `for (i = -R; i < R; i++)`
   const int w = hi - lo;
   if (w <= 0) return;
+  if (a.is3d) {
+    // spheres (no counterpart in the reference): offsets that leave the
+    // array along any axis are skipped
+    const int nyr = a.Ny + 2, nzr = a.Nz + 2;
+    const int x3 = int(e.cell % nxr), y3 = int((e.cell / nxr) % nyr);
+    const int z3 = int(e.cell / ((long long)nxr * nyr));
+    const long long n3 = (long long)w * w * w;
+    for (long long t = threadIdx.x; t < n3; t += blockDim.x) {
+      const int i = lo + int(t % w), j = lo + int((t / w) % w), k = lo + int(t / ((long long)w * w));
+      const int xx = x3 + i, yy = y3 + j, zz = z3 + k;
+      if (xx < 0 || xx >= nxr || yy < 0 || yy >= nyr || zz < 0 || zz >= nzr) continue;
+      // the FP32 form keeps no ghost ring: a nucleus never paints one there
+      if (a.compact && (xx == 0 || yy == 0 || zz == 0 || xx == nxr - 1 || yy == nyr - 1 ||
+                        zz == nzr - 1))
+        continue;
+      const size_t s = stor(a, xx, yy, zz);
+      const double r = sqrt(double(i * i + j * j + k * k));
+      if (r <= R) {
+        put<T>(a, 0, s, parCr);
+        put<T>(a, 1, s, parNb);
+        put<T>(a, 2 + ph, s, 1.0);
+      } else {
+        if (r <= RdCr) put<T>(a, 0, s, xgCr);
+        if (r <= RdNb) put<T>(a, 1, s, xgNb);
+      }
+    }
+    return;
+  }
   const long long n = (long long)w * w;
   for (long long t = threadIdx.x; t < n; t += blockDim.x) {
     const int i = lo + int(t / w), j = lo + int(t % w);
@@ -385,7 +430,7 @@ __global__ void __launch_bounds__(1024) k_nuc_apply(NucArgs a) {
 cudaError_t launch_nucleation(const NucArgs& a, cudaStream_t s) {
   cudaError_t err = cudaMemsetAsync(a.count, 0, sizeof(unsigned), s);
   if (err != cudaSuccess) return err;
-  dim3 grid((a.Nx + 31) / 32, (a.Ny + 7) / 8);
+  dim3 grid((a.Nx + 31) / 32, (a.Ny + 7) / 8, a.is3d ? a.Nz : 1);
   const size_t smem = sizeof(unsigned long long) * size_t(kNucCap);
   if (a.is_f32) {
     k_nuc_decide<float><<<grid, 256, 0, s>>>(a);
@@ -395,6 +440,50 @@ cudaError_t launch_nucleation(const NucArgs& a, cudaStream_t s) {
     k_nuc_apply<double><<<1, 1024, smem, s>>>(a);
   }
   return cudaGetLastError();
+}
+
+const char* nucleation_constants(NucArgs& a, double dx, double dy, double dz, double dt,
+                                 double unit_a) {
+  const bool ok = std::isfinite(dx) && std::isfinite(dy) && std::isfinite(dz) &&
+                  std::isfinite(dt) && std::isfinite(unit_a) && dx > 0 && dy > 0 && dz > 0 &&
+                  dt > 0 && unit_a > 0 && std::isfinite(a.sigma[0]) && std::isfinite(a.sigma[1]);
+  if (!ok) return "nucleation: spacing, time and lattice must be finite and > 0";
+  if (!(1.75e-9 / dx <= kNucMaxScan))
+    return "nucleation: neighbourhood scan radius 1.75 nm / dx exceeds 64 cells";
+  if (a.is3d && a.Nz > 65535) return "nucleation: more than 65535 planes";
+  a.dx = dx;
+  a.dV = dx * dy * dz;
+  a.Vatom = 0.25 * unit_a * unit_a * unit_a;
+  a.n_gam = a.dV / a.Vatom;
+  a.dt = dt;
+  a.R_scan = 1.75e-9 / dx;
+  a.ln_dtdV = std::log(dt * a.dV);
+  a.ln_ngam = std::log(a.n_gam);
+  // the reference's loop `for (int i = -R; i < R; i++)` with the test
+  // i*i + j*j < R*R, in integers: lo = (int)(-R), hi = first int >= R,
+  // r2 = largest int < R*R
+  const double R = a.R_scan;
+  a.scan_lo = int(-R);
+  int hi = a.scan_lo;
+  while (double(hi) < R) hi++;
+  a.scan_hi = hi;
+  const double R2 = R * R;
+  long long m = (long long)std::floor(R2);
+  if (double(m) >= R2) m--;  // strictly below R^2
+  a.scan_r2 = int(m);
+  // constants of the FP32 screening bound (ln_z_bound):
+  // ln z <= lnC1 + max e - C2 / (dG^2 max dc)
+  for (int ph = 0; ph < 2; ph++) {
+    const double sg = a.sigma[ph], s3 = sg * sg * sg;
+    const double a4 = std::pow(kLatticeConst, 4);
+    const double lnDpre = std::log(3.0 * 1.5e-20 * 2.5e6);            // |D| prefactor bound
+    const double lnG = std::log(16.0 * kPi * s3 / 3.0);                  // G* dG^2
+    const double lnZ = std::log(a.Vatom / (8.0 * kPi * std::sqrt(kKT * s3)));  // Zeldovich / dG^2
+    a.lnC1[ph] = float(std::log(3.0) + lnG - std::log(sg) - std::log(a4) + lnDpre + lnZ +
+                       a.ln_ngam + std::log(2.0) + a.ln_dtdV);
+    a.C2[ph] = float(16.0 * kPi * s3 / (3.0 * kKT));
+  }
+  return nullptr;
 }
 
 cudaError_t nucleation_setup() {

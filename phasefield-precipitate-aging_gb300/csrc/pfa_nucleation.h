@@ -30,6 +30,7 @@ struct NucArgs {
                        // as their mirrored interior cell, never painted)
   int stride;          // elements between consecutive cells of f[k] (4 for FP32 records)
   int Nx, Ny, pitch;
+  int Nz, is3d;        // 3D grids: Nz interior planes (halo layout: (Nz+2) planes)
   double sigma[2];
   double dx;           // kernel spacing (the reference passes dx * nx here)
   double dV, Vatom, n_gam, dt, R_scan;
@@ -46,6 +47,12 @@ struct NucArgs {
 };
 
 cudaError_t launch_nucleation(const NucArgs& a, cudaStream_t s);
+// Host part of a call: validates the spacing (dx sets the scan and nucleus
+// radii in cells, dV = dx dy dz), time step and lattice constant and fills
+// the derived fields of `a` (a.sigma, a.is3d, a.Nz set before); returns an
+// error message or nullptr.
+const char* nucleation_constants(NucArgs& a, double dx, double dy, double dz, double dt,
+                                 double unit_a);
 cudaError_t nucleation_setup();
 cudaError_t launch_philox_block(const void* ctr, uint64_t key, void* out, int n, cudaStream_t s);
 

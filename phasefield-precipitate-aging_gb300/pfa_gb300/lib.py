@@ -96,6 +96,9 @@ def load():
         "pfa3d_footprint": (ctypes.c_size_t, [_i, _i, _i, _i]),
         "pfa3d_sync": (_i, [ctypes.c_void_p]),
         "pfa3d_summarize_energy": (_i, [ctypes.c_void_p, _d, _dp]),
+        "pfa3d_set_nucleation": (_i, [ctypes.c_void_p, ctypes.c_uint64, _i] + [_d] * 7),
+        "pfa3d_last_nucleation_events": (_i, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64),
+                                              ctypes.POINTER(ctypes.c_int32), _i]),
         "pfa_summarize_energy": (_i, [P, _d, _d, _d, _dp, _dp, _dp]),
         "pfa_batch_footprint": (ctypes.c_size_t, [_i, _i]),
         "pfa_batch_create": (_i, [ctypes.POINTER(ctypes.c_void_p), _dp, _dp, ctypes.c_size_t]),
@@ -356,6 +359,22 @@ class Grid3D:
         check(self.L.pfa3d_summarize_energy(self.h, alpha, ctypes.byref(e)),
               "pfa3d_summarize_energy")
         return e.value
+
+    def set_nucleation(self, seed=42, interval=0, sigma=(0.13, 0.13), unit_a=0.352e-9, d=None,
+                       dt_nuc=None):
+        """Nucleation after every step k with k % interval == 0 (0: off)."""
+        d = d or (self.params["dx"],) * 3
+        dt_nuc = dt_nuc if dt_nuc is not None else max(interval, 1) * self.params["dt"]
+        check(self.L.pfa3d_set_nucleation(self.h, seed, interval, sigma[0], sigma[1], unit_a,
+                                          d[0], d[1], d[2], dt_nuc), "pfa3d_set_nucleation")
+
+    def events(self, cap=1 << 16):
+        cells = (ctypes.c_int64 * cap)()
+        ph = (ctypes.c_int32 * cap)()
+        n = self.L.pfa3d_last_nucleation_events(self.h, cells, ph, cap)
+        if n < 0:
+            check(self.L.pfa_last_error(), "events")
+        return [(cells[k], ph[k]) for k in range(min(n, cap))]
 
     def read(self):
         out = [np.empty(self.shape) for _ in range(4)]
