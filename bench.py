@@ -164,8 +164,9 @@ BATCH_WORKLOAD = (f"batch of {BATCH_COUNT} 2D grids, sides log-uniform in [128, 
                   f"all grids; one bench step = {STEPS_PER_BENCH_STEP} time steps")
 GRID3D_SIDE = 512
 GRID3D_WORKLOAD = (f"single 3D grid {GRID3D_SIDE}^3, dx=5nm, enriched slab 64 thick + 32 spheres "
-                   f"R=6 (seeded), zero-flux, 7-point Laplacian, KKS-stable dt; one bench step = "
-                   f"{STEPS_PER_BENCH_STEP} time steps")
+                   f"R=6 (seeded), zero-flux, 7-point Laplacian, KKS-stable dt, Philox nucleation "
+                   f"every {STEPS_PER_BENCH_STEP} steps (seed 42); one bench step = "
+                   f"{STEPS_PER_BENCH_STEP} time steps + 1 nucleation call")
 
 
 def _line(args, ws, metric_value, t, workload, config, **extra):
@@ -311,6 +312,8 @@ def bench_error(args, ws, rank, local, barrier, max_over_ranks, pl, ic):
     res3 = {}
     for prec in ("fp32", "fp64"):
         g = pl.Grid3D(f3, p3, precision=prec)
+        g.set_nucleation(seed=42, interval=100, sigma=NUC["sigma"], unit_a=NUC["unit_a"],
+                         d=(p3["dx"],) * 3, dt_nuc=100 * p3["dt"])
         res3[prec] = (g.run_timed(n3), g.read())
         g.close()
     err3 = [float(np.max(np.abs(a[1:-1, 1:-1, 1:-1] - b[1:-1, 1:-1, 1:-1])))
@@ -332,6 +335,9 @@ def bench_grid3d(args, ws, rank, local, barrier, max_over_ranks, pl, ic):
     params = pl.model_params(dim=3)
     cells = n ** 3
     g = pl.Grid3D(fields, params, precision="fp32")
+    g.set_nucleation(seed=42, interval=STEPS_PER_BENCH_STEP, sigma=NUC["sigma"],
+                     unit_a=NUC["unit_a"], d=(params["dx"],) * 3,
+                     dt_nuc=STEPS_PER_BENCH_STEP * params["dt"])
     g.run(args.warmup * STEPS_PER_BENCH_STEP)
     barrier()
     with ClockSampler(local) as clk:
@@ -345,6 +351,8 @@ def bench_grid3d(args, ws, rank, local, barrier, max_over_ranks, pl, ic):
                               "ms_per_step": 1e3 * t / args.steps, "partial": "value only"}))
         g.close()
         return
+    g.set_nucleation(interval=0)  # the step kernel alone for the roofline
+    g.run(2)
     kms = g.run_timed(50) / 50
     g.close()
     g64 = pl.Grid3D(fields, params, precision="fp64")
