@@ -117,7 +117,7 @@ int pfa_last_nucleation_events(struct CudaData* dev, int64_t* cells, int32_t* ph
  * kappa[2], omega[2], Lmob[2], alpha, dt (12 doubles, the layout of
  * pfa_model_params' output); dxyz = dx, dy, dz; precision PFA_FP64 or
  * PFA_FP32.  The handle owns its device buffers and stream. */
-/* device bytes of the field buffers pfa3d_create allocates (host-side) */
+/* device bytes pfa3d_create allocates: field buffers and nucleation scratch (host-side) */
 size_t pfa3d_footprint(int nx, int ny, int nz, int precision);
 int pfa3d_create(void** handle, int nx, int ny, int nz, const double* params, const double* dxyz,
                  const double* conc_Cr, const double* conc_Nb, const double* phi_del,

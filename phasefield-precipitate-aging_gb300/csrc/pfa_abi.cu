@@ -91,9 +91,11 @@ struct State {
   uint64_t step_counter = 0;
   // scratch (event buffer, counters, partial sums)
   NucEvent* ev = nullptr;
-  unsigned* ev_count = nullptr;
+  unsigned* ev_count = nullptr;  // [0] events, [1] listed cells
   int* ev_status = nullptr;
   unsigned long long* call_dev = nullptr;
+  long long* cand = nullptr;  // cells left to the FP64 nucleation decision
+  int cand_cap = 0;
   double* sum_partial = nullptr;
   double* sum_out = nullptr;
   double* nrg_map[2] = {};  // per-node chemical / gradient energy (on request)
@@ -278,6 +280,8 @@ static int nucleate(CudaData* dev, State* s, double sig_d, double sig_l, double 
   a.count = s->ev_count;
   a.status = s->ev_status;
   a.cap = kNucCap;
+  a.cand = s->cand;
+  a.cand_cap = s->cand_cap;
   CK(launch_nucleation(a, s->st));
   s->calls++;
   return 0;
@@ -532,12 +536,14 @@ static int init_core(CudaData* dev, int nx, int ny, int nm, const double* mask,
   for (auto p : main_f)
     if (alloc_field(p, n)) return PFA_ECUDA;
   CK(cudaMalloc(reinterpret_cast<void**>(&s->ev), sizeof(NucEvent) * kNucCap));
-  CK(cudaMalloc(reinterpret_cast<void**>(&s->ev_count), sizeof(unsigned)));
+  CK(cudaMalloc(reinterpret_cast<void**>(&s->ev_count), 2 * sizeof(unsigned)));
+  s->cand_cap = nucleation_cand_cap(n);
+  CK(cudaMalloc(reinterpret_cast<void**>(&s->cand), sizeof(long long) * size_t(s->cand_cap)));
   CK(cudaMalloc(reinterpret_cast<void**>(&s->ev_status), sizeof(int)));
   CK(cudaMalloc(reinterpret_cast<void**>(&s->call_dev), sizeof(unsigned long long)));
   CK(cudaMalloc(reinterpret_cast<void**>(&s->sum_partial), sizeof(double) * kSumBlocks * 5));
   CK(cudaMalloc(reinterpret_cast<void**>(&s->sum_out), sizeof(double) * 5));
-  CK(cudaMemsetAsync(s->ev_count, 0, sizeof(unsigned), s->st));
+  CK(cudaMemsetAsync(s->ev_count, 0, 2 * sizeof(unsigned), s->st));
   CK(cudaMemsetAsync(s->ev_status, 0, sizeof(int), s->st));
   CK(cudaMemsetAsync(s->call_dev, 0, sizeof(unsigned long long), s->st));
   static bool nuc_ready = false;
@@ -577,6 +583,7 @@ static int free_core(CudaData* dev) {
   cudaFree(s->f32mem);
   cudaFree(s->ev);
   cudaFree(s->ev_count);
+  cudaFree(s->cand);
   cudaFree(s->ev_status);
   cudaFree(s->call_dev);
   cudaFree(s->sum_partial);

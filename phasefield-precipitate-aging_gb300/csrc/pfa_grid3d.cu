@@ -46,9 +46,11 @@ struct Grid3D {
   double nuc_sigma[2] = {0.13, 0.13}, nuc_unit_a = 0.352e-9, nuc_d[3] = {}, nuc_dt = 0.0;
   uint64_t step_counter = 0;
   NucEvent* ev = nullptr;
-  unsigned* ev_count = nullptr;
+  unsigned* ev_count = nullptr;  // [0] events, [1] listed cells
   int* ev_status = nullptr;
   unsigned long long* call_dev = nullptr;  // Philox call counter
+  long long* cand = nullptr;               // cells left to the FP64 nucleation decision
+  int cand_cap = 0;
 };
 
 int err(int code, const char* what) {
@@ -182,6 +184,8 @@ int nucleate(Grid3D* g) {
   a.count = g->ev_count;
   a.status = g->ev_status;
   a.cap = kNucCap;
+  a.cand = g->cand;
+  a.cand_cap = g->cand_cap;
   CK3(launch_nucleation(a, g->st));
   return 0;
 }
@@ -274,9 +278,10 @@ extern "C" {
 size_t pfa3d_footprint(int nx, int ny, int nz, int precision) {
   if (nx < 3 || ny < 3 || nz < 3) return 0;
   const size_t ghost = size_t(nx) * ny * nz;
-  if (precision == PFA_FP64) return 2 * 4 * ghost * sizeof(double);
+  const size_t nuc = nucleation_scratch_bytes(size_t(nx - 2) * (ny - 2) * (nz - 2));
+  if (precision == PFA_FP64) return 2 * 4 * ghost * sizeof(double) + nuc;
   const size_t recs = size_t((nx - 2 + 31) / 32 * 32) * (ny - 2) * (nz - 2);
-  return 4 * ghost * sizeof(double) + 2 * recs * (16 + 8);
+  return 4 * ghost * sizeof(double) + 2 * recs * (16 + 8) + nuc;
 }
 
 int pfa3d_create(void** handle, int nx, int ny, int nz, const double* params, const double* dxyz,
@@ -334,10 +339,12 @@ int pfa3d_create(void** handle, int nx, int ny, int nz, const double* params, co
   CK3(cudaMalloc(reinterpret_cast<void**>(&g->sum_partial), sizeof(double) * kSumBlocks * 5));
   CK3(cudaMalloc(reinterpret_cast<void**>(&g->sum_out), sizeof(double) * 5));
   CK3(cudaMalloc(reinterpret_cast<void**>(&g->ev), sizeof(NucEvent) * kNucCap));
-  CK3(cudaMalloc(reinterpret_cast<void**>(&g->ev_count), sizeof(unsigned)));
+  CK3(cudaMalloc(reinterpret_cast<void**>(&g->ev_count), 2 * sizeof(unsigned)));
+  g->cand_cap = nucleation_cand_cap(size_t(g->Nx) * g->Ny * g->Nz);
+  CK3(cudaMalloc(reinterpret_cast<void**>(&g->cand), sizeof(long long) * size_t(g->cand_cap)));
   CK3(cudaMalloc(reinterpret_cast<void**>(&g->ev_status), sizeof(int)));
   CK3(cudaMalloc(reinterpret_cast<void**>(&g->call_dev), sizeof(unsigned long long)));
-  CK3(cudaMemsetAsync(g->ev_count, 0, sizeof(unsigned), g->st));
+  CK3(cudaMemsetAsync(g->ev_count, 0, 2 * sizeof(unsigned), g->st));
   CK3(cudaMemsetAsync(g->ev_status, 0, sizeof(int), g->st));
   CK3(cudaMemsetAsync(g->call_dev, 0, sizeof(unsigned long long), g->st));
   CK3(cudaStreamSynchronize(g->st));
@@ -372,7 +379,7 @@ int pfa3d_set_nucleation(void* handle, uint64_t seed, int interval, double sigma
   g->nuc_dt = dt_nuc;
   g->step_counter = 0;
   CK3(cudaMemsetAsync(g->call_dev, 0, sizeof(unsigned long long), g->st));
-  CK3(cudaMemsetAsync(g->ev_count, 0, sizeof(unsigned), g->st));
+  CK3(cudaMemsetAsync(g->ev_count, 0, 2 * sizeof(unsigned), g->st));
   CK3(cudaStreamSynchronize(g->st));
   return 0;
 }
@@ -529,6 +536,7 @@ int pfa3d_destroy(void* handle) {
   cudaFree(g->sum_out);
   cudaFree(g->ev);
   cudaFree(g->ev_count);
+  cudaFree(g->cand);
   cudaFree(g->ev_status);
   cudaFree(g->call_dev);
   if (g->st) cudaStreamDestroy(g->st);

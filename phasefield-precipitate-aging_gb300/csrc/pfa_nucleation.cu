@@ -9,13 +9,18 @@
 //      (neighbourhood scan, driving force g_gam, diffusivities, classical
 //      nucleation probability thermo/nucleation.c:30-69) with Philox4x32-10
 //      draws keyed by (seed, call counter, cell).  Events are compacted with a
-//      warp ballot and one atomic per warp.
+//      warp ballot and one atomic per warp.  The FP64 probability is
+//      evaluated only where an FP32 bound cannot exclude an event: if
+//      dt dV (J_Cr + J_Nb) < 1e-17 the FP64 P_nuc is 0 or 2^-53 and no draw
+//      u >= 2^-53 can fall below it, so skipping such cells changes no
+//      decision.  The cells the bound leaves open are listed (same atomic
+//      scheme) and
+//   1b. k_nuc_fp64 decides them in FP64, 32 listed cells per warp, with the
+//      same draws;
 //   2. k_nuc_apply: one CTA sorts the events by cell and paints them in that
 //      order, delta before laves (embed_OPC_kernel, :1046-1077).
-// The FP64 probability is evaluated only where an FP32 bound cannot exclude
-// an event: if dt dV (J_Cr + J_Nb) < 1e-17 the FP64 P_nuc is 0 or 2^-53 and
-// no draw u >= 2^-53 can fall below it, so skipping such cells changes no
-// decision.
+// The event set does not depend on which kernel decided a cell, and the sort
+// fixes the painting order.
 #include <cmath>
 #include <cstdint>
 
@@ -184,16 +189,79 @@ __device__ __forceinline__ bool clear_at(const NucArgs& a, size_t s) {
   return !(p64(ldval<T>(a, 2, s)) + p64(ldval<T>(a, 3, s)) >= 1e-10);
 }
 
+// Philox draw of a cell in a call: counter (cell, call), key = seed
+__device__ __forceinline__ uint4 nuc_draw(const NucArgs& a, long long idx) {
+  const unsigned long long call = *a.call_ptr;
+  return philox4x32_10(make_uint4(uint32_t(idx), uint32_t(uint64_t(idx) >> 32), uint32_t(call),
+                                  uint32_t(call >> 32)),
+                       make_uint2(uint32_t(a.seed), uint32_t(a.seed >> 32)));
+}
+
+// The FP64 decision of one clear cell (reference linear index idx, storage
+// index s) with its draw w: classical nucleation probability of each phase
+// against the draw; fills e and returns true on an event.
+template <class T>
+__device__ bool decide64(const NucArgs& a, long long idx, size_t s, uint4 w, NucEvent& e) {
+  const double X = ldval<T>(a, 0, s), Y = ldval<T>(a, 1, s);
+  const double u[2] = {u53(w.x, w.y), u53(w.z, w.w)};
+  const double dG = g64<0>(X, Y);
+  double dcc, dnn;
+  diffusivities(X, Y, dcc, dnn);
+  int mask = 0;
+  double rp[2] = {0.0, 0.0};
+#pragma unroll
+  for (int ph = 0; ph < 2; ph++) {
+    double Rstar = 0.0, P = 0.0;
+    probability_sphere(X, Y, dG, dcc, dnn, a.sigma[ph], a.Vatom, a.n_gam, a.dV, a.dt, Rstar, P);
+    if (Rstar > 0.) {
+      rp[ph] = Rstar / a.dx;
+      if (P - u[ph] > 0) {
+        if (rp[ph] <= kNucMaxRadius)
+          mask |= 1 << ph;
+        else
+          atomicExch(a.status, 2);  // nucleus wider than the paint limit: reported
+      }
+    }
+  }
+  if (!mask) return false;
+  e.cell = idx;
+  e.mask = mask;
+  e.pad = 0;
+  e.xcr = X;
+  e.xnb = Y;
+  e.r[0] = rp[0];
+  e.r[1] = rp[1];
+  return true;
+}
+
+// warp-aggregated append of the lanes' events (whole warp)
+__device__ __forceinline__ void append_events(const NucArgs& a, bool ev, const NucEvent& e) {
+  const unsigned bal = __ballot_sync(0xffffffffu, ev);
+  if (bal == 0) return;
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(bal) - 1;
+  unsigned base = 0;
+  if (lane == leader) base = atomicAdd(a.count, unsigned(__popc(bal)));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (ev) {
+    const unsigned slot = base + __popc(bal & ((1u << lane) - 1u));
+    if (slot < unsigned(a.cap)) a.events[slot] = e;
+  }
+}
+
 template <class T>
 __global__ void __launch_bounds__(256) k_nuc_decide(NucArgs a) {
   const int gx = blockIdx.x * 32 + (threadIdx.x & 31);
   const int gy = blockIdx.y * 8 + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
   const int nxr = a.Nx + 2, nyr = a.Ny + 2;
-  bool ev = false;
-  NucEvent e;
+  bool need = false;  // the FP32 screen leaves this cell to the FP64 decision
+  long long idx = 0;
+  size_t s = 0;
+  uint4 w = make_uint4(0, 0, 0, 0);
   if (gx < a.Nx && gy < a.Ny) {
     const int x = gx + 1, y = gy + 1, z = a.is3d ? int(blockIdx.z) + 1 : 0;
-    const long long idx = ((long long)z * nyr + y) * nxr + x;
+    idx = ((long long)z * nyr + y) * nxr + x;
     bool clear = true;
     if (a.is3d) {
       // the same scan over a ball; offsets that leave the array along any
@@ -230,7 +298,7 @@ __global__ void __launch_bounds__(256) k_nuc_decide(NucArgs a) {
         }
     }
     if (clear) {
-      const size_t s = stor(a, x, y, z);
+      s = stor(a, x, y, z);
       const T Xs = static_cast<const T*>(a.f[0])[s * a.stride];
       const T Ys = static_cast<const T*>(a.f[1])[s * a.stride];
       // Screen in FP32 on the bound z_up of z = dt dV (J_Cr + J_Nb), which
@@ -240,19 +308,12 @@ __global__ void __launch_bounds__(256) k_nuc_decide(NucArgs a) {
       //    every draw -- no event, no draw needed;
       //  * else draw, and skip the FP64 path when u >= hi32 2^-32 (rounded
       //    toward zero) >= P_up >= P_nuc.
-      // A tight screen matters: one lane that needs the FP64 path makes its
-      // whole warp issue it.
       constexpr float kMargin = 2.0f;
       float lnz[2];
       ln_z_bound(float(Xs), float(Ys), a, lnz);
       const float lnz_max = fmaxf(lnz[0], lnz[1]) + kMargin;
-      bool need = false;
-      uint4 w = make_uint4(0, 0, 0, 0);
       if (!(lnz_max < -38.8f)) {  // ln 2^-56
-        const unsigned long long call = *a.call_ptr;
-        w = philox4x32_10(make_uint4(uint32_t(idx), uint32_t(uint64_t(idx) >> 32),
-                                     uint32_t(call), uint32_t(call >> 32)),
-                          make_uint2(uint32_t(a.seed), uint32_t(a.seed >> 32)));
+        w = nuc_draw(a, idx);
         const float ulo[2] = {__uint2float_rz(w.x) * 0x1p-32f, __uint2float_rz(w.z) * 0x1p-32f};
 #pragma unroll
         for (int ph = 0; ph < 2; ph++) {
@@ -261,52 +322,51 @@ __global__ void __launch_bounds__(256) k_nuc_decide(NucArgs a) {
           if (!bounded || !(ulo[ph] >= pup)) need = true;
         }
       }
-      if (need) {
-        const double X = ldval<T>(a, 0, s), Y = ldval<T>(a, 1, s);
-        const double u[2] = {u53(w.x, w.y), u53(w.z, w.w)};
-        const double dG = g64<0>(X, Y);
-        double dcc, dnn;
-        diffusivities(X, Y, dcc, dnn);
-        int mask = 0;
-        double rp[2] = {0.0, 0.0};
-#pragma unroll
-        for (int ph = 0; ph < 2; ph++) {
-          double Rstar = 0.0, P = 0.0;
-          probability_sphere(X, Y, dG, dcc, dnn, a.sigma[ph], a.Vatom, a.n_gam, a.dV, a.dt, Rstar, P);
-          if (Rstar > 0.) {
-            rp[ph] = Rstar / a.dx;
-            if (P - u[ph] > 0) {
-              if (rp[ph] <= kNucMaxRadius)
-                mask |= 1 << ph;
-              else
-                atomicExch(a.status, 2);  // nucleus wider than the paint limit: reported
-            }
-          }
-        }
-        if (mask) {
-          ev = true;
-          e.cell = idx;
-          e.mask = mask;
-          e.pad = 0;
-          e.xcr = X;
-          e.xnb = Y;
-          e.r[0] = rp[0];
-          e.r[1] = rp[1];
-        }
+    }
+  }
+  // Cells the screen cannot settle go to k_nuc_fp64 as a compact list: a warp
+  // issues the FP64 path if any of its lanes needs it, so in place a few such
+  // cells would cost whole warps.  Cells past the list's capacity decide here.
+  const unsigned nb = __ballot_sync(0xffffffffu, need);
+  if (nb == 0) return;
+  {
+    const int leader = __ffs(nb) - 1;
+    unsigned base = 0;
+    if (lane == leader) base = atomicAdd(a.count + 1, unsigned(__popc(nb)));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (need) {
+      const unsigned slot = base + __popc(nb & ((1u << lane) - 1u));
+      if (slot < unsigned(a.cand_cap)) {
+        a.cand[slot] = idx;
+        need = false;
       }
     }
   }
-  // warp-aggregated append
-  const unsigned bal = __ballot_sync(0xffffffffu, ev);
-  if (bal == 0) return;
+  bool ev = false;
+  NucEvent e;
+  if (need) ev = decide64<T>(a, idx, s, w, e);
+  append_events(a, ev, e);
+}
+
+// The FP64 decisions of the listed cells, 32 per warp.
+template <class T>
+__global__ void __launch_bounds__(256) k_nuc_fp64(NucArgs a) {
+  const unsigned n = min(a.count[1], unsigned(a.cand_cap));
   const int lane = threadIdx.x & 31;
-  const int leader = __ffs(bal) - 1;
-  unsigned base = 0;
-  if (lane == leader) base = atomicAdd(a.count, unsigned(__popc(bal)));
-  base = __shfl_sync(0xffffffffu, base, leader);
-  if (ev) {
-    const unsigned slot = base + __popc(bal & ((1u << lane) - 1u));
-    if (slot < unsigned(a.cap)) a.events[slot] = e;
+  const unsigned step = gridDim.x * blockDim.x;  // a multiple of 32: warps stay whole
+  const long long nxr = a.Nx + 2, nyr = a.Ny + 2;
+  for (unsigned b = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); b < n; b += step) {
+    const unsigned i = b + lane;
+    bool ev = false;
+    NucEvent e;
+    if (i < n) {
+      const long long idx = a.cand[i];
+      const int x = int(idx % nxr);
+      const long long t = idx / nxr;
+      const int y = int(t % nyr), z = int(t / nyr);
+      ev = decide64<T>(a, idx, stor(a, x, y, z), nuc_draw(a, idx), e);
+    }
+    append_events(a, ev, e);
   }
 }
 
@@ -428,15 +488,18 @@ __global__ void __launch_bounds__(1024) k_nuc_apply(NucArgs a) {
 }  // namespace
 
 cudaError_t launch_nucleation(const NucArgs& a, cudaStream_t s) {
-  cudaError_t err = cudaMemsetAsync(a.count, 0, sizeof(unsigned), s);
+  cudaError_t err = cudaMemsetAsync(a.count, 0, 2 * sizeof(unsigned), s);
   if (err != cudaSuccess) return err;
   dim3 grid((a.Nx + 31) / 32, (a.Ny + 7) / 8, a.is3d ? a.Nz : 1);
   const size_t smem = sizeof(unsigned long long) * size_t(kNucCap);
+  const int fp64_blocks = 152 * 4;  // grid-stride over the list (its length is on the device)
   if (a.is_f32) {
     k_nuc_decide<float><<<grid, 256, 0, s>>>(a);
+    k_nuc_fp64<float><<<fp64_blocks, 256, 0, s>>>(a);
     k_nuc_apply<float><<<1, 1024, smem, s>>>(a);
   } else {
     k_nuc_decide<double><<<grid, 256, 0, s>>>(a);
+    k_nuc_fp64<double><<<fp64_blocks, 256, 0, s>>>(a);
     k_nuc_apply<double><<<1, 1024, smem, s>>>(a);
   }
   return cudaGetLastError();

@@ -41,10 +41,25 @@ struct NucArgs {
   uint64_t seed;
   unsigned long long* call_ptr;  // scratch: nucleation call counter (Philox counter word)
   NucEvent* events;    // scratch: kNucCap events
-  unsigned* count;     // scratch: event counter
+  unsigned* count;     // scratch: [0] events, [1] cells listed for the FP64 decision
   int* status;         // scratch: 1 = overflow
   int cap;
+  long long* cand;     // scratch: cells the FP32 screen left to the FP64 decision
+  int cand_cap;        // nucleation_cand_cap(cells)
 };
+
+// Length of the FP64-decision list: a quarter of the cells (at least 1024,
+// at most 2^24); cells beyond it are decided in place, with the same result.
+inline int nucleation_cand_cap(size_t cells) {
+  const size_t q = cells / 4;
+  return int(q < 1024 ? 1024 : (q > (size_t(1) << 24) ? (size_t(1) << 24) : q));
+}
+
+// Device scratch of a nucleation handle: events, counters, status, list.
+inline size_t nucleation_scratch_bytes(size_t cells) {
+  return sizeof(NucEvent) * kNucCap + 2 * sizeof(unsigned) + sizeof(int) +
+         sizeof(unsigned long long) + sizeof(long long) * size_t(nucleation_cand_cap(cells));
+}
 
 cudaError_t launch_nucleation(const NucArgs& a, cudaStream_t s);
 // Host part of a call: validates the spacing (dx sets the scan and nucleus

@@ -18,7 +18,8 @@
 //    phi_lav} (16 bytes) and B = the four compensations, packed into 16-bit
 //    counts (8 bytes, PACK) or as FP32 (16 bytes) -- so a row costs one
 //    128-bit and one 64-bit (128-bit) load and store and a single address per
-//    lane; records of the row after next are loaded one iteration ahead.
+//    lane; records of the row after next are loaded one iteration ahead (the
+//    batched kernel stages rows through a per-warp cp.async ring instead).
 //
 // Record layout: Ny rows of `pitch` records (pitch a multiple of 32), interior
 // cell (x, y) at record y * pitch + x, no ghost ring; zero-flux edges come
@@ -54,6 +55,28 @@ struct Raw {
   float4 a;       // x_Cr, x_Nb, phi_del, phi_lav
   CompT<PACK> c;  // Kahan compensations
 };
+
+// Per-warp staging ring in shared memory (the batched kernel): rows are
+// copied with cp.async kDepth-2 rows ahead of the row being solved, so a warp
+// keeps several rows of loads in flight without holding them in registers.
+constexpr int kDepth = 4;  // a power of two
+template <bool PACK>
+struct Ring {
+  float4 a[kDepth][32];
+  CompT<PACK> c[kDepth][32];
+};
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async8(uint32_t dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
 
 template <bool PACK>
 __device__ __forceinline__ float4 comps(const CompT<PACK>& c) {
@@ -137,12 +160,15 @@ struct Stream {
 
 // One warp updates the strip of output columns x0 .. x0+29 over rows
 // y0 .. y1-1 of one grid (the unit of work of both the single-grid and the
-// batched kernels).  Whole warp; x0 < Nx.
-template <bool PACK>
+// batched kernels).  Whole warp; x0 < Nx.  Rows reach the registers either
+// directly (one row ahead, !STAGED) or through the warp's staging ring
+// (STAGED): the batched kernel's units are short, and the ring's deeper
+// prefetch hides the start-up latency each unit pays.
+template <bool PACK, bool STAGED>
 __device__ __forceinline__ void stream_strip(const Step2DArgs& a, const float4* Ain,
                                              const CompT<PACK>* Bin, float4* Aout,
                                              CompT<PACK>* Bout, int Nx, int Ny, int P, int x0,
-                                             int y0, int y1) {
+                                             int y0, int y1, Ring<PACK>* ring) {
   const int lane = threadIdx.x & 31;
   const int gx = x0 - 1 + lane;  // lanes 0 and 31 hold the neighbour columns
   const int cx = min(max(gx, 0), Nx - 1);
@@ -161,30 +187,77 @@ __device__ __forceinline__ void stream_strip(const Step2DArgs& a, const float4* 
       gamma_u32(K, r.a.x, r.a.y, cxy.x, cxy.y, r.a.z, r.a.w, n.u1, n.u2);
     return n;
   };
-  // window rows y-1, y, y+1 and raw records of rows y, y+1, y+2
-  Raw<PACK> r0 = S.load(S.row(y0)), r1 = S.load(S.row(y0 + 1)), r2;
-  Nb n0 = solve_raw(S.load(S.row(y0 - 1))), n1 = solve_raw(r0), n2;
-  // three rows per iteration with rotated roles: no register moves
-  int y = y0;
-  for (; y + 2 < y1; y += 3) {
-    r2 = S.load(S.row(y + 2));
-    n2 = solve_raw(r1);
-    S.update(y, n0, n1, n2, r0);
-    r0 = S.load(S.row(y + 3));
-    n0 = solve_raw(r2);
-    S.update(y + 1, n1, n2, n0, r1);
-    r1 = S.load(S.row(y + 4));
-    n1 = solve_raw(r0);
-    S.update(y + 2, n2, n0, n1, r2);
-  }
-  for (; y < y1; y++) {
-    r2 = S.load(S.row(y + 2));
-    n2 = solve_raw(r1);
-    S.update(y, n0, n1, n2, r0);
-    n0 = n1;
-    n1 = n2;
-    r0 = r1;
-    r1 = r2;
+  if constexpr (!STAGED) {
+    // window rows y-1, y, y+1 and raw records of rows y, y+1, y+2
+    Raw<PACK> r0 = S.load(S.row(y0)), r1 = S.load(S.row(y0 + 1)), r2;
+    Nb n0 = solve_raw(S.load(S.row(y0 - 1))), n1 = solve_raw(r0), n2;
+    // three rows per iteration with rotated roles: no register moves
+    int y = y0;
+    for (; y + 2 < y1; y += 3) {
+      r2 = S.load(S.row(y + 2));
+      n2 = solve_raw(r1);
+      S.update(y, n0, n1, n2, r0);
+      r0 = S.load(S.row(y + 3));
+      n0 = solve_raw(r2);
+      S.update(y + 1, n1, n2, n0, r1);
+      r1 = S.load(S.row(y + 4));
+      n1 = solve_raw(r0);
+      S.update(y + 2, n2, n0, n1, r2);
+    }
+    for (; y < y1; y++) {
+      r2 = S.load(S.row(y + 2));
+      n2 = solve_raw(r1);
+      S.update(y, n0, n1, n2, r0);
+      n0 = n1;
+      n1 = n2;
+      r0 = r1;
+      r1 = r2;
+    }
+  } else {
+    // ring slot k holds rows y0-1+k, y0-1+k+kDepth, ...; each lane copies and
+    // reads back only its own column's records, so the wait needs no warp sync
+    const uint32_t sa = uint32_t(__cvta_generic_to_shared(&ring->a[0][lane]));
+    const uint32_t sc = uint32_t(__cvta_generic_to_shared(&ring->c[0][lane]));
+    constexpr uint32_t kSlotA = 32 * sizeof(float4), kSlotC = 32 * sizeof(CompT<PACK>);
+    auto issue = [&](int y, int slot) {
+      if (y <= y1) {  // rows past y1 are never read
+        const int off = S.row(y);
+        cp_async16(sa + slot * kSlotA, S.A + off);
+        if constexpr (PACK)
+          cp_async8(sc + slot * kSlotC, S.B + off);
+        else
+          cp_async16(sc + slot * kSlotC, S.B + off);
+      }
+      cp_commit();  // one group per row (empty past y1): the wait counts stay uniform
+    };
+    auto fetch = [&](int slot) { return Raw<PACK>{ring->a[slot][lane], ring->c[slot][lane]}; };
+#pragma unroll
+    for (int k = 0; k < kDepth; k++) issue(y0 - 1 + k, k);
+    cp_wait<kDepth - 2>();  // rows y0-1 and y0 have landed
+    Nb n0 = solve_raw(fetch(0)), n1 = solve_raw(fetch(1)), n2;
+    int s = 0;  // slot of row y-1
+    // row y: refill the slot of row y-1 (read for row y-1's update) with row
+    // y-1+kDepth, wait for row y+1 (kDepth-2 newer groups stay in flight),
+    // solve it, update row y.  Rows up to y1 were all waited for by the last
+    // row, so no copy into the ring is pending when the strip ends.
+    auto body = [&](int y, const Nb& up, const Nb& c, Nb& dn) {
+      issue(y - 1 + kDepth, s);
+      s = (s + 1) & (kDepth - 1);
+      cp_wait<kDepth - 2>();
+      dn = solve_raw(fetch((s + 1) & (kDepth - 1)));
+      S.update(y, up, c, dn, fetch(s));
+    };
+    int y = y0;
+    for (; y + 2 < y1; y += 3) {
+      body(y, n0, n1, n2);
+      body(y + 1, n1, n2, n0);
+      body(y + 2, n2, n0, n1);
+    }
+    for (; y < y1; y++) {
+      body(y, n0, n1, n2);
+      n0 = n1;
+      n1 = n2;
+    }
   }
 }
 
@@ -194,10 +267,10 @@ __global__ void __launch_bounds__(32 * kWarps, 8) k_stream_f32(Step2DArgs a) {
   const int x0 = strip * kCols;  // first output column of the strip
   if (x0 >= a.Nx) return;        // whole warp leaves together
   const int y0 = blockIdx.y * a.rows;
-  stream_strip<PACK>(a, static_cast<const float4*>(a.in[0]),
-                     static_cast<const CompT<PACK>*>(a.in[1]), static_cast<float4*>(a.out[0]),
-                     static_cast<CompT<PACK>*>(a.out[1]), a.Nx, a.Ny, a.pitch, x0, y0,
-                     min(y0 + a.rows, a.Ny));
+  stream_strip<PACK, false>(a, static_cast<const float4*>(a.in[0]),
+                            static_cast<const CompT<PACK>*>(a.in[1]),
+                            static_cast<float4*>(a.out[0]), static_cast<CompT<PACK>*>(a.out[1]),
+                            a.Nx, a.Ny, a.pitch, x0, y0, min(y0 + a.rows, a.Ny), nullptr);
 }
 
 // ---- many grids in one launch ----
@@ -209,10 +282,12 @@ __global__ void __launch_bounds__(32 * kWarps, 8) k_stream_f32(Step2DArgs a) {
 // has one CTA per resident slot; the other shape has one warp per unit (and
 // leaves the balancing to the block scheduler).  Unit indices come only from
 // the counter: ptxas keeps this form within 64 registers without spills.
+// Rows are staged through a cp.async ring per warp (12 KB per CTA).
 __global__ void __launch_bounds__(32 * kWarps, 8) k_batch_f32(Step2DArgs a, BatchArgs b) {
   const int p = b.parity;
   if (blockIdx.x == 0 && threadIdx.x == 0) b.counter[p ^ 1] = 0;
   const int units = b.counter[2];
+  __shared__ Ring<true> ring[kWarps];
   for (;;) {
     int u = 0;
     if ((threadIdx.x & 31) == 0) u = atomicAdd(b.counter + p, 1);
@@ -220,8 +295,8 @@ __global__ void __launch_bounds__(32 * kWarps, 8) k_batch_f32(Step2DArgs a, Batc
     if (u >= units) return;
     const BatchUnit w = b.unit[u];
     const BatchGrid& g = b.grid[w.grid];
-    stream_strip<true>(a, g.A[p], g.B[p], g.A[p ^ 1], g.B[p ^ 1], g.Nx, g.Ny, g.pitch, w.x0,
-                       w.y0, w.y1);
+    stream_strip<true, true>(a, g.A[p], g.B[p], g.A[p ^ 1], g.B[p ^ 1], g.Nx, g.Ny, g.pitch,
+                             w.x0, w.y0, w.y1, &ring[threadIdx.x >> 5]);
   }
 }
 

@@ -65,6 +65,9 @@ def test_events_match_reference_golden(pfa, tag):
 
 @pytest.mark.parametrize("seed", [1, 7, 2026])
 def test_event_sets_bit_exact_against_cpu_replica(pfa, orc, seed):
+    # nearly every cell of this enriched grid needs the FP64 decision: the
+    # first quarter of them is listed for the FP64 pass, the rest is decided
+    # in place, so both routes are checked against the replica
     from golden.make_golden import NUC_A, nuc_struct
     from pfa_gb300 import ic
     f = ic.grid2d(96, 80, seed=seed, matrix=(0.2600, 0.1680), enrich=(0.2720, 0.1692),
