@@ -401,10 +401,10 @@ def bench_serve(args, ws, rank, local, barrier, max_over_ranks, pl, ic):
     arena = 48 << 30
     budget3 = 48 << 30
 
-    def serve_once(realtime=True):
+    def serve_once(realtime=True, requests=reqs):
         be = GpuBackend(pl, p2, p3, arena, budget3)
         srv = Server(be, tick_steps=STEPS_PER_BENCH_STEP)
-        done = srv.run_trace(reqs, realtime=realtime)
+        done = srv.run_trace(requests, realtime=realtime)
         be.close()
         return done, srv
 
@@ -422,6 +422,15 @@ def bench_serve(args, ws, rank, local, barrier, max_over_ranks, pl, ic):
     t = max_over_ranks(span)
     value = ws * work / t
     stats = latency_stats(done)
+    # the same trace with every initial condition built on the device from its
+    # recipe (no host fields, no upload)
+    rreqs = [Request(t_["rid"], None, t_["steps"], t_["arrival"], recipe=ic.serve_recipe(t_))
+             for t_ in trace]
+    barrier()
+    done_r, _ = serve_once(requests=rreqs)
+    barrier()
+    span_r = max_over_ranks(max(r.finished for r in done_r) - min(r.req.arrival for r in done_r))
+    stats_r = latency_stats(done_r)
     # one-at-a-time FP64: each request's FP64 step time measured on a sample,
     # queueing in arrival order computed from those service times
     service = []
@@ -458,6 +467,11 @@ def bench_serve(args, ws, rank, local, barrier, max_over_ranks, pl, ic):
                      e2e={"value": value, "unit": "cell-updates/s",
                           "h2d_bytes_per_step": sum(4 * r.fields[0].size * 8 for r in reqs),
                           "d2h_bytes_per_step": sum(4 * r.fields[0].size * 8 for r in reqs)},
+                     ic_on_device={"value": ws * work / span_r, "unit": "cell-updates/s",
+                                   "p50_s": stats_r["p50_s"], "p99_s": stats_r["p99_s"],
+                                   "how": "the same trace, initial conditions built on the "
+                                          "device from recipes (pfa_ic_recipe), no upload"},
+                     gpu_launches=srv.step_launches + 2 * len(reqs),
                      clocks=clk.summary())
         print(json.dumps(line))
 

@@ -176,6 +176,53 @@ int pfa_batch_info(void* handle, int* grids, size_t* used_bytes, size_t* arena_b
 void* pfa_batch_stream(void* handle);
 int pfa_batch_destroy(void* handle);
 
+/* ---- on-device initial conditions ----
+ * The reference builds its initial grids on the host (src/alloy625.cpp:170-518:
+ * a matrix composition, enriched regions, particles embedded with
+ * embed_OPC's tanh profile, :262-294, tanh_interp thermo/nucleation.c:12-16)
+ * and writes them to disk for the GPU run.  A recipe describes the same kind
+ * of grid so the device builds it in place: no host arrays and no
+ * host-to-device copy (the serving layer admits requests this way).
+ *   fields = matrix + noise (2u - 1), u uniform in (0, 1] from Philox4x32-10
+ *            keyed by seed, counter (cell, 0, 0x49430000), cell = the
+ *            interior row-major index, u_Cr from words 0-1, u_Nb from 2-3;
+ *   every band adds (enrich - matrix) on interior columns lo <= x < hi
+ *            (stripes in 2D, slabs normal to x in 3D; overlapping bands add);
+ *   particles in order: inside the box |coord - floor(c)| <= pad on each axis,
+ *            pad = ceil(R + 3 width / dx) + 1, phi = 0.5 - 0.5 tanh(dx (r - R)
+ *            / (width / 2)), x = p(phi) xe_phase + (1 - p(phi)) x, phi_phase =
+ *            max(phi_phase, phi) (r: distance to the centre, in cells);
+ *   ghost ring = the zero-flux mirror of the interior.
+ * nz <= 1 makes a 2D grid (centre[k][2] ignored). */
+#define PFA_IC_MAX_BANDS 16
+#define PFA_IC_MAX_PARTICLES 64
+typedef struct pfa_ic_recipe {
+	int nx, ny, nz;            /* interior cells */
+	double matrix[2];          /* x_Cr, x_Nb */
+	double enrich[2];          /* x_Cr, x_Nb inside the bands */
+	double noise;              /* half-width of the composition noise */
+	uint64_t seed;
+	int n_bands;
+	int band[PFA_IC_MAX_BANDS][2];             /* interior columns [lo, hi) */
+	int n_particles;
+	double centre[PFA_IC_MAX_PARTICLES][3];    /* x, y, z in interior cells */
+	double radius[PFA_IC_MAX_PARTICLES];       /* cells */
+	int phase[PFA_IC_MAX_PARTICLES];           /* 0 delta, 1 laves */
+	double dx;                 /* spacing of the tanh profile (m) */
+	double width;              /* interface width 2 lambda (m) */
+} pfa_ic_recipe;
+
+/* writes the recipe's four fields into caller-owned device arrays in the
+ * reference layout ((ny+2) x (nx+2), or (nz+2) x (ny+2) x (nx+2)), enqueued on
+ * `stream` (a cudaStream_t, NULL = default stream) */
+int pfa_ic_generate(const pfa_ic_recipe* r, double* conc_Cr, double* conc_Nb, double* phi_del,
+                    double* phi_lav, void* stream);
+/* pfa_batch_add with the grid built on the device from a 2D recipe */
+int pfa_batch_add_ic(void* handle, const pfa_ic_recipe* r, int* slot);
+/* pfa3d_create with the grid built on the device from a 3D recipe */
+int pfa3d_create_ic(void** handle, const pfa_ic_recipe* r, const double* params,
+                    const double* dxyz, int precision);
+
 /* ---- on-device FP64 field summary (src/alloy625.cpp:811-863) ---- */
 /* out[5] = mean x_Cr, mean x_Nb, f_gamma, f_delta, f_laves over the interior */
 int pfa_summarize(struct CudaData* dev, double* out);

@@ -244,6 +244,45 @@ def model_params(dx=5e-9, ifce_width=10e-9, xcr0=0.30, xnb0=0.02, meshres=None,
     return p
 
 
+class OrcIcRecipe(ctypes.Structure):
+    """orc_ic_recipe (pfa_oracle.h)."""
+    _d, _i = ctypes.c_double, ctypes.c_int
+    _fields_ = [("nx", _i), ("ny", _i), ("nz", _i),
+                ("matrix", _d * 2), ("enrich", _d * 2), ("noise", _d), ("seed", ctypes.c_uint64),
+                ("n_bands", _i), ("band", (_i * 2) * 16),
+                ("n_particles", _i), ("centre", (_d * 3) * 64),
+                ("radius", _d * 64), ("phase", _i * 64),
+                ("dx", _d), ("width", _d)]
+
+
+def ic_fields(rec, lib=None):
+    """The four fields of a recipe dict (nx, ny, nz, matrix, enrich, noise,
+    seed, bands [(lo, hi)], particles [(x, y, z, radius, phase)], dx, width),
+    with the ghost ring."""
+    if lib is None:
+        lib = Oracle()
+    r = OrcIcRecipe()
+    r.nx, r.ny, r.nz = int(rec["nx"]), int(rec["ny"]), int(rec.get("nz", 0))
+    r.matrix[:] = rec["matrix"]
+    r.enrich[:] = rec["enrich"]
+    r.noise, r.seed = rec["noise"], int(rec["seed"])
+    bands, parts = rec.get("bands", []), rec.get("particles", [])
+    r.n_bands, r.n_particles = len(bands), len(parts)
+    for k, (lo, hi) in enumerate(bands):
+        r.band[k][0], r.band[k][1] = int(lo), int(hi)
+    for k, (x, y, z, rad, ph) in enumerate(parts):
+        r.centre[k][0], r.centre[k][1], r.centre[k][2] = x, y, z
+        r.radius[k], r.phase[k] = rad, int(ph)
+    r.dx, r.width = rec["dx"], rec["width"]
+    shape = ((r.nz + 2, r.ny + 2, r.nx + 2) if r.nz > 1 else (r.ny + 2, r.nx + 2))
+    out = [np.zeros(shape) for _ in range(4)]
+    f = lib.lib.orc_ic_fields
+    f.restype = None
+    f.argtypes = [ctypes.POINTER(OrcIcRecipe), ctypes.POINTER(_dbl_p)]
+    f(ctypes.byref(r), (_dbl_p * 4)(*[_ptr(a) for a in out]))
+    return out
+
+
 def philox(ctr, key, lib=None):
     if lib is None:
         lib = Oracle()

@@ -369,3 +369,94 @@ double orc_u53(uint32_t hi, uint32_t lo)
 #define E_XE_LAV_NB XE[2][1]
 #define ORC_RESTRICT restrict
 #include "step_impl.h"
+
+/* ---- initial conditions from a recipe ----
+ * Per interior cell (x, y, z), interior row-major index c:
+ *   u_Cr, u_Nb = orc_u53 of Philox4x32-10 words (0,1), (2,3), counter
+ *   (c lo, c hi, 0, 0x49430000), key = seed;
+ *   x = matrix + noise (2u - 1);  every band [lo, hi) over x adds enrich - matrix;
+ *   particles in order, inside the box |q - floor(c_q)| <= pad on every axis,
+ *   pad = ceil(R + 6 (width/2) / dx) + 1: the tanh profile of tanh_interp
+ *   (thermo/nucleation.c:12-16) phi = 0.5 - 0.5 tanh(dx (r - R) / (width/2)),
+ *   blended as embed_OPC does (src/alloy625.cpp:283-292):
+ *   x = p(phi) xe + (1 - p(phi)) x; the particle's phase takes max(phi_old, phi).
+ * Plain FP64 with no contraction (this file is built with -ffp-contract=off). */
+static double ic_p(double x)
+{
+	const double x2 = x * x, x3 = x2 * x;
+	return x3 * ((6.0 * x2 - 15.0 * x) + 10.0);
+}
+
+void orc_ic_fields(const orc_ic_recipe* r, double* f[4])
+{
+	const int is3d = r->nz > 1;
+	const int nz = is3d ? r->nz : 1;
+	const size_t sx = (size_t)r->nx + 2, sy = (size_t)r->ny + 2;
+	const double xe[2][2] = {{0.022966218927631978, 0.24984563695705883},
+	                         {0.37392129441013022, 0.25826261799015571}};
+	const double half_w = 0.5 * r->width;
+	const uint32_t key[2] = {(uint32_t)r->seed, (uint32_t)(r->seed >> 32)};
+	for (int z = 0; z < nz; z++)
+		for (int y = 0; y < r->ny; y++)
+			for (int x = 0; x < r->nx; x++) {
+				const uint64_t c = ((uint64_t)z * r->ny + y) * (uint64_t)r->nx + x;
+				const uint32_t ctr[4] = {(uint32_t)c, (uint32_t)(c >> 32), 0u, 0x49430000u};
+				uint32_t w[4];
+				orc_philox4x32_10(ctr, key, w);
+				double xcr = r->matrix[0] + r->noise * (2.0 * orc_u53(w[0], w[1]) - 1.0);
+				double xnb = r->matrix[1] + r->noise * (2.0 * orc_u53(w[2], w[3]) - 1.0);
+				const double dcr = r->enrich[0] - r->matrix[0], dnb = r->enrich[1] - r->matrix[1];
+				for (int b = 0; b < r->n_bands; b++)
+					if (x >= r->band[b][0] && x < r->band[b][1]) {
+						xcr += dcr;
+						xnb += dnb;
+					}
+				double ph[2] = {0.0, 0.0};
+				const int q[3] = {x, y, z};
+				for (int k = 0; k < r->n_particles; k++) {
+					const double R = r->radius[k];
+					const int pad = (int)ceil(R + 6.0 * half_w / r->dx) + 1;
+					int in = 1;
+					double r2 = 0.0;
+					for (int d = 0; d < (is3d ? 3 : 2); d++) {
+						const int fc = (int)floor(r->centre[k][d]);
+						if (q[d] < fc - pad || q[d] > fc + pad) in = 0;
+						const double t = (double)q[d] - r->centre[k][d];
+						r2 += t * t;
+					}
+					if (!in) continue;
+					const double phi = 0.5 - 0.5 * tanh(r->dx * (sqrt(r2) - R) / half_w);
+					const double pp = ic_p(phi), qq = 1.0 - pp;
+					const int ph_k = r->phase[k] == 0 ? 0 : 1;
+					xcr = pp * xe[ph_k][0] + qq * xcr;
+					xnb = pp * xe[ph_k][1] + qq * xnb;
+					if (phi > ph[ph_k]) ph[ph_k] = phi;
+				}
+				const double v[4] = {xcr, xnb, ph[0], ph[1]};
+				for (int k = 0; k < 4; k++) {
+					double* a = f[k] + (is3d ? (size_t)(z + 1) * sy * sx : 0);
+					a[(size_t)(y + 1) * sx + (x + 1)] = v[k];
+				}
+			}
+	/* ghost ring: the mirror of the interior, x then y then z */
+	for (int k = 0; k < 4; k++)
+		for (int z = 0; z < (is3d ? nz + 2 : 1); z++) {
+			double* a = f[k] + (is3d ? (size_t)z * sy * sx : 0);
+			for (size_t y = 1; y + 1 < sy; y++) {
+				a[y * sx] = a[y * sx + 1];
+				a[y * sx + sx - 1] = a[y * sx + sx - 2];
+			}
+			for (size_t x = 0; x < sx; x++) {
+				a[x] = a[sx + x];
+				a[(sy - 1) * sx + x] = a[(sy - 2) * sx + x];
+			}
+		}
+	if (is3d)
+		for (int k = 0; k < 4; k++) {
+			const size_t plane = sy * sx;
+			for (size_t i = 0; i < plane; i++) {
+				f[k][i] = f[k][plane + i];
+				f[k][(size_t)(nz + 1) * plane + i] = f[k][(size_t)nz * plane + i];
+			}
+		}
+}

@@ -107,6 +107,27 @@ double orc_energy2d(const double* f[4], int nx, int ny, double dx, double dy,
                     const double kappa[2], const double omega[2], double Omega,
                     double* chem, double* grad);
 
+/* ---- initial conditions from a recipe (the grids the reference builds on
+ * the host, src/alloy625.cpp:170-518, embed_OPC :262-294; the layout matches
+ * the library's recipe struct field for field) ---- */
+#define ORC_IC_MAX_BANDS 16
+#define ORC_IC_MAX_PARTICLES 64
+typedef struct {
+	int nx, ny, nz;
+	double matrix[2], enrich[2], noise;
+	uint64_t seed;
+	int n_bands;
+	int band[ORC_IC_MAX_BANDS][2];
+	int n_particles;
+	double centre[ORC_IC_MAX_PARTICLES][3];
+	double radius[ORC_IC_MAX_PARTICLES];
+	int phase[ORC_IC_MAX_PARTICLES];
+	double dx, width;
+} orc_ic_recipe;
+/* fields in the ghost-ring layout ((ny+2) x (nx+2), or (nz+2) x (ny+2) x (nx+2)
+ * when nz > 1), ghost ring = the mirror of the interior */
+void orc_ic_fields(const orc_ic_recipe* r, double* f[4]);
+
 #ifdef __cplusplus
 }
 #endif

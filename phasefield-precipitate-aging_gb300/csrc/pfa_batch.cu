@@ -302,6 +302,35 @@ const Slot* live_slot(Batch* b, int slot) {
   return &b->slots[slot];
 }
 
+// A slot for an nx x ny grid (ghost-ring sizes) in the arena; its records
+// are filled from the FP64 staging fields by the caller.
+int place(Batch* b, int nx, int ny, int* id_out) {
+  Slot s;
+  s.Nx = nx - 2;
+  s.Ny = ny - 2;
+  s.pitch = (s.Nx + 31) / 32 * 32;
+  s.bytes = block_bytes(s.Nx, s.Ny);
+  if (!arena_alloc(b, s.bytes, &s.off)) {
+    set_error(PFA_ENOMEM, "pfa_batch_add: the grid does not fit in the batch arena");
+    return PFA_ENOMEM;  // admission refusal: not printed
+  }
+  s.live = true;
+  int id = -1;
+  for (int i = 0; i < int(b->slots.size()); i++)
+    if (!b->slots[i].live) {
+      id = i;
+      break;
+    }
+  if (id < 0) {
+    id = int(b->slots.size());
+    b->slots.push_back(s);
+  } else {
+    b->slots[id] = s;
+  }
+  *id_out = id;
+  return 0;
+}
+
 }  // namespace
 }  // namespace pfa
 
@@ -366,34 +395,32 @@ int pfa_batch_add(void* handle, int nx, int ny, const double* conc_Cr, const dou
   if (!conc_Cr || !conc_Nb || !phi_del || !phi_lav || !slot)
     return fail(PFA_EINVAL, "pfa_batch_add: null argument");
   if (nx < 3 || ny < 3) return fail(PFA_EINVAL, "pfa_batch_add: grid smaller than 3x3");
-  Slot s;
-  s.Nx = nx - 2;
-  s.Ny = ny - 2;
-  s.pitch = (s.Nx + 31) / 32 * 32;
-  s.bytes = block_bytes(s.Nx, s.Ny);
-  if (!arena_alloc(b, s.bytes, &s.off)) {
-    set_error(PFA_ENOMEM, "pfa_batch_add: the grid does not fit in the batch arena");
-    return PFA_ENOMEM;  // admission refusal: not printed
-  }
-  s.live = true;
   int id = -1;
-  for (int i = 0; i < int(b->slots.size()); i++)
-    if (!b->slots[i].live) {
-      id = i;
-      break;
-    }
-  if (id < 0) {
-    id = int(b->slots.size());
-    b->slots.push_back(s);
-  } else {
-    b->slots[id] = s;
-  }
+  if (int r = place(b, nx, ny, &id)) return r;
   const size_t cells = size_t(nx) * ny;
   if (int r = ensure_stage(b, cells)) return r;
   const double* src[4] = {conc_Cr, conc_Nb, phi_del, phi_lav};
   for (int k = 0; k < 4; k++)
     CKB(cudaMemcpyAsync(b->stage[k], src[k], cells * sizeof(double), cudaMemcpyHostToDevice, b->st));
-  CKB(launch_import_f32(conv(b, s), b->st));
+  CKB(launch_import_f32(conv(b, b->slots[id]), b->st));
+  b->dirty = true;
+  *slot = id;
+  return 0;
+}
+
+int pfa_batch_add_ic(void* handle, const pfa_ic_recipe* r, int* slot) {
+  Batch* b = get(handle);
+  if (!b) return fail(PFA_ESTATE, "pfa_batch_add_ic: null handle");
+  if (!slot) return fail(PFA_EINVAL, "pfa_batch_add_ic: null argument");
+  if (const char* msg = ic_check(r)) return fail(PFA_EINVAL, msg);
+  if (r->nz > 1) return fail(PFA_EINVAL, "pfa_batch_add_ic: the batch holds 2D grids (nz <= 1)");
+  const int nx = r->nx + 2, ny = r->ny + 2;
+  if (nx < 3 || ny < 3) return fail(PFA_EINVAL, "pfa_batch_add_ic: grid smaller than 3x3");
+  int id = -1;
+  if (int e = place(b, nx, ny, &id)) return e;
+  if (int e = ensure_stage(b, size_t(nx) * ny)) return e;
+  CKB(launch_ic_fill(*r, b->stage, b->st));
+  CKB(launch_import_f32(conv(b, b->slots[id]), b->st));
   b->dirty = true;
   *slot = id;
   return 0;

@@ -284,11 +284,10 @@ size_t pfa3d_footprint(int nx, int ny, int nz, int precision) {
   return 4 * ghost * sizeof(double) + 2 * recs * (16 + 8) + nuc;
 }
 
-int pfa3d_create(void** handle, int nx, int ny, int nz, const double* params, const double* dxyz,
-                 const double* conc_Cr, const double* conc_Nb, const double* phi_del,
-                 const double* phi_lav, int precision) {
-  if (!handle || !params || !dxyz || !conc_Cr || !conc_Nb || !phi_del || !phi_lav)
-    return err(PFA_EINVAL, "pfa3d_create: null argument");
+// pfa3d_create's body: the initial fields come from host arrays (src) or
+// are built on the device from a recipe (r)
+static int create3d(void** handle, int nx, int ny, int nz, const double* params, const double* dxyz,
+                    const double* const* src, const pfa_ic_recipe* r, int precision) {
   if (nx < 3 || ny < 3 || nz < 3) return err(PFA_EINVAL, "pfa3d_create: grid smaller than 3^3");
   if (precision != PFA_FP64 && precision != PFA_FP32)
     return err(PFA_EINVAL, "pfa3d_create: 3D grids run in PFA_FP64 or PFA_FP32");
@@ -320,12 +319,15 @@ int pfa3d_create(void** handle, int nx, int ny, int nz, const double* params, co
   }
   CK3(cudaStreamCreateWithFlags(&g->st, cudaStreamNonBlocking));
   const size_t n = ghost_cells(g);
-  const double* src[4] = {conc_Cr, conc_Nb, phi_del, phi_lav};
   const int sets = precision == PFA_FP64 ? 2 : 1;
   for (int b = 0; b < sets; b++)
     for (int k = 0; k < 4; k++) CK3(cudaMalloc(reinterpret_cast<void**>(&g->f64[b][k]), n * sizeof(double)));
-  for (int k = 0; k < 4; k++)
-    CK3(cudaMemcpyAsync(g->f64[0][k], src[k], n * sizeof(double), cudaMemcpyHostToDevice, g->st));
+  if (r) {
+    CK3(launch_ic_fill(*r, g->f64[0], g->st));
+  } else {
+    for (int k = 0; k < 4; k++)
+      CK3(cudaMemcpyAsync(g->f64[0][k], src[k], n * sizeof(double), cudaMemcpyHostToDevice, g->st));
+  }
   if (precision == PFA_FP32) {
     g->pitch32 = ((g->Nx + 31) / 32) * 32;
     const size_t recs = size_t(g->pitch32) * g->Ny * g->Nz;
@@ -349,6 +351,23 @@ int pfa3d_create(void** handle, int nx, int ny, int nz, const double* params, co
   CK3(cudaMemsetAsync(g->call_dev, 0, sizeof(unsigned long long), g->st));
   CK3(cudaStreamSynchronize(g->st));
   return 0;
+}
+
+int pfa3d_create(void** handle, int nx, int ny, int nz, const double* params, const double* dxyz,
+                 const double* conc_Cr, const double* conc_Nb, const double* phi_del,
+                 const double* phi_lav, int precision) {
+  if (!handle || !params || !dxyz || !conc_Cr || !conc_Nb || !phi_del || !phi_lav)
+    return err(PFA_EINVAL, "pfa3d_create: null argument");
+  const double* src[4] = {conc_Cr, conc_Nb, phi_del, phi_lav};
+  return create3d(handle, nx, ny, nz, params, dxyz, src, nullptr, precision);
+}
+
+int pfa3d_create_ic(void** handle, const pfa_ic_recipe* r, const double* params,
+                    const double* dxyz, int precision) {
+  if (!handle || !params || !dxyz) return err(PFA_EINVAL, "pfa3d_create_ic: null argument");
+  if (const char* msg = ic_check(r)) return err(PFA_EINVAL, msg);
+  if (r->nz <= 1) return err(PFA_EINVAL, "pfa3d_create_ic: a 3D recipe needs nz > 1");
+  return create3d(handle, r->nx + 2, r->ny + 2, r->nz + 2, params, dxyz, nullptr, r, precision);
 }
 
 int pfa3d_set_nucleation(void* handle, uint64_t seed, int interval, double sigma_del,

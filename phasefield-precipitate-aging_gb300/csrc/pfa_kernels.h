@@ -7,6 +7,8 @@
 
 #include "pfa_internal.h"
 
+struct pfa_ic_recipe;  // pfa_gb300.h
+
 namespace pfa {
 
 // Arguments of one fused 2D step (passed by value to the kernel).
@@ -84,6 +86,11 @@ int batch_resident_ctas();   // CTAs of k_batch_f32 resident on the device at on
 int batch_warps_per_cta();
 int batch_strip_cols();
 cudaError_t launch_import_f32(const ConvArgs& a, cudaStream_t s);
+
+// initial conditions from a recipe (pfa_ic.cu): validation (message or
+// nullptr) and the fill of four FP64 fields in the reference layout
+const char* ic_check(const ::pfa_ic_recipe* r);
+cudaError_t launch_ic_fill(const ::pfa_ic_recipe& r, double* const f[4], cudaStream_t s);
 cudaError_t launch_export_f32(const ConvArgs& a, cudaStream_t s);
 
 // Arguments of one 3D step (pfa_step3d.cu).  F64: in/out = four ghost-ring

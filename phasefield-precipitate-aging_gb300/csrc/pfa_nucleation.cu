@@ -31,31 +31,6 @@ namespace pfa {
 
 using namespace dev;
 
-// ---- Philox4x32-10 (Salmon, Moraes, Dror, Shaw: "Parallel random numbers:
-// as easy as 1, 2, 3", SC'11): 10 rounds of two 32x32->64 multiplies with
-// Weyl-sequence key bumps. ----
-__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
-  constexpr uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
-  constexpr uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
-#pragma unroll
-  for (int r = 0; r < 10; r++) {
-    if (r > 0) {
-      k.x += W0;
-      k.y += W1;
-    }
-    const uint32_t hi0 = __umulhi(M0, c.x), lo0 = M0 * c.x;
-    const uint32_t hi1 = __umulhi(M1, c.z), lo1 = M1 * c.z;
-    c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
-  }
-  return c;
-}
-
-// 53 random bits -> uniform double in (0, 1]
-__device__ __forceinline__ double u53(uint32_t hi, uint32_t lo) {
-  const unsigned long long k = ((((unsigned long long)hi) << 32) | lo) >> 11;
-  return double(k + 1ull) * (1.0 / 9007199254740992.0);
-}
-
 namespace {
 
 template <class T>

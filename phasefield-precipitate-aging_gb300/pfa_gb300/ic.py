@@ -169,6 +169,38 @@ def batch_grid(side, seed):
                   stripe_width=max(4, min(64, side // 4)), n_particles=4)
 
 
+# ---- recipes: the same kinds of grid, built on the device (pfa_ic_recipe) ----
+
+def recipe2d(nx, ny, seed, matrix=MATRIX, enrich=ENRICH, noise=0.002, stripes=None,
+             stripe_width=64, n_particles=4, radius=8.0, dx=5e-9, width=10e-9):
+    """Recipe of a 2D grid like grid2d's: noise from the device's Philox
+    stream (keyed by seed), stripes along y, particles at seeded centres
+    alternating delta / laves."""
+    rng = np.random.default_rng(seed)
+    if stripes is None:
+        stripes = [nx // 2 - stripe_width // 2]
+    bands = [(max(0, s), min(nx, s + stripe_width)) for s in stripes]
+    centres = _centres(rng, n_particles, (ny, nx), radius, width / dx)
+    parts = [(float(c[1]), float(c[0]), 0.0, float(radius), k % 2) for k, c in enumerate(centres)]
+    return {"nx": nx, "ny": ny, "nz": 0, "matrix": tuple(matrix), "enrich": tuple(enrich),
+            "noise": noise, "seed": int(seed), "bands": bands, "particles": parts,
+            "dx": dx, "width": width}
+
+
+def recipe3d(nx, ny, nz, seed, matrix=MATRIX, enrich=ENRICH, noise=0.002, slab=64,
+             n_particles=32, radius=6.0, dx=5e-9, width=10e-9):
+    """Recipe of a 3D grid like grid3d's: one seeded enriched slab normal to
+    x, seeded spheres alternating delta / laves."""
+    rng = np.random.default_rng(seed)
+    s = int(rng.integers(0, max(1, nx - slab)))
+    centres = _centres(rng, n_particles, (nz, ny, nx), radius, width / dx)
+    parts = [(float(c[2]), float(c[1]), float(c[0]), float(radius), k % 2)
+             for k, c in enumerate(centres)]
+    return {"nx": nx, "ny": ny, "nz": nz, "matrix": tuple(matrix), "enrich": tuple(enrich),
+            "noise": noise, "seed": int(seed), "bands": [(s, min(nx, s + slab))],
+            "particles": parts, "dx": dx, "width": width}
+
+
 # request sizes of the serving workload: (dimension, side)
 SERVE_SIZES = ((2, 256), (2, 1024), (2, 4096), (3, 128), (3, 256))
 
@@ -199,3 +231,17 @@ def serve_fields(item):
                       stripe_width=max(4, min(64, s // 4)), n_particles=4)
     return grid3d(s, s, s, item["seed"] + 7, matrix=m, enrich=e, slab=max(4, s // 8),
                   n_particles=8, radius=6.0)
+
+
+def serve_recipe(item):
+    """serve_fields' request as a recipe the device builds (same composition
+    draws, stripe / slab and particle counts)."""
+    rng = np.random.default_rng(item["seed"])
+    m = (rng.uniform(*MATRIX_RANGE[0]), rng.uniform(*MATRIX_RANGE[1]))
+    e = (rng.uniform(*ENRICH_RANGE[0]), rng.uniform(*ENRICH_RANGE[1]))
+    s = item["side"]
+    if item["dim"] == 2:
+        return recipe2d(s, s, item["seed"] + 7, matrix=m, enrich=e,
+                        stripe_width=max(4, min(64, s // 4)), n_particles=4)
+    return recipe3d(s, s, s, item["seed"] + 7, matrix=m, enrich=e, slab=max(4, s // 8),
+                    n_particles=8, radius=6.0)

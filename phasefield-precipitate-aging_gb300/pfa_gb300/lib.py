@@ -35,6 +35,59 @@ class CudaData(ctypes.Structure):
                                     "conc_Cr_lav", "conc_Nb_gam", "conc_Nb_del", "conc_Nb_lav")])
 
 
+IC_MAX_BANDS, IC_MAX_PARTICLES = 16, 64
+
+
+class IcRecipe(ctypes.Structure):
+    """Layout of pfa_ic_recipe (pfa_gb300.h): a grid the device builds."""
+    _fields_ = [("nx", _i), ("ny", _i), ("nz", _i),
+                ("matrix", _d * 2), ("enrich", _d * 2), ("noise", _d), ("seed", ctypes.c_uint64),
+                ("n_bands", _i), ("band", (_i * 2) * IC_MAX_BANDS),
+                ("n_particles", _i), ("centre", (_d * 3) * IC_MAX_PARTICLES),
+                ("radius", _d * IC_MAX_PARTICLES), ("phase", _i * IC_MAX_PARTICLES),
+                ("dx", _d), ("width", _d)]
+
+
+def ic_recipe(rec):
+    """IcRecipe from a recipe dict: nx, ny, nz (interior; nz <= 1 for 2D),
+    matrix, enrich, noise, seed, bands [(lo, hi)], particles
+    [(x, y, z, radius, phase)], dx, width."""
+    r = IcRecipe()
+    r.nx, r.ny, r.nz = int(rec["nx"]), int(rec["ny"]), int(rec.get("nz", 0))
+    r.matrix[:] = rec["matrix"]
+    r.enrich[:] = rec["enrich"]
+    r.noise = rec["noise"]
+    r.seed = int(rec["seed"])
+    bands, parts = rec.get("bands", []), rec.get("particles", [])
+    if len(bands) > IC_MAX_BANDS or len(parts) > IC_MAX_PARTICLES:
+        raise ValueError("recipe: too many bands or particles")
+    r.n_bands = len(bands)
+    for k, (lo, hi) in enumerate(bands):
+        r.band[k][0], r.band[k][1] = int(lo), int(hi)
+    r.n_particles = len(parts)
+    for k, (x, y, z, rad, ph) in enumerate(parts):
+        r.centre[k][0], r.centre[k][1], r.centre[k][2] = x, y, z
+        r.radius[k] = rad
+        r.phase[k] = int(ph)
+    r.dx, r.width = rec["dx"], rec["width"]
+    return r
+
+
+def ic_shape(rec):
+    """Shape of the recipe's fields with the ghost ring."""
+    if int(rec.get("nz", 0)) > 1:
+        return (rec["nz"] + 2, rec["ny"] + 2, rec["nx"] + 2)
+    return (rec["ny"] + 2, rec["nx"] + 2)
+
+
+def ic_generate(rec, ptrs, stream=None):
+    """Build the recipe's four fields in caller-owned device arrays (device
+    addresses, reference layout) on `stream` (a cudaStream_t value or None)."""
+    r = ic_recipe(rec)
+    check(load().pfa_ic_generate(ctypes.byref(r), *[ctypes.c_void_p(int(q)) for q in ptrs],
+                                 ctypes.c_void_p(stream or 0)), "pfa_ic_generate")
+
+
 _lib = None
 
 
@@ -117,6 +170,10 @@ def load():
                                 ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)]),
         "pfa_batch_stream": (ctypes.c_void_p, [ctypes.c_void_p]),
         "pfa_batch_destroy": (_i, [ctypes.c_void_p]),
+        "pfa_ic_generate": (_i, [ctypes.POINTER(IcRecipe)] + [ctypes.c_void_p] * 5),
+        "pfa_batch_add_ic": (_i, [ctypes.c_void_p, ctypes.POINTER(IcRecipe), ctypes.POINTER(_i)]),
+        "pfa3d_create_ic": (_i, [ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(IcRecipe), _dp,
+                                 _dp, _i]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -322,19 +379,27 @@ def params_vector(p):
 class Grid3D:
     """One 3D grid (7-point Laplacian), fields (nz, ny, nx) with the ghost ring."""
 
-    def __init__(self, fields, params, precision="fp64"):
+    def __init__(self, fields, params, precision="fp64", recipe=None):
+        """From host fields, or (fields None) built on the device from a 3D
+        recipe dict (see ic_recipe)."""
         L = load()
         self.L = L
-        f = [np.ascontiguousarray(a, dtype=np.float64) for a in fields]
-        self.shape = f[0].shape
-        nz, ny, nx = self.shape
         self.params = dict(params)
         self._pv = params_vector(params)
         self._d = np.array([params["dx"], params.get("dy", params["dx"]),
                             params.get("dz", params["dx"])], dtype=np.float64)
         self.h = ctypes.c_void_p()
-        check(L.pfa3d_create(ctypes.byref(self.h), nx, ny, nz, _ptr(self._pv), _ptr(self._d),
-                             *[_ptr(a) for a in f], PRECISIONS[precision]), "pfa3d_create")
+        if fields is None:
+            self.shape = ic_shape(recipe)
+            r = ic_recipe(recipe)
+            check(L.pfa3d_create_ic(ctypes.byref(self.h), ctypes.byref(r), _ptr(self._pv),
+                                    _ptr(self._d), PRECISIONS[precision]), "pfa3d_create_ic")
+        else:
+            f = [np.ascontiguousarray(a, dtype=np.float64) for a in fields]
+            self.shape = f[0].shape
+            nz, ny, nx = self.shape
+            check(L.pfa3d_create(ctypes.byref(self.h), nx, ny, nz, _ptr(self._pv), _ptr(self._d),
+                                 *[_ptr(a) for a in f], PRECISIONS[precision]), "pfa3d_create")
         self._live = True
 
     @staticmethod
@@ -437,6 +502,17 @@ class Batch:
             return None
         check(rc, "pfa_batch_add")
         self.shapes[slot.value] = (ny, nx)
+        return slot.value
+
+    def add_recipe(self, rec):
+        """add() with the grid built on the device from a 2D recipe dict."""
+        r = ic_recipe(rec)
+        slot = _i()
+        rc = self.L.pfa_batch_add_ic(self.h, ctypes.byref(r), ctypes.byref(slot))
+        if rc == ENOMEM:
+            return None
+        check(rc, "pfa_batch_add_ic")
+        self.shapes[slot.value] = ic_shape(rec)
         return slot.value
 
     def remove(self, slot):

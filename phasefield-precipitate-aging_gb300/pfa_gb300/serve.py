@@ -2,8 +2,8 @@
 HBM-footprint admission.
 
 A request is one initial condition (four fields in the reference layout, 2D
-(ny, nx) or 3D (nz, ny, nx) with the ghost ring) and a number of explicit
-steps.  Requests are admitted first-in first-out while their device
+(ny, nx) or 3D (nz, ny, nx) with the ghost ring, or a recipe the device
+builds them from, pfa_ic_recipe) and a number of explicit steps.  Requests are admitted first-in first-out while their device
 footprint fits the budget; 2D requests join one ``Batch`` (all advance with
 one launch per time step), 3D requests get their own ``Grid3D`` handle on
 their own stream, so 2D and 3D work overlap on the GPU.  Every tick advances
@@ -25,17 +25,28 @@ import numpy as np
 @dataclass
 class Request:
     rid: int
-    fields: list              # four float64 arrays with the ghost ring
+    fields: Optional[list]    # four float64 arrays with the ghost ring (or None: recipe)
     steps: int
     arrival: float = 0.0      # seconds after the start of the trace
+    recipe: Optional[dict] = None  # initial condition the device builds (pfa_ic_recipe)
+
+    @property
+    def shape(self):
+        """Field shape with the ghost ring."""
+        if self.fields is not None:
+            return self.fields[0].shape
+        r = self.recipe
+        if int(r.get("nz", 0)) > 1:
+            return (r["nz"] + 2, r["ny"] + 2, r["nx"] + 2)
+        return (r["ny"] + 2, r["nx"] + 2)
 
     @property
     def dim(self):
-        return self.fields[0].ndim
+        return len(self.shape)
 
     @property
     def cells(self):
-        return int(np.prod([n - 2 for n in self.fields[0].shape]))
+        return int(np.prod([n - 2 for n in self.shape]))
 
 
 @dataclass
@@ -71,18 +82,22 @@ class GpuBackend:
 
     def footprint(self, req):
         if req.dim == 2:
-            return self.lib.Batch.footprint(req.fields[0].shape)
-        return self.lib.Grid3D.footprint(req.fields[0].shape, "fp32")
+            return self.lib.Batch.footprint(req.shape)
+        return self.lib.Grid3D.footprint(req.shape, "fp32")
 
     def admit(self, req):
-        """Place the request on the device; None when its budget has no room."""
+        """Place the request on the device (its fields uploaded, or built
+        there from its recipe); None when its budget has no room."""
         if req.dim == 2:
-            slot = self.batch.add(req.fields)
+            if req.fields is None:
+                slot = self.batch.add_recipe(req.recipe)
+            else:
+                slot = self.batch.add(req.fields)
             return None if slot is None else ("2d", slot)
         need = self.footprint(req)
         if self.used_3d + need > self.budget_3d:
             return None
-        g = self.lib.Grid3D(req.fields, self.params3d, precision="fp32")
+        g = self.lib.Grid3D(req.fields, self.params3d, precision="fp32", recipe=req.recipe)
         self.used_3d += need
         return ("3d", g, need)
 
@@ -124,6 +139,7 @@ class Server:
         self.done: List[Record] = []
         self.ticks = 0
         self.cell_updates = 0
+        self.step_launches = 0  # step kernels enqueued: one per batch step, one per 3D step
 
     def now(self):
         if self.t0 is None:
@@ -158,6 +174,7 @@ class Server:
         n2 = min([self.tick_steps] + [r.remaining for r in two]) if two else 0
         items3 = [(r.handle, min(self.tick_steps, r.remaining)) for r in three]
         self.backend.advance(n2, [r.handle for r in two], items3)
+        self.step_launches += n2 + sum(n for _, n in items3)
         for r in two:
             r.done_steps += n2
             self.cell_updates += n2 * r.req.cells
