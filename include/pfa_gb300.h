@@ -153,7 +153,9 @@ int pfa3d_destroy(void* handle);
  * doubles of pfa3d_create) and dxy = dx, dy.  Grids join (pfa_batch_add:
  * fields in the reference layout, ny x nx doubles with the ghost ring;
  * PFA_ENOMEM, not printed, when the arena has no room) and leave
- * (pfa_batch_remove) between runs; slot ids are reused.  A member advances
+ * (pfa_batch_remove) between runs; slot ids are reused.  pfa_batch_add reads
+ * page-locked host arrays asynchronously: keep them unchanged until the next
+ * pfa_batch_sync (or pfa_batch_read, which waits).  A member advances
  * bit-for-bit as it would alone.  pfa_batch_footprint gives the arena bytes a
  * grid takes.  pfa_batch_tune times the launch shapes (rows per segment,
  * persistent or one warp per unit) on the current members without advancing
@@ -263,6 +265,9 @@ int pfa_model_fast_coef(float* out, int n);
 /* Philox4x32-10 on the device for n counters (4 words each) under one
  * 64-bit key, for the generator's known-answer test */
 int pfa_philox_block(const uint32_t* ctr, uint64_t key, uint32_t* out, int n);
+/* the FP32 form's split of n doubles on the device: hi = nearest FP32,
+ * c = float(double(hi) - v) (value = hi - c), for its test */
+int pfa_split_block(const double* in, float* hi, float* c, int n);
 
 #ifdef __cplusplus
 }

@@ -98,6 +98,7 @@ struct State {
   int cand_cap = 0;
   double* sum_partial = nullptr;
   double* sum_out = nullptr;
+  cudaEvent_t xev[8] = {};  // chunked transfers (created on first use)
   double* nrg_map[2] = {};  // per-node chemical / gradient energy (on request)
   std::vector<GraphEntry> graphs;
 };
@@ -590,6 +591,8 @@ static int free_core(CudaData* dev) {
   cudaFree(s->sum_out);
   cudaFree(s->nrg_map[0]);
   cudaFree(s->nrg_map[1]);
+  for (cudaEvent_t e : s->xev)
+    if (e) cudaEventDestroy(e);
   cudaStream_t st[4] = {dev->str_A, dev->str_B, dev->str_C, dev->str_D};
   for (auto x : st)
     if (x) cudaStreamDestroy(x);
@@ -602,15 +605,55 @@ static int free_core(CudaData* dev) {
   return 0;
 }
 
+// Read-outs of the FP32 form move the FP64 fields in row bands so that the
+// layout conversion of one band overlaps the copy of the one before: the
+// conversions run on the library stream, the copies on the CudaData's second
+// stream (str_B), ordered band by band with events.
+constexpr int kXferBands = 8;
+
+static int ensure_xfer(State* s) {
+  if (s->xev[0]) return 0;
+  for (int i = 0; i < kXferBands; i++)
+    CK(cudaEventCreateWithFlags(&s->xev[i], cudaEventDisableTiming));
+  return 0;
+}
+
+// interior rows whose FP64 row (ghost-ring layout) lies in [r0, r1)
+static void band_rows(const State* s, int r0, int r1, ConvArgs& c) {
+  c.y0 = r0 > 0 ? r0 - 1 : 0;
+  c.y1 = r1 - 1 < s->Ny ? r1 - 1 : s->Ny;
+}
+
 static int read_core(CudaData* dev, double* cr, double* nb, double* pd, double* pl, int nx,
                      int ny) {
   State* s = lookup(dev);
   if (!s) return fail(PFA_ESTATE, "read_out_result: unknown CudaData");
   if (nx != s->nx || ny != s->ny) return fail(PFA_EINVAL, "read_out_result: size mismatch");
-  if (int r = f32_export(dev, s)) return r;
-  const size_t n = size_t(nx) * ny;
   double* dst[4] = {cr, nb, pd, pl};
   const double* src[4] = {dev->conc_Cr_old, dev->conc_Nb_old, dev->phi_del_old, dev->phi_lav_old};
+  if (s->precision != PFA_FP64 && s->f32_live && dev->str_B) {
+    if (int r = ensure_xfer(s)) return r;
+    const int rows = (ny + kXferBands - 1) / kXferBands;
+    for (int i = 0; i < kXferBands; i++) {
+      const int r0 = i * rows, r1 = r0 + rows < ny ? r0 + rows : ny;
+      if (r0 >= r1) break;
+      ConvArgs c = conv_args(dev, s);
+      band_rows(s, r0, r1, c);
+      // a band's rows are written by its own interior rows (ghost rows by the
+      // first and last interior row, which lie in the first and last band)
+      if (c.y1 > c.y0) CK(launch_export_f32(c, s->st));
+      CK(cudaEventRecord(s->xev[i], s->st));
+      CK(cudaStreamWaitEvent(dev->str_B, s->xev[i], 0));
+      const size_t off = size_t(r0) * nx, bytes = size_t(r1 - r0) * nx * sizeof(double);
+      for (int k = 0; k < 4; k++)
+        if (dst[k])
+          CK(cudaMemcpyAsync(dst[k] + off, src[k] + off, bytes, cudaMemcpyDeviceToHost, dev->str_B));
+    }
+    CK(cudaStreamSynchronize(dev->str_B));
+    return 0;
+  }
+  if (int r = f32_export(dev, s)) return r;
+  const size_t n = size_t(nx) * ny;
   for (int k = 0; k < 4; k++)
     if (dst[k]) CK(cudaMemcpyAsync(dst[k], src[k], n * sizeof(double), cudaMemcpyDeviceToHost, s->st));
   CK(cudaStreamSynchronize(s->st));
@@ -627,6 +670,17 @@ static int upload_core(CudaData* dev, const double* cr, const double* nb, const 
   double* dst[4] = {dev->conc_Cr_old, dev->conc_Nb_old, dev->phi_del_old, dev->phi_lav_old};
   for (int k = 0; k < 4; k++)
     CK(cudaMemcpyAsync(dst[k], src[k], n * sizeof(double), cudaMemcpyHostToDevice, s->st));
+  if (s->precision != PFA_FP64) {
+    // convert now (whole-field copies: each extra copy call costs ~15 us, more
+    // than banding the conversion behind the copies would save)
+    if (int r = ensure_f32(s)) return r;
+    s->cur = 0;
+    CK(launch_import_f32(conv_args(dev, s), s->st));
+    CK(cudaStreamSynchronize(s->st));  // page-locked sources are read asynchronously
+    s->f32_live = true;
+    return 0;
+  }
+  CK(cudaStreamSynchronize(s->st));  // page-locked sources are read asynchronously
   s->f32_live = false;
   return 0;
 }
@@ -1103,6 +1157,21 @@ int pfa_model_fast_coef(float* out, int n) {
   std::memcpy(out + 6, k.num, 24 * sizeof(float));
   std::memcpy(out + 30, k.dP, 12 * sizeof(float));
   std::memcpy(out + 42, k.xe_gam, 2 * sizeof(float));
+  return 0;
+}
+
+int pfa_split_block(const double* in, float* hi, float* c, int n) {
+  if (n <= 0 || !in || !hi || !c) return fail(PFA_EINVAL, "pfa_split_block: bad argument");
+  double* din = nullptr;
+  float* dout = nullptr;
+  CK(cudaMalloc(reinterpret_cast<void**>(&din), size_t(n) * 8));
+  CK(cudaMalloc(reinterpret_cast<void**>(&dout), size_t(n) * 8));
+  CK(cudaMemcpy(din, in, size_t(n) * 8, cudaMemcpyHostToDevice));
+  CK(launch_split_block(din, dout, dout + n, n, 0));
+  CK(cudaMemcpy(hi, dout, size_t(n) * 4, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(c, dout + n, size_t(n) * 4, cudaMemcpyDeviceToHost));
+  cudaFree(din);
+  cudaFree(dout);
   return 0;
 }
 

@@ -191,6 +191,44 @@ __device__ __forceinline__ float dF_local32(float ph, float pj, float dP, float 
   return fmaf(-pp, dP, fmaf(alpha2 * ph, pj * pj, well));
 }
 
+// hi = the FP32 value nearest v and c = float(double(hi) - v): the split of
+// the FP32 form (value = hi - c), computed from the bits of v without FP64
+// arithmetic (this part issues FP64 at ~1/64 of the FP32 rate, and the
+// conversions would bound the layout conversion kernels).  For 950 <= E <=
+// 1149 (E: v's biased exponent) hi and c are FP32-normal and double(hi) - v
+// = -rem 2^(E-1075) is exact with |rem| <= 2^28, so rounding -rem to FP32
+// and scaling by the power of two gives the FP64 expression's result
+// bit-for-bit; zeros take hi = v, c = +0; every other double takes the FP64
+// expression itself.
+__device__ __forceinline__ void split_f64(double v, float& hi, float& c) {
+  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v));
+  const int E = int((b >> 52) & 0x7ff);
+  const unsigned sign = unsigned(b >> 32) & 0x80000000u;
+  if ((b << 1) == 0ull) {
+    hi = __int_as_float(int(sign));
+    c = 0.0f;
+    return;
+  }
+  if (E < 950 || E > 1149) {
+    hi = float(v);
+    c = float(double(hi) - v);
+    return;
+  }
+  const unsigned long long M = (b & 0xfffffffffffffull) | (1ull << 52);
+  unsigned q = unsigned(M >> 29);  // the 24 leading bits
+  int rem = int(M & 0x1fffffffull);  // the 29 dropped bits
+  if (rem > (1 << 28) || (rem == (1 << 28) && (q & 1u))) {  // round to nearest even
+    q += 1u;
+    rem -= 1 << 29;
+  }
+  // q = 2^24 carries into the exponent field
+  hi = __int_as_float(int(sign | ((unsigned(E - 896) << 23) + (q - (1u << 23)))));
+  const float scale = __int_as_float((E - 1075 + 127) << 23);
+  // c = hi - v = -rem 2^(E-1075) for v > 0, +rem 2^(E-1075) for v < 0
+  // (rem = 0 gives +0, as the FP64 subtraction does)
+  c = __int2float_rn(sign ? rem : -rem) * scale;
+}
+
 // Philox4x32-10 (Salmon, Moraes, Dror, Shaw: "Parallel random numbers: as
 // easy as 1, 2, 3", SC'11): 10 rounds of two 32x32->64 multiplies with
 // Weyl-sequence key bumps (nucleation draws, initial-condition noise).

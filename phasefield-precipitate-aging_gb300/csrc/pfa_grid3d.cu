@@ -482,6 +482,7 @@ int pfa3d_upload(void* handle, const double* conc_Cr, const double* conc_Nb,
   const size_t n = ghost_cells(g) * sizeof(double);
   for (int k = 0; k < 4; k++)
     CK3(cudaMemcpyAsync(g->f64[0][k], src[k], n, cudaMemcpyHostToDevice, g->st));
+  CK3(cudaStreamSynchronize(g->st));  // page-locked sources are read asynchronously
   g->cur = 0;
   g->f32_live = false;
   return 0;

@@ -43,6 +43,7 @@ struct ConvArgs {
   void* B;
   int pack;
   int Nx, Ny, pitch64, pitch32;
+  int y0, y1;  // interior rows converted, [y0, y1); y1 = 0: all rows
 };
 
 // Arguments of the reference's per-stage kernels (compat mode).

@@ -531,6 +531,17 @@ cudaError_t nucleation_setup() {
   return cudaFuncSetAttribute(k_nuc_apply<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
 }
 
+// The FP32-form split exposed for its test (one block of doubles).
+__global__ void k_split_block(const double* in, float* hi, float* c, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) split_f64(in[i], hi[i], c[i]);
+}
+
+cudaError_t launch_split_block(const double* in, float* hi, float* c, int n, cudaStream_t s) {
+  k_split_block<<<(n + 255) / 256, 256, 0, s>>>(in, hi, c, n);
+  return cudaGetLastError();
+}
+
 // Philox exposed for the generator test (one block of counters).
 __global__ void k_philox_block(const uint4* ctr, uint2 key, uint4* out, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;

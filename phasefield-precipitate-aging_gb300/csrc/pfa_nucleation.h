@@ -70,5 +70,6 @@ const char* nucleation_constants(NucArgs& a, double dx, double dy, double dz, do
                                  double unit_a);
 cudaError_t nucleation_setup();
 cudaError_t launch_philox_block(const void* ctr, uint64_t key, void* out, int n, cudaStream_t s);
+cudaError_t launch_split_block(const double* in, float* hi, float* c, int n, cudaStream_t s);
 
 }  // namespace pfa

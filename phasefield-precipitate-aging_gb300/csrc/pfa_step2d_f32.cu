@@ -306,17 +306,13 @@ __global__ void __launch_bounds__(32 * kWarps, 8) k_batch_f32(Step2DArgs a, Batc
 // ---- layout conversion between the reference's FP64 fields and the form ----
 __global__ void k_import_records(ConvArgs a) {
   const int gx = blockIdx.x * blockDim.x + threadIdx.x;
-  const int gy = blockIdx.y * blockDim.y + threadIdx.y;
-  if (gx >= a.Nx || gy >= a.Ny) return;
+  const int gy = a.y0 + int(blockIdx.y * blockDim.y + threadIdx.y);
+  if (gx >= a.Nx || gy >= (a.y1 > 0 ? a.y1 : a.Ny)) return;
   const size_t i64 = size_t(gy + 1) * a.pitch64 + gx + 1;
   const size_t r = size_t(gy) * a.pitch32 + gx;
   float hi[4], c[4];
 #pragma unroll
-  for (int k = 0; k < 4; k++) {
-    const double v = a.f64[k][i64];
-    hi[k] = float(v);
-    c[k] = float(double(hi[k]) - v);  // value = hi - c
-  }
+  for (int k = 0; k < 4; k++) split_f64(a.f64[k][i64], hi[k], c[k]);  // value = hi - c
   reinterpret_cast<float4*>(a.A)[r] = make_float4(hi[0], hi[1], hi[2], hi[3]);
   if (a.pack)
     static_cast<uint2*>(a.B)[r] = cq_pack(c[0], c[1], c[2], c[3]);
@@ -326,8 +322,8 @@ __global__ void k_import_records(ConvArgs a) {
 
 __global__ void k_export_records(ConvArgs a) {
   const int gx = blockIdx.x * blockDim.x + threadIdx.x;
-  const int gy = blockIdx.y * blockDim.y + threadIdx.y;
-  if (gx >= a.Nx || gy >= a.Ny) return;
+  const int gy = a.y0 + int(blockIdx.y * blockDim.y + threadIdx.y);
+  if (gx >= a.Nx || gy >= (a.y1 > 0 ? a.y1 : a.Ny)) return;
   const size_t r = size_t(gy) * a.pitch32 + gx;
   const float4 v = reinterpret_cast<const float4*>(a.A)[r];
   const float4 c = a.pack ? cq_unpack(static_cast<const uint2*>(a.B)[r])
@@ -429,15 +425,19 @@ int batch_warps_per_cta() { return kWarps; }
 int batch_strip_cols() { return kCols; }
 
 cudaError_t launch_import_f32(const ConvArgs& a, cudaStream_t s) {
+  const int rows = (a.y1 > 0 ? a.y1 : a.Ny) - a.y0;
+  if (rows <= 0) return cudaSuccess;
   dim3 block(32, 8);
-  dim3 grid((a.Nx + 31) / 32, (a.Ny + 7) / 8);
+  dim3 grid((a.Nx + 31) / 32, (rows + 7) / 8);
   k_import_records<<<grid, block, 0, s>>>(a);
   return cudaGetLastError();
 }
 
 cudaError_t launch_export_f32(const ConvArgs& a, cudaStream_t s) {
+  const int rows = (a.y1 > 0 ? a.y1 : a.Ny) - a.y0;
+  if (rows <= 0) return cudaSuccess;
   dim3 block(32, 8);
-  dim3 grid((a.Nx + 31) / 32, (a.Ny + 7) / 8);
+  dim3 grid((a.Nx + 31) / 32, (rows + 7) / 8);
   k_export_records<<<grid, block, 0, s>>>(a);
   return cudaGetLastError();
 }

@@ -252,9 +252,7 @@ __global__ void k_import3d(Conv3DArgs a) {
     float hi[4], c[4];
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-      const double v = a.f64[k][i64];
-      hi[k] = float(v);
-      c[k] = float(double(hi[k]) - v);  // value = hi - c
+      split_f64(a.f64[k][i64], hi[k], c[k]);  // value = hi - c
     }
     reinterpret_cast<float4*>(a.A)[r] = make_float4(hi[0], hi[1], hi[2], hi[3]);
     static_cast<uint2*>(a.B)[r] = cq_pack(c[0], c[1], c[2], c[3]);

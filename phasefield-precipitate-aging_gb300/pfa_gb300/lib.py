@@ -171,6 +171,7 @@ def load():
         "pfa_batch_stream": (ctypes.c_void_p, [ctypes.c_void_p]),
         "pfa_batch_destroy": (_i, [ctypes.c_void_p]),
         "pfa_ic_generate": (_i, [ctypes.POINTER(IcRecipe)] + [ctypes.c_void_p] * 5),
+        "pfa_split_block": (_i, [_dp, _fp, _fp, _i]),
         "pfa_batch_add_ic": (_i, [ctypes.c_void_p, ctypes.POINTER(IcRecipe), ctypes.POINTER(_i)]),
         "pfa3d_create_ic": (_i, [ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(IcRecipe), _dp,
                                  _dp, _i]),
@@ -441,8 +442,8 @@ class Grid3D:
             check(self.L.pfa_last_error(), "events")
         return [(cells[k], ph[k]) for k in range(min(n, cap))]
 
-    def read(self):
-        out = [np.empty(self.shape) for _ in range(4)]
+    def read(self, out=None):
+        out = out or [np.empty(self.shape) for _ in range(4)]
         check(self.L.pfa3d_read(self.h, *[_ptr(a) for a in out]), "pfa3d_read")
         return out
 
@@ -584,6 +585,16 @@ def philox_device(ctr, key):
     check(load().pfa_philox_block(ctr.ctypes.data_as(u32p), int(key), out.ctypes.data_as(u32p), n),
           "pfa_philox_block")
     return out
+
+
+def split_device(v):
+    """The FP32 form's split (hi, c) of an array of doubles on the device."""
+    v = np.ascontiguousarray(v, dtype=np.float64).ravel()
+    hi = np.zeros(v.size, dtype=np.float32)
+    c = np.zeros(v.size, dtype=np.float32)
+    check(load().pfa_split_block(_ptr(v), hi.ctypes.data_as(_fp), c.ctypes.data_as(_fp), v.size),
+          "pfa_split_block")
+    return hi, c
 
 
 def fast_coef():
