@@ -362,13 +362,21 @@ __device__ void paint(const NucArgs& a, const NucEvent& e, int ph) {
   constexpr double xgCr = kXe[0][0], xgNb = kXe[0][1];
   constexpr double xdCr = kXe[1][0], xdNb = kXe[1][1], xlCr = kXe[2][0], xlNb = kXe[2][1];
   const double parCr = ph == 0 ? xdCr : xlCr, parNb = ph == 0 ? xdNb : xlNb;
-  const double RdCr = R * sqrt((parCr - e.xcr) / (e.xcr - xgCr));
-  const double RdNb = R * sqrt((parNb - e.xnb) / (e.xnb - xgNb));
   const int lo = int(-R);
   int hi = lo;
   while (double(hi) < R) hi++;  // loop bound of `for (i = -R; i < R; i++)`
   const int w = hi - lo;
-  if (w <= 0) return;
+  if (w <= 0) return;  // (uniform over the block: every thread paints the same event)
+  // depletion radii: one thread evaluates them (an FP64 divide and square
+  // root per thread of the block would cost ~50 us per event on this part's
+  // FP64 unit) and shares them
+  __shared__ double s_rd[2];
+  if (threadIdx.x == 0) {
+    s_rd[0] = R * sqrt((parCr - e.xcr) / (e.xcr - xgCr));
+    s_rd[1] = R * sqrt((parNb - e.xnb) / (e.xnb - xgNb));
+  }
+  __syncthreads();
+  const double RdCr = s_rd[0], RdNb = s_rd[1];
   if (a.is3d) {
     // spheres (no counterpart in the reference): offsets that leave the
     // array along any axis are skipped
