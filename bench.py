@@ -374,7 +374,7 @@ def bench_grid3d(args, ws, rank, local, barrier, max_over_ranks, pl, ic):
                            "speedup_fp32_over_fp64": value / ws / (cells / (ms64 / 1e3))},
                      roofline={"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                                "frac": achieved / peak, "traffic": profiled_traffic("step3d_f32_512"),
-                               "kernel": "k_stream3d", "bytes_per_cell": 48, "kernel_ms": kms,
+                               "kernel": "k_stream3d_f32", "bytes_per_cell": 48, "kernel_ms": kms,
                                "peak_kind": peak_kind},
                      cpu_baseline=None,
                      gpu_launches=args.steps * (STEPS_PER_BENCH_STEP + NUC_LAUNCHES),
