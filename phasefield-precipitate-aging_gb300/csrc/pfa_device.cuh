@@ -106,19 +106,40 @@ constexpr float kCqP = 549755813888.0f;   // 2^39
 constexpr float kCqXi = 1.0f / 1099511627776.0f;
 constexpr float kCqPi = 1.0f / 549755813888.0f;
 
-__device__ __forceinline__ float4 cq_unpack(uint2 w) {
-  const int a = int(w.x), b = int(w.y);
-  return make_float4(float((a << 16) >> 16) * kCqXi, float(a >> 16) * kCqXi,
-                     float((b << 16) >> 16) * kCqPi, float(b >> 16) * kCqPi);
+// Two counts (values already scaled) as the 16-bit halves of one word: cvt's
+// float-to-integer conversion rounds to nearest even and saturates to
+// [-32768, 32767] in one instruction per half.
+__device__ __forceinline__ unsigned cq_pair(float lo, float hi) {
+  unsigned r;
+  asm("{\n\t.reg .s16 l, h;\n\tcvt.rni.s16.f32 l, %1;\n\tcvt.rni.s16.f32 h, %2;\n\t"
+      "mov.b32 %0, {l, h};\n\t}"
+      : "=r"(r)
+      : "f"(lo), "f"(hi));
+  return r;
 }
 
+// the two signed 16-bit halves of a word as FP32 (exact)
+__device__ __forceinline__ float2 cq_halves(unsigned w) {
+  float2 f;
+  asm("{\n\t.reg .s16 l, h;\n\tmov.b32 {l, h}, %2;\n\tcvt.rn.f32.s16 %0, l;\n\t"
+      "cvt.rn.f32.s16 %1, h;\n\t}"
+      : "=f"(f.x), "=f"(f.y)
+      : "r"(w));
+  return f;
+}
+
+__device__ __forceinline__ float4 cq_unpack(uint2 w) {
+  const float2 a = cq_halves(w.x), b = cq_halves(w.y);
+  return make_float4(a.x * kCqXi, a.y * kCqXi, b.x * kCqPi, b.y * kCqPi);
+}
+
+// one compensation as its 16-bit count (the halves cq_pair writes)
 __device__ __forceinline__ unsigned cq_count(float c, float scale) {
-  return unsigned(max(-32767, min(32767, __float2int_rn(c * scale)))) & 0xffffu;
+  return cq_pair(c * scale, 0.0f) & 0xffffu;
 }
 
 __device__ __forceinline__ uint2 cq_pack(float cx, float cy, float cd, float cl) {
-  return make_uint2(cq_count(cx, kCqX) | (cq_count(cy, kCqX) << 16),
-                    cq_count(cd, kCqP) | (cq_count(cl, kCqP) << 16));
+  return make_uint2(cq_pair(cx * kCqX, cy * kCqX), cq_pair(cd * kCqP, cl * kCqP));
 }
 
 // 1 - p(x) = p(1 - x): the gamma fraction without cancellation near a pure

@@ -89,10 +89,12 @@ __device__ __forceinline__ float4 comps(const CompT<PACK>& c) {
 // the composition compensations only (what the gamma solve needs)
 template <bool PACK>
 __device__ __forceinline__ float2 comps_x(const CompT<PACK>& c) {
-  if constexpr (PACK)
-    return make_float2(float((int(c.x) << 16) >> 16) * kCqXi, float(int(c.x) >> 16) * kCqXi);
-  else
+  if constexpr (PACK) {
+    const float2 h = cq_halves(c.x);
+    return make_float2(h.x * kCqXi, h.y * kCqXi);
+  } else {
     return make_float2(c.x, c.y);
+  }
 }
 
 template <bool PACK>

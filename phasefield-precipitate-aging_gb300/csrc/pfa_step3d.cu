@@ -107,8 +107,8 @@ struct S3 {
       poly64(pD, pG, pL, m);
       return Nb3<R>{fict64<0, 0>(r.x, r.y, m), fict64<0, 1>(r.x, r.y, m), r.pd, r.pl};
     } else {
-      const float cx = float((int(r.cq.x) << 16) >> 16) * kCqXi;
-      const float cy = float(int(r.cq.x) >> 16) * kCqXi;
+      const float2 h = cq_halves(r.cq.x);
+      const float cx = h.x * kCqXi, cy = h.y * kCqXi;
       Nb3<R> n;
       n.pd = r.pd;
       n.pl = r.pl;
