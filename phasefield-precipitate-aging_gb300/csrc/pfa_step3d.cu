@@ -15,9 +15,11 @@
 // from planes published in shared memory, z-neighbours from a register
 // window of solved planes.  F64 (k_stream3d<true>): a three-plane window
 // rotated by a 3x-unrolled loop, one barrier per plane.  F32
-// (k_stream3d_f32): records staged through a four-plane cp.async ring, a
-// four-plane window, two planes per barrier (512^3: 1.380 ms against 1.420 ms
-// with the F64 kernel's scheme; wider CTAs of 20 warps: 1.510 ms).
+// (k_stream3d_f32): records staged through a four-plane cp.async ring (read
+// once each: the record a plane's solve reads is kept for its update), a
+// four-plane window of solved planes, two planes per barrier (512^3: 1.29 ms
+// against 1.42 ms with the F64 kernel's scheme; wider CTAs of 20 warps were
+// slower).
 #include <cstdint>
 #include <type_traits>
 
@@ -257,7 +259,8 @@ __global__ void __launch_bounds__(32 * kW) k_stream3d(Step3DArgs a) {
 // (each thread copies and reads back only its own column), so the window of
 // four solved planes fits the register budget; each iteration solves planes
 // z+1 and z+2, publishes z and z+1 for the neighbouring warps and passes one
-// barrier for both updates.
+// barrier for both updates.  A plane's record is read from the ring once, for
+// its solve, and kept in registers until its update.
 constexpr int kRing3 = 4;  // planes in the ring (a power of two)
 struct Smem3 {
   float4 ra[kRing3][32 * kW];
@@ -309,14 +312,17 @@ __global__ void __launch_bounds__(32 * kW) k_stream3d_f32(Step3DArgs a) {
   };
   for (int k = -1; k <= 2; k++) issue(z0 + k);
   cp_wait<2>();  // planes z0-1 and z0
-  Nb3<float> nA = S.solve(fetch(z0 - 1)), nB = S.solve(fetch(z0)), nC, nD;
+  Raw3<float> rB = fetch(z0), rC, rD;  // raw records kept for the updates
+  Nb3<float> nA = S.solve(fetch(z0 - 1)), nB = S.solve(rB), nC, nD;
   int z = z0, it = 0;
   // issued up to plane z+2 at the top of every iteration
   for (; z + 1 < z1; z += 2, it ^= 1) {
     issue(z + 3);  // into the slot of plane z-1
     cp_wait<1>();  // planes up to z+2 have landed
-    nC = S.solve(fetch(z + 1));
-    nD = S.solve(fetch(z + 2));
+    rC = fetch(z + 1);
+    rD = fetch(z + 2);
+    nC = S.solve(rC);
+    nD = S.solve(rD);
     Nb3<float>(*b0)[32] = sm.sh[2 * it];
     Nb3<float>(*b1)[32] = sm.sh[2 * it + 1];
     b0[w][lane] = nB;
@@ -324,11 +330,12 @@ __global__ void __launch_bounds__(32 * kW) k_stream3d_f32(Step3DArgs a) {
     // the slots of this parity were last read two iterations ago, before the
     // previous iteration's barrier
     __syncthreads();
-    S.update_from(z, nA, nB, nC, fetch(z), b0);
-    issue(z + 4);  // into the slot of plane z, read just now
-    S.update_from(z + 1, nB, nC, nD, fetch(z + 1), b1);
+    issue(z + 4);  // into the slot of plane z (its record is held in rB)
+    S.update_from(z, nA, nB, nC, rB, b0);
+    S.update_from(z + 1, nB, nC, nD, rC, b1);
     nA = nC;
     nB = nD;
+    rB = rD;
   }
   if (z < z1) {  // one plane left
     issue(z + 3);
@@ -337,7 +344,7 @@ __global__ void __launch_bounds__(32 * kW) k_stream3d_f32(Step3DArgs a) {
     Nb3<float>(*b0)[32] = sm.sh[2 * it];
     b0[w][lane] = nB;
     __syncthreads();
-    S.update_from(z, nA, nB, nC, fetch(z), b0);
+    S.update_from(z, nA, nB, nC, rB, b0);
   }
   cp_wait<0>();  // no copy into shared memory outlives the block
 }
