@@ -633,7 +633,9 @@ static int read_core(CudaData* dev, double* cr, double* nb, double* pd, double* 
   const double* src[4] = {dev->conc_Cr_old, dev->conc_Nb_old, dev->phi_del_old, dev->phi_lav_old};
   if (s->precision != PFA_FP64 && s->f32_live && dev->str_B) {
     if (int r = ensure_xfer(s)) return r;
-    const int rows = (ny + kXferBands - 1) / kXferBands;
+    // at least two rows per band: the first band then holds the bottom ghost
+    // row together with the interior row that writes it
+    const int rows = std::max(2, (ny + kXferBands - 1) / kXferBands);
     for (int i = 0; i < kXferBands; i++) {
       const int r0 = i * rows, r1 = r0 + rows < ny ? r0 + rows : ny;
       if (r0 >= r1) break;

@@ -72,6 +72,28 @@ def test_fp64_config1_1000_steps(pfa, orc):
     grid.close()
 
 
+@pytest.mark.parametrize("precision", ["fp32", "fp32k"])
+@pytest.mark.parametrize("shape", [(1, 1), (2, 5), (3, 4), (5, 7), (7, 30), (9, 13), (17, 33),
+                                   (100, 3)])
+def test_fp32_odd_sizes_match_oracle(pfa, orc, shape, precision):
+    """The FP32 form on odd and tiny sizes (partial strips, short segments,
+    read-out bands of one or two rows): within the stated bound of the oracle,
+    with the ghost ring the mirror of the interior."""
+    from pfa_gb300 import ic
+    ny, nx = shape
+    f = ic.grid2d(nx, ny, seed=nx * 31 + ny, stripe_width=max(1, nx // 3),
+                  n_particles=1 if min(nx, ny) > 12 else 0, radius=3.0)
+    want = orc.run2d(f, O.model_params(), 40)
+    grid = pfa.Grid2D(f, _params(pfa), precision=precision)
+    grid.run(40)
+    got = grid.read()
+    grid.close()
+    for a, b in zip(got, want):
+        assert np.max(np.abs(a[1:-1, 1:-1] - b[1:-1, 1:-1])) <= FP32_TOL
+        assert np.array_equal(a[0, :], a[1, :]) and np.array_equal(a[-1, :], a[-2, :])
+        assert np.array_equal(a[:, 0], a[:, 1]) and np.array_equal(a[:, -1], a[:, -2])
+
+
 def test_halo_mirrors_interior(pfa):
     from pfa_gb300 import ic
     f = ic.grid2d(40, 30, seed=5, stripe_width=8, n_particles=2, radius=4.0)
