@@ -51,6 +51,23 @@ def test_generate_into_device_arrays(pfa, dims):
         _compare(got, want, rec)
 
 
+@pytest.mark.parametrize("dims", [(1, 1, 0), (3, 2, 0), (1, 7, 0), (2, 1, 3), (1, 1, 2)])
+def test_generate_tiny_grids(pfa, dims):
+    """One-cell-wide grids: every interior cell writes several ghost cells."""
+    import torch
+    import oracle as O
+    nx, ny, nz = dims
+    rec = {"nx": nx, "ny": ny, "nz": nz, "matrix": (0.30, 0.02), "enrich": (0.27, 0.17),
+           "noise": 0.002, "seed": 77, "bands": [(0, 1)],
+           "particles": [(0.2, 0.4, 0.3, 1.5, 1)], "dx": 5e-9, "width": 10e-9}
+    want = O.ic_fields(rec)
+    dev = [torch.full(want[0].shape, -1.0, dtype=torch.float64, device="cuda") for _ in range(4)]
+    pfa.ic_generate(rec, [t.data_ptr() for t in dev])
+    torch.cuda.synchronize()
+    for g, w in zip([t.cpu().numpy() for t in dev], want):
+        assert np.max(np.abs(g - w)) <= TANH_TOL
+
+
 def test_batch_slot_from_recipe(pfa):
     import oracle as O
     recs = [ic.recipe2d(n, m, seed=20 + n, stripe_width=8, n_particles=3, radius=4.0)
