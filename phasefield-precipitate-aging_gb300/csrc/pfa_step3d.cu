@@ -212,7 +212,7 @@ struct S3 {
       const float dFl = fmaf(-a.kap[1], lapL, dF_local32(pl, pd, quad2(K.dP[1], u1, u2), a.om2[1], a.alpha2));
       const float yd = fmaf(-a.dtL[0], dFd, -cc.z), td = pd + yd;
       const float yl = fmaf(-a.dtL[1], dFl, -cc.w), tl = pl + yl;
-      const long long i = cell(z);
+      const long long i = z * plane + col;  // z is an interior plane here
       static_cast<float4*>(a.out[0])[i] = make_float4(tcr, tnb, td, tl);
       static_cast<uint2*>(a.out[1])[i] =
           cq_pack((tcr - X) - ycr, (tnb - Y) - ynb, (td - pd) - yd, (tl - pl) - yl);
