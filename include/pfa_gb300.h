@@ -195,6 +195,14 @@ int pfa_batch_destroy(void* handle);
  *            / (width / 2)), x = p(phi) xe_phase + (1 - p(phi)) x, phi_phase =
  *            max(phi_phase, phi) (r: distance to the centre, in cells);
  *   ghost ring = the zero-flux mirror of the interior.
+ * profile 1 replaces matrix_k by init_gaussian_enrichment's bell curve
+ * along x (src/alloy625.cpp:210-259, bell_curve of thermo/enrichment.py):
+ *   A_k (exp(-(pos / sigma_k)^2 / 2) - 1) + enrich_k, clamped to [0, 1],
+ *   pos = dx (x - bell_x0), A_k such that the mean of the unclamped curve
+ *   over bell_range [a, b] (m) is matrix_k (noise and bands still apply).
+ * particle_mode 1 embeds like embed_OPC (src/alloy625.cpp:262-294): every
+ * cell with |q - floor(c_q)| <= int(R + 4 width / dx) on each axis takes the
+ * blend and phi_phase = phi (overwritten), in particle order.
  * nz <= 1 makes a 2D grid (centre[k][2] ignored). */
 #define PFA_IC_MAX_BANDS 16
 #define PFA_IC_MAX_PARTICLES 64
@@ -212,6 +220,11 @@ typedef struct pfa_ic_recipe {
 	int phase[PFA_IC_MAX_PARTICLES];           /* 0 delta, 1 laves */
 	double dx;                 /* spacing of the tanh profile (m) */
 	double width;              /* interface width 2 lambda (m) */
+	int profile;               /* 0: matrix + noise + bands; 1: bell curve along x */
+	double bell_sigma[2];      /* profile 1: Gaussian widths (m) for x_Cr, x_Nb */
+	double bell_range[2];      /* profile 1: [a, b] (m) holding the mean */
+	double bell_x0;            /* profile 1: the column (cells) at position 0 */
+	int particle_mode;         /* 0: blend, phase = max; 1: embed_OPC's box, phase set */
 } pfa_ic_recipe;
 
 /* writes the recipe's four fields into caller-owned device arrays in the

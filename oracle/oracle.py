@@ -252,7 +252,8 @@ class OrcIcRecipe(ctypes.Structure):
                 ("n_bands", _i), ("band", (_i * 2) * 16),
                 ("n_particles", _i), ("centre", (_d * 3) * 64),
                 ("radius", _d * 64), ("phase", _i * 64),
-                ("dx", _d), ("width", _d)]
+                ("dx", _d), ("width", _d), ("profile", _i), ("bell_sigma", _d * 2),
+                ("bell_range", _d * 2), ("bell_x0", _d), ("particle_mode", _i)]
 
 
 def ic_fields(rec, lib=None):
@@ -274,6 +275,11 @@ def ic_fields(rec, lib=None):
         r.centre[k][0], r.centre[k][1], r.centre[k][2] = x, y, z
         r.radius[k], r.phase[k] = rad, int(ph)
     r.dx, r.width = rec["dx"], rec["width"]
+    r.profile = int(rec.get("profile", 0))
+    r.bell_sigma[:] = rec.get("bell_sigma", (0.0, 0.0))
+    r.bell_range[:] = rec.get("bell_range", (0.0, 0.0))
+    r.bell_x0 = rec.get("bell_x0", 0.0)
+    r.particle_mode = int(rec.get("particle_mode", 0))
     shape = ((r.nz + 2, r.ny + 2, r.nx + 2) if r.nz > 1 else (r.ny + 2, r.nx + 2))
     out = [np.zeros(shape) for _ in range(4)]
     f = lib.lib.orc_ic_fields

@@ -381,6 +381,14 @@ double orc_u53(uint32_t hi, uint32_t lo)
  *   blended as embed_OPC does (src/alloy625.cpp:283-292):
  *   x = p(phi) xe + (1 - p(phi)) x; the particle's phase takes max(phi_old, phi).
  * Plain FP64 with no contraction (this file is built with -ffp-contract=off). */
+/* bell_curve of thermo/enrichment.py: A (exp(-x^2/(2 s^2)) - 1) + xe with
+ * A set so that the mean over [a, b] is x0 */
+static double ic_bell_amplitude(double s, double a, double b, double x0, double xe)
+{
+	const double I = s * sqrt(M_PI / 2.0) * (erf(b / (s * sqrt(2.0))) - erf(a / (s * sqrt(2.0))));
+	return (x0 - xe) / (I / (b - a) - 1.0);
+}
+
 static double ic_p(double x)
 {
 	const double x2 = x * x, x3 = x2 * x;
@@ -396,6 +404,11 @@ void orc_ic_fields(const orc_ic_recipe* r, double* f[4])
 	                         {0.37392129441013022, 0.25826261799015571}};
 	const double half_w = 0.5 * r->width;
 	const uint32_t key[2] = {(uint32_t)r->seed, (uint32_t)(r->seed >> 32)};
+	double bellA[2] = {0.0, 0.0};
+	if (r->profile == 1)
+		for (int k = 0; k < 2; k++)
+			bellA[k] = ic_bell_amplitude(r->bell_sigma[k], r->bell_range[0], r->bell_range[1],
+			                             r->matrix[k], r->enrich[k]);
 	for (int z = 0; z < nz; z++)
 		for (int y = 0; y < r->ny; y++)
 			for (int x = 0; x < r->nx; x++) {
@@ -403,8 +416,18 @@ void orc_ic_fields(const orc_ic_recipe* r, double* f[4])
 				const uint32_t ctr[4] = {(uint32_t)c, (uint32_t)(c >> 32), 0u, 0x49430000u};
 				uint32_t w[4];
 				orc_philox4x32_10(ctr, key, w);
-				double xcr = r->matrix[0] + r->noise * (2.0 * orc_u53(w[0], w[1]) - 1.0);
-				double xnb = r->matrix[1] + r->noise * (2.0 * orc_u53(w[2], w[3]) - 1.0);
+				double base[2] = {r->matrix[0], r->matrix[1]};
+				if (r->profile == 1) {
+					/* init_gaussian_enrichment, src/alloy625.cpp:240-255 */
+					const double pos = r->dx * ((double)x - r->bell_x0);
+					for (int k = 0; k < 2; k++) {
+						const double t = pos / r->bell_sigma[k];
+						const double v = bellA[k] * (exp(-0.5 * (t * t)) - 1.0) + r->enrich[k];
+						base[k] = fmin(1.0, fmax(0.0, v));
+					}
+				}
+				double xcr = base[0] + r->noise * (2.0 * orc_u53(w[0], w[1]) - 1.0);
+				double xnb = base[1] + r->noise * (2.0 * orc_u53(w[2], w[3]) - 1.0);
 				const double dcr = r->enrich[0] - r->matrix[0], dnb = r->enrich[1] - r->matrix[1];
 				for (int b = 0; b < r->n_bands; b++)
 					if (x >= r->band[b][0] && x < r->band[b][1]) {
@@ -415,7 +438,9 @@ void orc_ic_fields(const orc_ic_recipe* r, double* f[4])
 				const int q[3] = {x, y, z};
 				for (int k = 0; k < r->n_particles; k++) {
 					const double R = r->radius[k];
-					const int pad = (int)ceil(R + 6.0 * half_w / r->dx) + 1;
+					/* embed_OPC's box: R + 4 w / dx, truncated (src/alloy625.cpp:275-276) */
+					const int pad = r->particle_mode == 1 ? (int)(R + 4.0 * r->width / r->dx)
+					                                      : (int)ceil(R + 6.0 * half_w / r->dx) + 1;
 					int in = 1;
 					double r2 = 0.0;
 					for (int d = 0; d < (is3d ? 3 : 2); d++) {
@@ -430,7 +455,7 @@ void orc_ic_fields(const orc_ic_recipe* r, double* f[4])
 					const int ph_k = r->phase[k] == 0 ? 0 : 1;
 					xcr = pp * xe[ph_k][0] + qq * xcr;
 					xnb = pp * xe[ph_k][1] + qq * xnb;
-					if (phi > ph[ph_k]) ph[ph_k] = phi;
+					if (r->particle_mode == 1 || phi > ph[ph_k]) ph[ph_k] = phi;
 				}
 				const double v[4] = {xcr, xnb, ph[0], ph[1]};
 				for (int k = 0; k < 4; k++) {

@@ -123,6 +123,9 @@ typedef struct {
 	double radius[ORC_IC_MAX_PARTICLES];
 	int phase[ORC_IC_MAX_PARTICLES];
 	double dx, width;
+	int profile;               /* 1: init_gaussian_enrichment's bell curve along x */
+	double bell_sigma[2], bell_range[2], bell_x0;
+	int particle_mode;         /* 1: embed_OPC's square box, phase overwritten */
 } orc_ic_recipe;
 /* fields in the ghost-ring layout ((ny+2) x (nx+2), or (nz+2) x (ny+2) x (nx+2)
  * when nz > 1), ghost ring = the mirror of the interior */

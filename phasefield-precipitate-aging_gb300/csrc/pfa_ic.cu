@@ -64,6 +64,7 @@ __device__ void store_mirrored(double* f, const pfa_ic_recipe& r, bool is3d, int
 
 struct IcOut {
   double* f[4];
+  double bellA[2];  // profile 1: the amplitudes that give the curve its mean
 };
 
 __global__ void __launch_bounds__(256) k_ic_fill(pfa_ic_recipe r, IcOut o, int is3d) {
@@ -76,9 +77,18 @@ __global__ void __launch_bounds__(256) k_ic_fill(pfa_ic_recipe r, IcOut o, int i
   const uint4 w = philox4x32_10(
       make_uint4(uint32_t(cell), uint32_t(cell >> 32), 0u, kIcStream),
       make_uint2(uint32_t(r.seed), uint32_t(r.seed >> 32)));
+  double base[2] = {r.matrix[0], r.matrix[1]};
+  if (r.profile == 1) {
+    const double pos = mul(r.dx, sub(double(x), r.bell_x0));
+    for (int k = 0; k < 2; k++) {
+      const double t = pos / r.bell_sigma[k];
+      const double v = add(mul(o.bellA[k], sub(exp(mul(-0.5, mul(t, t))), 1.0)), r.enrich[k]);
+      base[k] = fmin(1.0, fmax(0.0, v));
+    }
+  }
   // 2u - 1 is exact for u on the 2^-53 grid
-  double xcr = add(r.matrix[0], mul(r.noise, sub(mul(2.0, u53(w.x, w.y)), 1.0)));
-  double xnb = add(r.matrix[1], mul(r.noise, sub(mul(2.0, u53(w.z, w.w)), 1.0)));
+  double xcr = add(base[0], mul(r.noise, sub(mul(2.0, u53(w.x, w.y)), 1.0)));
+  double xnb = add(base[1], mul(r.noise, sub(mul(2.0, u53(w.z, w.w)), 1.0)));
   const double dcr = sub(r.enrich[0], r.matrix[0]), dnb = sub(r.enrich[1], r.matrix[1]);
   for (int b = 0; b < r.n_bands; b++)
     if (x >= r.band[b][0] && x < r.band[b][1]) {
@@ -91,7 +101,8 @@ __global__ void __launch_bounds__(256) k_ic_fill(pfa_ic_recipe r, IcOut o, int i
   const int dims = is3d ? 3 : 2;
   for (int k = 0; k < r.n_particles; k++) {
     const double R = r.radius[k];
-    const int pad = int(ceil(R + 6.0 * half_w / r.dx)) + 1;
+    const int pad = r.particle_mode == 1 ? int(R + 4.0 * r.width / r.dx)
+                                         : int(ceil(R + 6.0 * half_w / r.dx)) + 1;
     bool in = true;
     double r2 = 0.0;
     for (int d = 0; d < dims; d++) {
@@ -112,7 +123,7 @@ __global__ void __launch_bounds__(256) k_ic_fill(pfa_ic_recipe r, IcOut o, int i
     const double xe_cr = phase == 0 ? xdCr : xlCr, xe_nb = phase == 0 ? xdNb : xlNb;
     xcr = add(mul(pp, xe_cr), mul(q, xcr));
     xnb = add(mul(pp, xe_nb), mul(q, xnb));
-    ph[phase] = fmax(ph[phase], phi);
+    ph[phase] = r.particle_mode == 1 ? phi : fmax(ph[phase], phi);
   }
   const double v[4] = {xcr, xnb, ph[0], ph[1]};
   for (int f = 0; f < 4; f++) store_mirrored(o.f[f], r, is3d, x, y, z, v[f]);
@@ -138,15 +149,39 @@ const char* ic_check(const pfa_ic_recipe* r) {
       if (!std::isfinite(r->centre[k][d]) || std::fabs(r->centre[k][d]) > 1e9)
         return "initial condition: particle centre not finite";
   }
-  // the box pad (radius + three widths) stays an int
-  if (r->n_particles > 0 && !(3.0 * r->width / r->dx < 1e6))
+  // the box pad (radius + three or four widths) stays an int
+  if (r->n_particles > 0 && !(4.0 * r->width / r->dx < 1e6))
     return "initial condition: interface width above 1e6 cells";
+  if (r->profile != 0 && r->profile != 1) return "initial condition: profile must be 0 or 1";
+  if (r->particle_mode != 0 && r->particle_mode != 1)
+    return "initial condition: particle_mode must be 0 or 1";
+  if (r->profile == 1) {
+    for (int k = 0; k < 2; k++)
+      if (!(r->bell_sigma[k] > 0) || !std::isfinite(r->bell_sigma[k]))
+        return "initial condition: bell widths must be finite and > 0";
+    if (!(r->bell_range[1] > r->bell_range[0]) || !std::isfinite(r->bell_range[0]) ||
+        !std::isfinite(r->bell_range[1]) || !std::isfinite(r->bell_x0))
+      return "initial condition: bell range must be finite with a < b";
+  }
   return nullptr;
+}
+
+// amplitude of the bell curve whose mean over [a, b] is x0 (thermo/enrichment.py:
+// mean of A (exp(-x^2/(2 s^2)) - 1) + xe over [a, b] = A (I / (b - a) - 1) + xe,
+// I = s sqrt(pi/2) (erf(b / (s sqrt 2)) - erf(a / (s sqrt 2))))
+double ic_bell_amplitude(double sigma, double a, double b, double x0, double xe) {
+  const double I = sigma * std::sqrt(M_PI / 2.0) *
+                   (std::erf(b / (sigma * std::sqrt(2.0))) - std::erf(a / (sigma * std::sqrt(2.0))));
+  return (x0 - xe) / (I / (b - a) - 1.0);
 }
 
 cudaError_t launch_ic_fill(const pfa_ic_recipe& r, double* const f[4], cudaStream_t s) {
   const bool is3d = r.nz > 1;
-  IcOut o{{f[0], f[1], f[2], f[3]}};
+  IcOut o{{f[0], f[1], f[2], f[3]}, {0.0, 0.0}};
+  if (r.profile == 1)
+    for (int k = 0; k < 2; k++)
+      o.bellA[k] = ic_bell_amplitude(r.bell_sigma[k], r.bell_range[0], r.bell_range[1],
+                                     r.matrix[k], r.enrich[k]);
   dim3 grid((r.nx + 31) / 32, (r.ny + 7) / 8, is3d ? r.nz : 1);
   k_ic_fill<<<grid, 256, 0, s>>>(r, o, is3d ? 1 : 0);
   return cudaGetLastError();

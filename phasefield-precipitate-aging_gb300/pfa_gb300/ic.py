@@ -201,6 +201,29 @@ def recipe3d(nx, ny, nz, seed, matrix=MATRIX, enrich=ENRICH, noise=0.002, slab=6
             "particles": parts, "dx": dx, "width": width}
 
 
+def reference_recipe2d(nx, ny, seed, radius=8.0, matrix=None, enrich=None, dx=5e-9,
+                       width=10e-9):
+    """The reference's default 2D initial condition as a recipe
+    (src/alloy625.cpp:520-600): matrix and enrichment compositions drawn from
+    the alloy ranges (here with numpy's generator, seeded), the bell-curve
+    enrichment of init_gaussian_enrichment along x (widths bell = 150, 50 nm,
+    src/parameters.h:32; mean over the middle two thirds = the matrix), no
+    noise, and one delta seed embedded at the centre with embed_OPC's box and
+    overwrite (seed_solitaire_delta).  The reference sizes the seed from the
+    critical radius (2 x R* / dx) and blends toward the curvature-shifted
+    delta composition; here the radius in cells is an argument and the blend
+    goes to the flat equilibrium composition (as seed_pair's does)."""
+    rng = np.random.default_rng(seed)
+    m = matrix or (rng.uniform(*MATRIX_RANGE[0]), rng.uniform(*MATRIX_RANGE[1]))
+    e = enrich or (rng.uniform(*ENRICH_RANGE[0]), rng.uniform(*ENRICH_RANGE[1]))
+    return {"nx": nx, "ny": ny, "nz": 0, "matrix": tuple(m), "enrich": tuple(e), "noise": 0.0,
+            "seed": int(seed), "bands": [], "dx": dx, "width": width,
+            "particles": [(float(nx // 2), float(ny // 2), 0.0, float(radius), 0)],
+            "profile": 1, "bell_sigma": (150e-9, 50e-9),
+            "bell_range": (-nx * dx / 3.0, nx * dx / 3.0), "bell_x0": float(nx // 2),
+            "particle_mode": 1}
+
+
 # request sizes of the serving workload: (dimension, side)
 SERVE_SIZES = ((2, 256), (2, 1024), (2, 4096), (3, 128), (3, 256))
 

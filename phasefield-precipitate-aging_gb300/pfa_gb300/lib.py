@@ -45,7 +45,8 @@ class IcRecipe(ctypes.Structure):
                 ("n_bands", _i), ("band", (_i * 2) * IC_MAX_BANDS),
                 ("n_particles", _i), ("centre", (_d * 3) * IC_MAX_PARTICLES),
                 ("radius", _d * IC_MAX_PARTICLES), ("phase", _i * IC_MAX_PARTICLES),
-                ("dx", _d), ("width", _d)]
+                ("dx", _d), ("width", _d), ("profile", _i), ("bell_sigma", _d * 2),
+                ("bell_range", _d * 2), ("bell_x0", _d), ("particle_mode", _i)]
 
 
 def ic_recipe(rec):
@@ -70,6 +71,11 @@ def ic_recipe(rec):
         r.radius[k] = rad
         r.phase[k] = int(ph)
     r.dx, r.width = rec["dx"], rec["width"]
+    r.profile = int(rec.get("profile", 0))
+    r.bell_sigma[:] = rec.get("bell_sigma", (0.0, 0.0))
+    r.bell_range[:] = rec.get("bell_range", (0.0, 0.0))
+    r.bell_x0 = rec.get("bell_x0", 0.0)
+    r.particle_mode = int(rec.get("particle_mode", 0))
     return r
 
 

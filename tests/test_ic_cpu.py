@@ -18,7 +18,8 @@ LAYOUT_C = r"""
 int main(void) {
   printf("size %zu\n", sizeof(pfa_ic_recipe));
   F(nx) F(ny) F(nz) F(matrix) F(enrich) F(noise) F(seed) F(n_bands) F(band)
-  F(n_particles) F(centre) F(radius) F(phase) F(dx) F(width)
+  F(n_particles) F(centre) F(radius) F(phase) F(dx) F(width) F(profile) F(bell_sigma)
+  F(bell_range) F(bell_x0) F(particle_mode)
   return 0;
 }
 """
@@ -109,3 +110,28 @@ def test_oracle_recipe_semantics(orc):
         assert f[2 + ph][yi + 1, xi + 1] > 0.99
         xe = ic.XE["del" if ph == 0 else "lav"]
         assert abs(f[0][yi + 1, xi + 1] - xe[0]) < 1e-2 and abs(f[1][yi + 1, xi + 1] - xe[1]) < 1e-2
+
+
+def test_oracle_reference_profile_and_embedding(orc):
+    """The reference's default 2D initial condition as a recipe: the bell
+    curve's mean over its range is the matrix composition and its peak the
+    enrichment (thermo/enrichment.py); embed_OPC's box overwrites the phase
+    (a second, overlapping particle of the same phase replaces the first's
+    values inside its box)."""
+    import oracle as O
+    from pfa_gb300 import ic
+    r = ic.reference_recipe2d(600, 60, seed=3, radius=6.0)
+    f = O.ic_fields(r)
+    nx, dx = r["nx"], r["dx"]
+    pos = dx * (np.arange(nx) - nx // 2)
+    inside = (pos >= r["bell_range"][0]) & (pos <= r["bell_range"][1])
+    for k in range(2):
+        row = f[k][1 + 55, 1:-1]  # a row outside the seed's box (rows 16..44)
+        # the midpoint sum of the bell curve over the range: its mean to 1e-3
+        assert abs(row[inside].mean() - r["matrix"][k]) < 3e-3 * r["matrix"][k]
+        assert row[nx // 2] == r["enrich"][k]  # the peak
+    assert f[2][1 + 30, 1 + 300] > 0.999  # the seed
+    # overwrite: a small second particle over the first one lowers phi there
+    r2 = dict(r, particles=r["particles"] + [(300.0, 30.0, 0.0, 1.0, 0)])
+    g = O.ic_fields(r2)
+    assert g[2][1 + 30, 1 + 306] < f[2][1 + 30, 1 + 306]

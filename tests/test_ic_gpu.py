@@ -68,6 +68,26 @@ def test_generate_tiny_grids(pfa, dims):
         assert np.max(np.abs(g - w)) <= TANH_TOL
 
 
+@pytest.mark.parametrize("dims", [2, 3])
+def test_reference_profile_and_embedding_on_device(pfa, dims):
+    """The bell-curve profile and embed_OPC's box on the device against the
+    oracle (exp and tanh to rounding; the amplitude comes from the host)."""
+    import torch
+    import oracle as O
+    if dims == 2:
+        rec = ic.reference_recipe2d(300, 50, seed=8, radius=5.0)
+    else:
+        rec = ic.recipe3d(40, 30, 24, seed=9, slab=6, n_particles=3, radius=3.0)
+        rec.update(profile=1, bell_sigma=(60e-9, 30e-9), bell_range=(-40 * 5e-9 / 3, 40 * 5e-9 / 3),
+                   bell_x0=20.0, particle_mode=1, bands=[])
+    want = O.ic_fields(rec)
+    dev = [torch.full(want[0].shape, -1.0, dtype=torch.float64, device="cuda") for _ in range(4)]
+    pfa.ic_generate(rec, [t.data_ptr() for t in dev])
+    torch.cuda.synchronize()
+    for g, w in zip([t.cpu().numpy() for t in dev], want):
+        assert np.max(np.abs(g - w)) <= TANH_TOL
+
+
 def test_batch_slot_from_recipe(pfa):
     import oracle as O
     recs = [ic.recipe2d(n, m, seed=20 + n, stripe_width=8, n_particles=3, radius=4.0)
