@@ -355,7 +355,31 @@ def bench_grid3d(args, ws, rank, local, barrier, max_over_ranks, pl, ic):
     g.set_nucleation(interval=0)  # the step kernel alone for the roofline
     g.run(2)
     kms = g.run_timed(50) / 50
+    # e2e: every bench step uploads the four FP64 fields from page-locked host
+    # memory, runs 100 steps with nucleation and reads the fields back
+    import torch
+    host_in = [torch.from_numpy(a).pin_memory().numpy() for a in fields]
+    host_out = [torch.empty(a.shape, dtype=torch.float64, pin_memory=True).numpy()
+                for a in fields]
+    g.set_nucleation(seed=42, interval=STEPS_PER_BENCH_STEP, sigma=NUC["sigma"],
+                     unit_a=NUC["unit_a"], d=(params["dx"],) * 3,
+                     dt_nuc=STEPS_PER_BENCH_STEP * params["dt"])
+
+    def e2e_step():
+        g.upload(host_in)
+        g.run(STEPS_PER_BENCH_STEP)
+        g.read(host_out)
+
+    e2e_step()
+    barrier()
+    t0 = time.perf_counter()
+    e2e_steps = max(1, min(args.steps, 3))
+    for _ in range(e2e_steps):
+        e2e_step()
+    barrier()
+    te = max_over_ranks(time.perf_counter() - t0)
     g.close()
+    io_bytes = 4 * fields[0].size * 8
     g64 = pl.Grid3D(fields, params, precision="fp64")
     g64.run(2)
     ms64 = g64.run_timed(6) / 6
@@ -377,6 +401,9 @@ def bench_grid3d(args, ws, rank, local, barrier, max_over_ranks, pl, ic):
                                "kernel": "k_stream3d_f32", "bytes_per_cell": 48, "kernel_ms": kms,
                                "peak_kind": peak_kind},
                      cpu_baseline=None,
+                     e2e={"value": ws * cells * STEPS_PER_BENCH_STEP * e2e_steps / te,
+                          "unit": "cell-updates/s", "h2d_bytes_per_step": io_bytes,
+                          "d2h_bytes_per_step": io_bytes, "steps": e2e_steps},
                      gpu_launches=args.steps * (STEPS_PER_BENCH_STEP + NUC_LAUNCHES),
                      clocks=clk.summary())
         print(json.dumps(line))
