@@ -104,16 +104,21 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-def profiled_traffic(kernel):
-    """dram read+write bytes per launch from the committed ncu summary, if any."""
+def profiled_value(kernel, key):
+    """A `key: value` line of the committed ncu summary of `kernel`, if any."""
     path = os.path.join(ROOT, "profiles", f"{kernel}.txt")
     try:
         for line in open(path):
-            if line.startswith("traffic_bytes_per_launch:"):
+            if line.startswith(key + ":"):
                 return float(line.split(":", 1)[1])
     except OSError:
         pass
     return None
+
+
+def profiled_traffic(kernel):
+    """dram read+write bytes per launch from the committed ncu summary, if any."""
+    return profiled_value(kernel, "traffic_bytes_per_launch")
 
 
 def cpu_baseline(fields, params, steps, fast=True):
@@ -662,14 +667,22 @@ def main():
                        "l2": "inputs larger than L2 (FP32 state 6 x 67 MB)",
                        "parallelism": f"replicas x{ws}"},
             "fp64": {"value": fp64_value, "unit": "cell-updates/s",
-                     "ms_per_step": ms64, "speedup_fp32_over_fp64": value / ws / fp64_value},
+                     "ms_per_step": ms64, "speedup_fp32_over_fp64": value / ws / fp64_value,
+                     "fp64_flops_per_cell": profiled_value("step2d_f64_4096",
+                                                           "fp64_flops_per_cell"),
+                     "bound": "FP64 pipe"},
             "max_field_error": {"vs": "fp64 GPU step (pinned to the reference at 1e-12)",
                                 "steps": 400, "x_Cr": err[0], "x_Nb": err[1],
                                 "phi_delta": err[2], "phi_laves": err[3]},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "kernel": "k_stream_f32", "bytes_per_cell": bytes_per_cell,
-                         "kernel_ms": kms, "peak_kind": peak_kind},
+                         "kernel_ms": kms, "peak_kind": peak_kind,
+                         # secondary: the 32 B/cell floor of the four fields alone
+                         "no_compensation_floor": {
+                             "bytes_per_cell": 32,
+                             "achieved": 32 * cells / (kms / 1e3) / 1e9,
+                             "frac": 32 * cells / (kms / 1e3) / 1e9 / peak}},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": io_bytes,
                     "d2h_bytes_per_step": io_bytes},
