@@ -18,6 +18,7 @@ Under torchrun each rank runs an independent replica on its own GPU
 import argparse
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -121,6 +122,24 @@ def profiled_traffic(kernel):
     return profiled_value(kernel, "traffic_bytes_per_launch")
 
 
+def cpu_model():
+    """The host CPU's model name (lscpu / /proc/cpuinfo), for the baseline's record."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return platform.machine()
+
+
 def cpu_baseline(fields, params, steps, fast=True):
     """The CPU oracle (the reference's step semantics, reference host flags,
     OpenMP on every host core) on the same workload."""
@@ -156,7 +175,7 @@ def run_reference(args, ws, rank):
             "data": "synthetic", "impl": "reference",
             "config": {"workload": WORKLOAD, "sample": f"{per} time steps of the full grid per step"},
             "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": cores,
-                             "kind": "port",
+                             "kind": "port", "cpu": cpu_model(),
                              "sample": f"{per} FP64 time steps of the {N_SIDE}^2 grid per step"},
             "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
@@ -654,7 +673,7 @@ def main():
             sample_steps = 3
             tc = cpu_baseline(fields, pl.model_params(), sample_steps)
             cpu = {"value": cells * sample_steps / tc, "unit": "cell-updates/s",
-                   "cores": os.cpu_count(), "kind": "port",
+                   "cores": os.cpu_count(), "kind": "port", "cpu": cpu_model(),
                    "sample": f"{sample_steps} FP64 time steps of the {N_SIDE}^2 grid, "
                              f"OpenMP, reference host flags"}
         line = {
