@@ -308,7 +308,9 @@ def bench_batch(args, ws, rank, local, barrier, max_over_ranks, pl, ic):
 def bench_error(args, ws, rank, local, barrier, max_over_ranks, pl, ic):
     """Stated error at the configurations' full step counts: the FP32 form
     against the FP64 step on the 4096^2 grid (10000 steps, nucleation every
-    100 steps with the same seed in both) and the 512^3 grid (2000 steps).
+    100 steps with the same seed in both), the 512^3 grid (2000 steps) and
+    the batch of 64 uneven grids (5000 steps, each grid against its own FP64
+    run).
     Prints one JSON line; `value` is the FP32 rate of the 2D run."""
     if rank != 0:
         return
@@ -346,6 +348,27 @@ def bench_error(args, ws, rank, local, barrier, max_over_ranks, pl, ic):
     out["grid3d"] = {"side": side, "steps": n3, "x_Cr": err3[0], "x_Nb": err3[1],
                      "phi_delta": err3[2], "phi_laves": err3[3], "fp32_ms": res3["fp32"][0],
                      "fp64_ms": res3["fp64"][0]}
+    # the batch of 64 uneven grids, 5000 steps in the batched FP32 form, each
+    # grid against its own FP64 run
+    nb = 5000
+    sides = ic.batch_sides(BATCH_COUNT, seed=3)
+    fields = [ic.batch_grid(sd, seed=1000 + k) for k, sd in enumerate(sides)]
+    arena = sum(pl.Batch.footprint(f[0].shape) for f in fields) + (1 << 20)
+    b = pl.Batch(p2, arena)
+    slots = [b.add(f) for f in fields]
+    tb = b.run_timed(nb)
+    errb = [0.0] * 4
+    t64 = 0.0
+    for f, sl in zip(fields, slots):
+        g = pl.Grid2D(f, p2, precision="fp64")
+        t64 += g.run_timed(nb)
+        for i, (x, y) in enumerate(zip(b.read(sl), g.read())):
+            errb[i] = max(errb[i], float(np.max(np.abs(x[1:-1, 1:-1] - y[1:-1, 1:-1]))))
+        g.close()
+    b.close()
+    out["batch64"] = {"grids": BATCH_COUNT, "steps": nb, "x_Cr": errb[0], "x_Nb": errb[1],
+                      "phi_delta": errb[2], "phi_laves": errb[3], "fp32_ms": tb,
+                      "fp64_ms_one_at_a_time": t64}
     value = N_SIDE * N_SIDE * n2 / (runs["fp32"][1] / 1e3)
     args.steps = 1
     print(json.dumps(_line(args, ws, value, runs["fp32"][1] / 1e3,
