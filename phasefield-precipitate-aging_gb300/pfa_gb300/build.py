@@ -6,6 +6,7 @@ Compiles translation units in parallel and skips the work when the library
 is newer than every source and header.
 """
 import concurrent.futures as cf
+import fcntl
 import glob
 import os
 import subprocess
@@ -52,10 +53,23 @@ def _compile(src):
 
 
 def build(force=False, verbose=False):
-    """Compile the CUDA library; returns its path."""
+    """Compile the CUDA library; returns its path.  Processes that build at
+    the same time (ranks of one job) take turns on a lock file, and the ones
+    that come after the first find the library up to date."""
     if not force and not _stale():
         return LIB
     os.makedirs(BUILD, exist_ok=True)
+    with open(os.path.join(BUILD, ".lock"), "w") as lock:
+        fcntl.flock(lock, fcntl.LOCK_EX)
+        try:
+            if not force and not _stale():
+                return LIB
+            return _build(verbose)
+        finally:
+            fcntl.flock(lock, fcntl.LOCK_UN)
+
+
+def _build(verbose):
     srcs = _sources()
     with cf.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(_compile, srcs))
