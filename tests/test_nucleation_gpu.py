@@ -151,6 +151,28 @@ def test_nucleation_in_the_step_loop(pfa):
     b.close()
 
 
+@pytest.mark.parametrize("precision", ["fp32", "fp32k"])
+def test_fp32_events_match_replica_on_the_same_state(pfa, orc, precision):
+    """The FP32 forms decide on their exact stored values (hi - c): the CPU
+    replica run on the state they hold gives the same events and painted
+    fields (painted values keep a compensation: 16-bit counts of 2^-39 at
+    most, or FP32)."""
+    from golden.make_golden import NUC_A, nuc_struct
+    from pfa_gb300 import ic
+    f = ic.grid2d(96, 80, seed=7, matrix=(0.2600, 0.1680), enrich=(0.2720, 0.1692),
+                  stripes=[30], stripe_width=20, n_particles=2, radius=5.0)
+    g = pfa.Grid2D(f, pfa.model_params(), precision=precision)
+    state = g.read()
+    g.close()
+    want, ev, n = orc.nucleation2d(state, nuc_struct(NUC_A), 11, 0)
+    assert n > 0
+    out, events = _nucleate_once(pfa, f, NUC_A, seed=11, precision=precision)
+    assert events[0] == [(e[0], e[1]) for e in ev]
+    tol = 2.0 ** -39 if precision == "fp32" else 1e-15
+    for a, b in zip(out, want):
+        assert np.max(np.abs(a[1:-1, 1:-1] - b[1:-1, 1:-1])) <= tol
+
+
 def test_fp32_nucleation_runs_and_paints(pfa):
     from golden.make_golden import NUC_A
     g = golden("nucleation.npz")
