@@ -33,6 +33,7 @@ struct Grid3D {
   double* f64[2][4] = {};
   float* A[2] = {};
   float* B[2] = {};
+  Tma3 tm[2] = {};  // TMA maps of (A[b], B[b])
   int pitch32 = 0;
   double dxyz[3] = {};
   int cur = 0;
@@ -116,14 +117,15 @@ int step(Grid3D* g) {
       a.out[k] = g->f64[n][k];
     }
     a.pitch = g->Nx + 2;
-    CK3(launch_step3d(a, true, g->st));
+    CK3(launch_step3d(a, true, nullptr, g->st));
   } else {
     a.in[0] = g->A[c];
     a.in[1] = g->B[c];
     a.out[0] = g->A[n];
     a.out[1] = g->B[n];
     a.pitch = g->pitch32;
-    CK3(launch_step3d(a, false, g->st));
+    a.status = g->ev_status;
+    CK3(launch_step3d(a, false, &g->tm[c], g->st));
   }
   g->cur = n;
   return 0;
@@ -233,6 +235,7 @@ int check_status(Grid3D* g) {
   CK3(cudaStreamSynchronize(g->st));
   if (st) {
     CK3(cudaMemsetAsync(g->ev_status, 0, sizeof(int), g->st));
+    if (st == 3) return err(PFA_ECUDA, "3D step: a TMA staging wait gave up (plane copy never landed)");
     if (st == 2) return err(PFA_EINVAL, "nucleation: a nucleus radius exceeded 256 cells (not painted)");
     return err(PFA_EOVERFLOW, "nucleation: more events than the event buffer holds");
   }
@@ -336,6 +339,7 @@ static int create3d(void** handle, int nx, int ny, int nz, const double* params,
       CK3(cudaMalloc(reinterpret_cast<void**>(&g->B[b]), recs * 8));
       CK3(cudaMemsetAsync(g->A[b], 0, recs * 16, g->st));
       CK3(cudaMemsetAsync(g->B[b], 0, recs * 8, g->st));
+      CK3(encode_step3d_maps(&g->tm[b], g->A[b], g->B[b], g->Nx, g->Ny, g->Nz, g->pitch32));
     }
   }
   CK3(cudaMalloc(reinterpret_cast<void**>(&g->sum_partial), sizeof(double) * kSumBlocks * 5));
@@ -458,8 +462,7 @@ int pfa3d_run_timed(void* handle, int nsteps, float* ms) {
 int pfa3d_sync(void* handle) {
   Grid3D* g = static_cast<Grid3D*>(handle);
   if (!g) return err(PFA_ESTATE, "pfa3d_sync: null handle");
-  CK3(cudaStreamSynchronize(g->st));
-  return 0;
+  return check_status(g);
 }
 
 int pfa3d_read(void* handle, double* conc_Cr, double* conc_Nb, double* phi_del, double* phi_lav) {
@@ -470,8 +473,7 @@ int pfa3d_read(void* handle, double* conc_Cr, double* conc_Nb, double* phi_del, 
   const size_t n = ghost_cells(g) * sizeof(double);
   for (int k = 0; k < 4; k++)
     if (dst[k]) CK3(cudaMemcpyAsync(dst[k], g->f64[0][k], n, cudaMemcpyDeviceToHost, g->st));
-  CK3(cudaStreamSynchronize(g->st));
-  return 0;
+  return check_status(g);
 }
 
 int pfa3d_upload(void* handle, const double* conc_Cr, const double* conc_Nb,

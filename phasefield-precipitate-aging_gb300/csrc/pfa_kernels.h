@@ -3,6 +3,7 @@
 
 #include <cstdint>
 
+#include <cuda.h>  // CUtensorMap
 #include <cuda_runtime.h>
 
 #include "pfa_internal.h"
@@ -106,6 +107,14 @@ struct Step3DArgs {
   ModelConst m;         // m.idx2 = 1/dx^2, 1/dy^2, 1/dz^2
   FastCoef k;
   float dtD[2][2], dtL[2], om2[2], alpha2, kap[2], idx2f[3];
+  int* status;          // FP32 form: set to 3 when a staging wait gave up (may be null)
+};
+
+// TMA descriptors of one FP32-form record pair (A: the float4 records as an
+// FP32 tensor of (4 Nx, Ny, Nz); B: the packed compensations as a uint32
+// tensor of (2 Nx, Ny, Nz); rows pitch records apart)
+struct Tma3 {
+  CUtensorMap a, b;
 };
 
 struct Conv3DArgs {
@@ -116,7 +125,10 @@ struct Conv3DArgs {
 };
 
 cudaError_t prepare_step3d();
-cudaError_t launch_step3d(Step3DArgs a, bool f64, cudaStream_t s);
+cudaError_t encode_step3d_maps(Tma3* t, const void* A, const void* B, int Nx, int Ny, int Nz,
+                               int pitch);
+// t: the maps of a.in[0] / a.in[1] (FP32 form; unused for FP64)
+cudaError_t launch_step3d(Step3DArgs a, bool f64, const Tma3* t, cudaStream_t s);
 cudaError_t launch_import3d(const Conv3DArgs& a, cudaStream_t s);
 cudaError_t launch_export3d(const Conv3DArgs& a, cudaStream_t s);
 

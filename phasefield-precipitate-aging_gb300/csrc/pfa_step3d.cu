@@ -15,17 +15,17 @@
 // from planes published in shared memory, z-neighbours from a register
 // window of solved planes.  F64 (k_stream3d<true>): a three-plane window
 // rotated by a 3x-unrolled loop, one barrier per plane.  F32
-// (k_stream3d_f32): records staged through a four-plane cp.async ring (read
-// once each: the record a plane's solve reads is kept for its update), a
-// four-plane window of solved planes, two planes per barrier, the loop
-// unrolled over four planes so every ring and exchange slot is a constant
-// (512^3: 1.205 ms against 1.42 ms with the F64 kernel's scheme; wider CTAs
-// of 20 warps were slower).
+// (k_stream3d_f32): each plane's box of records staged by TMA tile copies
+// into a four-plane ring completed on mbarriers (read once each: the record
+// a plane's solve reads is kept for its update), a four-plane window of
+// solved planes, two planes per barrier, the loop unrolled over four planes
+// so every ring and exchange slot is a constant.
 #include <cstdint>
 #include <type_traits>
 
 #include "pfa_device.cuh"
 #include "pfa_kernels.h"
+#include "pfa_tma.cuh"
 
 namespace pfa {
 
@@ -257,75 +257,98 @@ __global__ void __launch_bounds__(32 * kW) k_stream3d(Step3DArgs a) {
 }
 
 // ---- FP32 form, two planes per barrier ----
-// Rows reach the threads through a four-plane cp.async ring in shared memory
-// (each thread copies and reads back only its own column), so the window of
-// four solved planes fits the register budget; each iteration solves planes
-// z+1 and z+2, publishes z and z+1 for the neighbouring warps and passes one
-// barrier for both updates.  A plane's record is read from the ring once, for
-// its solve, and kept in registers until its update.
-constexpr int kRing3 = 4;  // planes in the ring (a power of two)
+// Planes reach shared memory through a four-plane ring filled by TMA: one
+// thread issues, per plane, a tiled copy of the CTA's box of A records and
+// one of B records, both completing on the plane slot's mbarrier; every
+// thread reads its own (clamped) record from the slot.  The A box spans the
+// warp's 32 columns, so a warp's reads of a row fall on whole 128-byte
+// lines; the B box spans 34 records from one further left, so that it
+// starts on a 16-byte boundary for the 8-byte records (30 * blockIdx.x - 2
+// is even).  Records outside the grid arrive as zeros and are never read
+// (threads past an edge read the clamped record).  Each iteration solves
+// planes z+1 and z+2, publishes z and z+1 for the neighbouring warps and
+// passes one barrier for both updates; a plane's record is read from the
+// ring once, for its solve, and kept in registers until its update.
+constexpr int kRing3 = 4;          // planes in the ring (a power of two)
+constexpr int kBoxA = 32;          // A records per staged row (512 B)
+constexpr int kBoxB = kCols + 4;   // B records per staged row (34 * 8 B = 272 B)
 struct Smem3 {
-  float4 ra[kRing3][32 * kW];
-  uint2 rc[kRing3][32 * kW];
+  float4 ra[kRing3][kW][kBoxA];
+  uint2 rc[kRing3][kW][kBoxB];
   Nb3<float> sh[4][kW][32];  // two published planes per iteration, two iterations
+  unsigned long long bar[kRing3];
 };
-constexpr size_t kSmem3 = sizeof(Smem3);
+constexpr uint32_t kSlotA = kW * kBoxA * sizeof(float4), kSlotB = kW * kBoxB * sizeof(uint2);
+constexpr uint32_t kTxPlane = kSlotA + kSlotB;  // bytes one plane's two copies deliver
+static_assert(kSlotA % 128 == 0 && kSlotB % 128 == 0 && (kRing3 * kSlotA) % 128 == 0,
+              "ring slots must stay 128-byte aligned");
+constexpr size_t kSmem3 = sizeof(Smem3) + 128;  // + slack to align the base to 128 B
 
-__device__ __forceinline__ void cp16(uint32_t dst, const void* src) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp8(uint32_t dst, const void* src) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(dst), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_wait() {
-  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
-}
-
-__global__ void __launch_bounds__(32 * kW) k_stream3d_f32(Step3DArgs a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  Smem3& sm = *reinterpret_cast<Smem3*>(smem_raw);
+__global__ void __launch_bounds__(32 * kW)
+    k_stream3d_f32(Step3DArgs a, const __grid_constant__ Tma3 t) {
+  extern __shared__ unsigned char smem_raw[];
+  const uint32_t raw = tma::smem_addr(smem_raw);
+  Smem3& sm = *reinterpret_cast<Smem3*>(smem_raw + ((128u - (raw & 127u)) & 127u));
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-  const int x = blockIdx.x * kCols - 1 + lane;
-  const int y = blockIdx.y * kRowsOut - 1 + w;
+  const int xa = blockIdx.x * kCols - 1;     // first record of the staged A box
+  const int yb = blockIdx.y * kRowsOut - 1;  // first row of the staged boxes
+  const int x = xa + lane, y = yb + w;
   const int z0 = blockIdx.z * a.zrows;
   const int z1 = min(z0 + a.zrows, a.Nz);
   S3<false> S{a, min(max(x, 0), a.Nx - 1), min(max(y, 0), a.Ny - 1),
               lane >= 1 && lane <= kCols && w >= 1 && w <= kRowsOut && x < a.Nx && y < a.Ny};
   S.col = (long long)S.cy * a.pitch + S.cx;
   S.plane = (long long)a.Ny * a.pitch;
-  const float4* A = static_cast<const float4*>(a.in[0]);
-  const uint2* B = static_cast<const uint2*>(a.in[1]);
-  const uint32_t sa = uint32_t(__cvta_generic_to_shared(&sm.ra[0][tid]));
-  const uint32_t sc = uint32_t(__cvta_generic_to_shared(&sm.rc[0][tid]));
-  constexpr uint32_t kPlaneA = 32 * kW * sizeof(float4), kPlaneC = 32 * kW * sizeof(uint2);
-  // plane p lives in ring slot (p - z0 + 1) & 3; planes past z1 are never read.
-  // The slot arguments below are compile-time constants.
+  const int bx = S.cx - xa, by = S.cy - yb;  // this thread's record in a staged A plane
+                                             // (bx + 1 in a B plane)
+  const uint32_t bar0 = tma::smem_addr(&sm.bar[0]);
+  const uint32_t dA = tma::smem_addr(&sm.ra[0][0][0]), dB = tma::smem_addr(&sm.rc[0][0][0]);
+  if (tid == 0) {
+    tma::prefetch_map(&t.a);
+    tma::prefetch_map(&t.b);
+    for (int k = 0; k < kRing3; k++) tma::bar_init(bar0 + 8 * k, 1);
+    tma::bar_init_fence();
+  }
+  __syncthreads();
+  // plane p lives in ring slot (p - z0 + 1) & 3 and completes that slot's
+  // phase (p - z0 + 1) >> 2; planes past z1 are never issued.  The slot
+  // arguments below are compile-time constants.
+  int last[kRing3] = {-2, -2, -2, -2};  // thread 0: last plane issued into each slot
   auto issue = [&](int p, int sl) {
-    if (p <= z1) {
-      const long long i = S.cell(p);
-      cp16(sa + sl * kPlaneA, A + i);
-      cp8(sc + sl * kPlaneC, B + i);
+    if (tid == 0 && p <= z1) {
+      const int zc = min(max(p, 0), a.Nz - 1);
+      tma::proxy_fence();  // the slot's earlier reads (ordered by the barrier) come first
+      tma::bar_arrive_tx(bar0 + 8 * sl, kTxPlane);
+      tma::load3(dA + sl * kSlotA, &t.a, 4 * xa, yb, zc, bar0 + 8 * sl);
+      tma::load3(dB + sl * kSlotB, &t.b, 2 * (xa - 1), yb, zc, bar0 + 8 * sl);
+      last[sl] = p;
     }
-    cp_commit();  // one group per plane: the wait counts stay uniform
+  };
+  bool gave_up = false;
+  auto wait = [&](int p, int sl) {
+    if (!tma::bar_wait(bar0 + 8 * sl, uint32_t((p - z0 + 1) >> 2) & 1u)) gave_up = true;
   };
   auto fetch = [&](int sl) {
-    const float4 v = sm.ra[sl][tid];
-    return Raw3<float>{v.x, v.y, v.z, v.w, sm.rc[sl][tid]};
+    const float4 v = sm.ra[sl][by][bx];
+    return Raw3<float>{v.x, v.y, v.z, v.w, sm.rc[sl][by][bx + 1]};
   };
   for (int k = -1; k <= 2; k++) issue(z0 + k, k + 1);
-  cp_wait<2>();  // planes z0-1 and z0
+  wait(z0 - 1, 0);
+  wait(z0, 1);
   Raw3<float> rB = fetch(1), rC, rD;  // raw records kept for the updates
   Nb3<float> nA = S.solve(fetch(0)), nB = S.solve(rB), nC, nD;
+  __syncthreads();  // slots 0 and 1 are read before the first pair refills them
   // two planes z, z+1; issued up to plane z+2 on entry.  Q = (z - z0) & 3
   // (0 or 2) fixes the ring slots and the exchange slots.
   auto pair = [&](auto q, int z) {
     constexpr int Q = decltype(q)::value;
     constexpr int s1 = (2 + Q) & 3, s2 = (3 + Q) & 3, s3 = Q & 3, s4 = (1 + Q) & 3;
-    issue(z + 3, s3);  // into the slot of plane z-1
-    cp_wait<1>();      // planes up to z+2 have landed
+    // the slots of planes z-1 and z: read before the previous barrier
+    issue(z + 3, s3);
+    issue(z + 4, s4);
+    wait(z + 1, s1);
     rC = fetch(s1);
+    wait(z + 2, s2);
     rD = fetch(s2);
     nC = S.solve(rC);
     nD = S.solve(rD);
@@ -336,7 +359,6 @@ __global__ void __launch_bounds__(32 * kW) k_stream3d_f32(Step3DArgs a) {
     // these exchange slots were last read two pairs ago, before the previous
     // pair's barrier
     __syncthreads();
-    issue(z + 4, s4);  // into the slot of plane z (its record is held in rB)
     S.update_from(z, nA, nB, nC, rB, b0);
     S.update_from(z + 1, nB, nC, nD, rC, b1);
     nA = nC;
@@ -354,17 +376,22 @@ __global__ void __launch_bounds__(32 * kW) k_stream3d_f32(Step3DArgs a) {
     z += 2;
     q = 2;
   }
-  if (z < z1) {  // one plane left
-    const int s1 = (2 + q) & 3, s3 = q & 3;
-    issue(z + 3, s3);
-    cp_wait<2>();  // plane z+1
+  if (z < z1) {  // one plane left; plane z+1 (<= z1) was issued by the last pair
+    const int s1 = (2 + q) & 3;
+    wait(z + 1, s1);
     nC = S.solve(fetch(s1));
     Nb3<float>(*b0)[32] = sm.sh[q];
     b0[w][lane] = nB;
     __syncthreads();
     S.update_from(z, nA, nB, nC, rB, b0);
   }
-  cp_wait<0>();  // no copy into shared memory outlives the block
+  if (gave_up && a.status) atomicExch(a.status, 3);
+  // thread 0 waits for every plane it issued, so its copies have all landed
+  // unless one of its waits gave up: then it waits again (bounded) before
+  // the block exits
+  if (tid == 0 && gave_up)
+    for (int k = 0; k < kRing3; k++)
+      if (last[k] >= z0 - 1) tma::bar_wait(bar0 + 8 * k, uint32_t((last[k] - z0 + 1) >> 2) & 1u);
 }
 
 // FP64 ghost-ring fields <-> FP32 records (3D)
@@ -453,15 +480,51 @@ cudaError_t prepare_step3d() {
   return e == cudaSuccess ? query3<false>() : e;
 }
 
-cudaError_t launch_step3d(Step3DArgs a, bool f64, cudaStream_t s) {
+// cuTensorMapEncodeTiled through the runtime's driver entry point (the
+// library links the static runtime, not the driver library)
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                 const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                 const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                 CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+cudaError_t encode_step3d_maps(Tma3* t, const void* A, const void* B, int Nx, int Ny, int Nz,
+                               int pitch) {
+  static EncodeTiled encode = nullptr;
+  if (!encode) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    const cudaError_t e =
+        cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+    if (e != cudaSuccess) return e;
+    if (q != cudaDriverEntryPointSuccess || !fn) return cudaErrorNotSupported;
+    encode = reinterpret_cast<EncodeTiled>(fn);
+  }
+  const cuuint32_t box_a[3] = {4 * kBoxA, kW, 1}, box_b[3] = {2 * kBoxB, kW, 1}, one[3] = {1, 1, 1};
+  const cuuint64_t dim_a[3] = {4ull * Nx, cuuint64_t(Ny), cuuint64_t(Nz)};
+  const cuuint64_t dim_b[3] = {2ull * Nx, cuuint64_t(Ny), cuuint64_t(Nz)};
+  const cuuint64_t str_a[2] = {16ull * pitch, 16ull * pitch * Ny};
+  const cuuint64_t str_b[2] = {8ull * pitch, 8ull * pitch * Ny};
+  CUresult r = encode(&t->a, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void*>(A), dim_a, str_a,
+                      box_a, one, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r == CUDA_SUCCESS)
+    r = encode(&t->b, CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, const_cast<void*>(B), dim_b, str_b, box_b,
+               one, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+cudaError_t launch_step3d(Step3DArgs a, bool f64, const Tma3* t, cudaStream_t s) {
   const int resident = g_resident3[f64] > 0 ? g_resident3[f64] : 152;
   a.zrows = segment_planes(a.Nx, a.Ny, a.Nz, resident);
   dim3 grid((a.Nx + kCols - 1) / kCols, (a.Ny + kRowsOut - 1) / kRowsOut,
             (a.Nz + a.zrows - 1) / a.zrows);
-  if (f64)
+  if (f64) {
     k_stream3d<true><<<grid, 32 * kW, 0, s>>>(a);
-  else
-    k_stream3d_f32<<<grid, 32 * kW, kSmem3, s>>>(a);
+  } else {
+    if (!t) return cudaErrorInvalidValue;
+    k_stream3d_f32<<<grid, 32 * kW, kSmem3, s>>>(a, *t);
+  }
   return cudaGetLastError();
 }
 
