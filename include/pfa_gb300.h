@@ -74,6 +74,17 @@ int pfa_read_out_result(struct CudaData* dev, double* conc_Cr, double* conc_Nb,
 /* the host-to-device half of init_cuda (src/data.cu:83-91) on a live CudaData */
 int pfa_upload_fields(struct CudaData* dev, const double* conc_Cr, const double* conc_Nb,
                       const double* phi_del, const double* phi_lav, int nx, int ny);
+/* pfa_read_out_result / pfa_upload_fields without waiting: the copies (and,
+ * for the FP32 forms, the layout conversion) are enqueued behind the work
+ * already issued on dev and the call returns.  The host buffers must stay
+ * valid, and an upload's sources unchanged, until pfa_sync(dev) returns;
+ * they overlap other work only when page-locked.  Later work on dev (steps,
+ * uploads, read-outs) is ordered after them, so a handle can read out one
+ * job, take the next job's fields and step it without waiting in between. */
+int pfa_read_out_result_async(struct CudaData* dev, double* conc_Cr, double* conc_Nb,
+                              double* phi_del, double* phi_lav, int nx, int ny);
+int pfa_upload_fields_async(struct CudaData* dev, const double* conc_Cr, const double* conc_Nb,
+                            const double* phi_del, const double* phi_lav, int nx, int ny);
 /* src/discretization.cuh:39-111 */
 int pfa_device_boundaries(struct CudaData* dev, int nx, int ny, int nm, int bx, int by);
 int pfa_device_fictitious(struct CudaData* dev, int nx, int ny, int nm, int bx, int by);
@@ -104,6 +115,7 @@ int pfa_set_nucleation_args(struct CudaData* dev, int nuc_interval, double sigma
                             double dt_nuc);
 /* pfa_run bracketed by CUDA events on the library's stream; ms = elapsed */
 int pfa_run_timed(struct CudaData* dev, int nsteps, double alpha, double dt, float* ms);
+/* waits for all work issued on dev, asynchronous read-outs included */
 int pfa_sync(struct CudaData* dev);
 void* pfa_stream(struct CudaData* dev);
 /* number of nucleation events of the last nucleation call, and the events

@@ -99,6 +99,7 @@ struct State {
   double* sum_partial = nullptr;
   double* sum_out = nullptr;
   cudaEvent_t xev[8] = {};  // chunked transfers (created on first use)
+  cudaEvent_t xdone = nullptr;  // the read-out's last copy on str_B
   double* nrg_map[2] = {};  // per-node chemical / gradient energy (on request)
   std::vector<GraphEntry> graphs;
 };
@@ -573,6 +574,7 @@ static int free_core(CudaData* dev) {
     g_tab.erase(it);
   }
   if (s->st) cudaStreamSynchronize(s->st);
+  if (dev->str_B) cudaStreamSynchronize(dev->str_B);  // an asynchronous read-out
   drop_graphs(s);
   double* f[16] = {dev->conc_Cr_old, dev->conc_Cr_new, dev->conc_Nb_old, dev->conc_Nb_new,
                    dev->phi_del_old, dev->phi_del_new, dev->phi_lav_old, dev->phi_lav_new,
@@ -593,6 +595,7 @@ static int free_core(CudaData* dev) {
   cudaFree(s->nrg_map[1]);
   for (cudaEvent_t e : s->xev)
     if (e) cudaEventDestroy(e);
+  if (s->xdone) cudaEventDestroy(s->xdone);
   cudaStream_t st[4] = {dev->str_A, dev->str_B, dev->str_C, dev->str_D};
   for (auto x : st)
     if (x) cudaStreamDestroy(x);
@@ -615,6 +618,7 @@ static int ensure_xfer(State* s) {
   if (s->xev[0]) return 0;
   for (int i = 0; i < kXferBands; i++)
     CK(cudaEventCreateWithFlags(&s->xev[i], cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&s->xdone, cudaEventDisableTiming));
   return 0;
 }
 
@@ -624,8 +628,10 @@ static void band_rows(const State* s, int r0, int r1, ConvArgs& c) {
   c.y1 = r1 - 1 < s->Ny ? r1 - 1 : s->Ny;
 }
 
+// wait = false: enqueue only; later work on the library stream (uploads,
+// steps, exports that overwrite the FP64 fields) is ordered after the copies
 static int read_core(CudaData* dev, double* cr, double* nb, double* pd, double* pl, int nx,
-                     int ny) {
+                     int ny, bool wait) {
   State* s = lookup(dev);
   if (!s) return fail(PFA_ESTATE, "read_out_result: unknown CudaData");
   if (nx != s->nx || ny != s->ny) return fail(PFA_EINVAL, "read_out_result: size mismatch");
@@ -651,19 +657,22 @@ static int read_core(CudaData* dev, double* cr, double* nb, double* pd, double* 
         if (dst[k])
           CK(cudaMemcpyAsync(dst[k] + off, src[k] + off, bytes, cudaMemcpyDeviceToHost, dev->str_B));
     }
-    CK(cudaStreamSynchronize(dev->str_B));
+    CK(cudaEventRecord(s->xdone, dev->str_B));
+    CK(cudaStreamWaitEvent(s->st, s->xdone, 0));
+    if (wait) CK(cudaStreamSynchronize(dev->str_B));
     return 0;
   }
   if (int r = f32_export(dev, s)) return r;
   const size_t n = size_t(nx) * ny;
   for (int k = 0; k < 4; k++)
     if (dst[k]) CK(cudaMemcpyAsync(dst[k], src[k], n * sizeof(double), cudaMemcpyDeviceToHost, s->st));
-  CK(cudaStreamSynchronize(s->st));
+  if (wait) CK(cudaStreamSynchronize(s->st));
   return 0;
 }
 
+// wait = false: enqueue only (the sources are read asynchronously)
 static int upload_core(CudaData* dev, const double* cr, const double* nb, const double* pd,
-                       const double* pl, int nx, int ny) {
+                       const double* pl, int nx, int ny, bool wait) {
   State* s = lookup(dev);
   if (!s) return fail(PFA_ESTATE, "upload: unknown CudaData");
   if (nx != s->nx || ny != s->ny) return fail(PFA_EINVAL, "upload: size mismatch");
@@ -678,11 +687,11 @@ static int upload_core(CudaData* dev, const double* cr, const double* nb, const 
     if (int r = ensure_f32(s)) return r;
     s->cur = 0;
     CK(launch_import_f32(conv_args(dev, s), s->st));
-    CK(cudaStreamSynchronize(s->st));  // page-locked sources are read asynchronously
+    if (wait) CK(cudaStreamSynchronize(s->st));  // page-locked sources are read asynchronously
     s->f32_live = true;
     return 0;
   }
-  CK(cudaStreamSynchronize(s->st));  // page-locked sources are read asynchronously
+  if (wait) CK(cudaStreamSynchronize(s->st));  // page-locked sources are read asynchronously
   s->f32_live = false;
   return 0;
 }
@@ -749,7 +758,7 @@ void free_cuda(struct CudaData* dev) { free_core(dev); }
 
 void read_out_result(struct CudaData* dev, struct HostData* host, const int nx, const int ny) {
   read_core(dev, host->conc_Cr_new[0], host->conc_Nb_new[0], host->phi_del_new[0],
-            host->phi_lav_new[0], nx, ny);
+            host->phi_lav_new[0], nx, ny, true);
 }
 
 float nTiles(int domain_size, int tile_loc, int mask_size) {
@@ -918,12 +927,22 @@ int pfa_free_cuda(struct CudaData* dev) { return free_core(dev); }
 
 int pfa_read_out_result(struct CudaData* dev, double* cr, double* nb, double* pd, double* pl,
                         int nx, int ny) {
-  return read_core(dev, cr, nb, pd, pl, nx, ny);
+  return read_core(dev, cr, nb, pd, pl, nx, ny, true);
 }
 
 int pfa_upload_fields(struct CudaData* dev, const double* cr, const double* nb, const double* pd,
                       const double* pl, int nx, int ny) {
-  return upload_core(dev, cr, nb, pd, pl, nx, ny);
+  return upload_core(dev, cr, nb, pd, pl, nx, ny, true);
+}
+
+int pfa_read_out_result_async(struct CudaData* dev, double* cr, double* nb, double* pd, double* pl,
+                              int nx, int ny) {
+  return read_core(dev, cr, nb, pd, pl, nx, ny, false);
+}
+
+int pfa_upload_fields_async(struct CudaData* dev, const double* cr, const double* nb,
+                            const double* pd, const double* pl, int nx, int ny) {
+  return upload_core(dev, cr, nb, pd, pl, nx, ny, false);
 }
 
 #define PFA_CSTAGE(fn)                                        \
@@ -1011,6 +1030,7 @@ int pfa_sync(struct CudaData* dev) {
   State* s = lookup(dev);
   if (!s) return fail(PFA_ESTATE, "pfa_sync: unknown CudaData");
   CK(cudaStreamSynchronize(s->st));
+  if (dev->str_B) CK(cudaStreamSynchronize(dev->str_B));
   return 0;
 }
 

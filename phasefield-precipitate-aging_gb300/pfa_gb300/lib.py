@@ -121,6 +121,8 @@ def load():
         "pfa_free_cuda": (_i, [P]),
         "pfa_read_out_result": (_i, [P, _dp, _dp, _dp, _dp, _i, _i]),
         "pfa_upload_fields": (_i, [P, _dp, _dp, _dp, _dp, _i, _i]),
+        "pfa_read_out_result_async": (_i, [P, _dp, _dp, _dp, _dp, _i, _i]),
+        "pfa_upload_fields_async": (_i, [P, _dp, _dp, _dp, _dp, _i, _i]),
         "pfa_device_boundaries": (_i, [P, _i, _i, _i, _i, _i]),
         "pfa_device_fictitious": (_i, [P, _i, _i, _i, _i, _i]),
         "pfa_fictitious_boundaries": (_i, [P, _i, _i, _i, _i, _i]),
@@ -328,16 +330,28 @@ class Grid2D:
             check(self.L.pfa_last_error(), "events")
         return [(cells[k], ph[k]) for k in range(min(n, cap))]
 
-    def read(self, out=None):
+    def read(self, out=None, wait=True):
+        """read_out_result into `out` (new arrays if None).  wait=False only
+        enqueues the copies: `out` (page-locked to overlap other work) is
+        filled once sync() returns."""
         out = out or [np.empty((self.ny, self.nx)) for _ in range(4)]
-        check(self.L.pfa_read_out_result(self.ref, *[_ptr(a) for a in out], self.nx, self.ny),
-              "read_out_result")
+        fn = self.L.pfa_read_out_result if wait else self.L.pfa_read_out_result_async
+        check(fn(self.ref, *[_ptr(a) for a in out], self.nx, self.ny), "read_out_result")
         return out
 
-    def upload(self, fields):
-        f = [np.ascontiguousarray(a, dtype=np.float64) for a in fields]
-        check(self.L.pfa_upload_fields(self.ref, *[_ptr(a) for a in f], self.nx, self.ny),
-              "upload_fields")
+    def upload(self, fields, wait=True):
+        """Replace the fields.  wait=False only enqueues the copies: the
+        arrays must be C-contiguous float64 and stay unchanged until sync()."""
+        if wait:
+            f = [np.ascontiguousarray(a, dtype=np.float64) for a in fields]
+            check(self.L.pfa_upload_fields(self.ref, *[_ptr(a) for a in f], self.nx, self.ny),
+                  "upload_fields")
+            return
+        for a in fields:
+            if a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"]:
+                raise ValueError("upload(wait=False) needs C-contiguous float64 arrays")
+        check(self.L.pfa_upload_fields_async(self.ref, *[_ptr(a) for a in fields], self.nx,
+                                             self.ny), "upload_fields")
 
     def dataviz(self):
         out = [np.empty((self.ny, self.nx)) for _ in range(6)]

@@ -1,8 +1,10 @@
 """Page-locked host buffers (the fast path of the copy engines, read
 asynchronously): uploads and read-outs give the same bits as pageable
 buffers; a caller may overwrite its buffer as soon as an upload returns
-(batch members: after pfa_batch_sync).  Also the FP64-free split of the
-layout conversion against the FP64 expression it replaces."""
+(batch members: after pfa_batch_sync); the asynchronous upload and
+read-out keep stream order on a handle and across two alternating handles.
+Also the FP64-free split of the layout conversion against the FP64
+expression it replaces."""
 import numpy as np
 import pytest
 
@@ -120,3 +122,63 @@ def test_split_matches_the_fp64_expression(pfa):
     assert np.array_equal(hi.view(np.uint32), want_hi.view(np.uint32))
     ok = np.isfinite(want_c)
     assert np.array_equal(c[ok].view(np.uint32), want_c[ok].view(np.uint32))
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_async_read_then_upload_keeps_order(pfa, precision):
+    """A read-out enqueued without waiting, then an upload and steps on the
+    same handle: the read-out still returns the state before the upload
+    (the upload waits for its copies), and the steps run on the uploaded
+    fields."""
+    f = ic.grid2d(150, 97, seed=6, stripe_width=20, n_particles=2, radius=5.0)
+    g = ic.grid2d(150, 97, seed=7, stripe_width=20, n_particles=2, radius=5.0)
+    p = pfa.model_params()
+    ref = pfa.Grid2D(f, p, precision=precision)
+    ref.run(20)
+    want_read = ref.read()
+    ref.upload(g)
+    ref.run(15)
+    want_end = ref.read()
+    ref.close()
+    grid = pfa.Grid2D(f, p, precision=precision)
+    grid.run(20)
+    out = _pinned_like([np.zeros_like(a) for a in f])
+    src = _pinned_like(g)
+    grid.read(out, wait=False)
+    grid.upload(src, wait=False)
+    grid.run(15)
+    grid.sync()
+    assert _same(out, want_read)
+    assert _same(grid.read(), want_end)
+    grid.close()
+
+
+def test_two_handles_pipelined_jobs_match_serial(pfa):
+    """Independent jobs on two alternating handles with asynchronous
+    transfers (job k+1's upload and job k-1's read-out overlap job k's
+    steps): every job's result is the one a serial upload / run / read gives."""
+    p = pfa.model_params()
+    jobs = [ic.grid2d(256, 192, seed=s, stripes=[40, 150], stripe_width=24, n_particles=3,
+                      radius=6.0) for s in range(5)]
+    want = []
+    g = pfa.Grid2D(jobs[0], p, precision="fp32")
+    for f in jobs:
+        g.upload(f)
+        g.run(40)
+        want.append(g.read())
+    g.close()
+    host_in = [_pinned_like(f) for f in jobs]
+    host_out = [_pinned_like([np.zeros_like(a) for a in f]) for f in jobs]
+    h = [pfa.Grid2D(jobs[0], p, precision="fp32"), pfa.Grid2D(jobs[0], p, precision="fp32")]
+    h[0].upload(host_in[0], wait=False)
+    for k in range(len(jobs)):
+        d, o = h[k % 2], h[(k + 1) % 2]
+        if k + 1 < len(jobs):
+            o.upload(host_in[k + 1], wait=False)
+        d.run(40)
+        d.read(host_out[k], wait=False)
+    for x in h:
+        x.sync()
+        x.close()
+    for k in range(len(jobs)):
+        assert _same(host_out[k], want[k]), k
