@@ -140,6 +140,14 @@ int pfa3d_sync(void* handle);  /* wait for the handle's enqueued work */
 int pfa3d_read(void* handle, double* conc_Cr, double* conc_Nb, double* phi_del, double* phi_lav);
 int pfa3d_upload(void* handle, const double* conc_Cr, const double* conc_Nb,
                  const double* phi_del, const double* phi_lav);
+/* pfa3d_read / pfa3d_upload without waiting (as pfa_read_out_result_async /
+ * pfa_upload_fields_async): the buffers stay valid, and an upload's sources
+ * unchanged, until pfa3d_sync returns; later work on the handle is ordered
+ * after them */
+int pfa3d_read_async(void* handle, double* conc_Cr, double* conc_Nb, double* phi_del,
+                     double* phi_lav);
+int pfa3d_upload_async(void* handle, const double* conc_Cr, const double* conc_Nb,
+                       const double* phi_del, const double* phi_lav);
 int pfa3d_summarize(void* handle, double* out);
 /* free energy as pfa_summarize_energy, dV = dx dy dz, gradients in 3D */
 int pfa3d_summarize_energy(void* handle, double Omega, double* energy);

@@ -465,29 +465,58 @@ int pfa3d_sync(void* handle) {
   return check_status(g);
 }
 
-int pfa3d_read(void* handle, double* conc_Cr, double* conc_Nb, double* phi_del, double* phi_lav) {
-  Grid3D* g = static_cast<Grid3D*>(handle);
-  if (!g) return err(PFA_ESTATE, "pfa3d_read: null handle");
+// the read-out and the upload, waiting at the end or (wait = 0) only
+// enqueued on the handle's stream, which orders everything after them
+static int read3d(Grid3D* g, double* const* dst, bool wait) {
   if (int r = sync_f64(g)) return r;
-  double* dst[4] = {conc_Cr, conc_Nb, phi_del, phi_lav};
   const size_t n = ghost_cells(g) * sizeof(double);
   for (int k = 0; k < 4; k++)
     if (dst[k]) CK3(cudaMemcpyAsync(dst[k], g->f64[0][k], n, cudaMemcpyDeviceToHost, g->st));
-  return check_status(g);
+  return wait ? check_status(g) : 0;
+}
+
+static int upload3d(Grid3D* g, const double* const* src, bool wait) {
+  const size_t n = ghost_cells(g) * sizeof(double);
+  for (int k = 0; k < 4; k++)
+    CK3(cudaMemcpyAsync(g->f64[0][k], src[k], n, cudaMemcpyHostToDevice, g->st));
+  if (wait) CK3(cudaStreamSynchronize(g->st));  // page-locked sources are read asynchronously
+  g->cur = 0;
+  g->f32_live = false;
+  return 0;
+}
+
+int pfa3d_read(void* handle, double* conc_Cr, double* conc_Nb, double* phi_del, double* phi_lav) {
+  Grid3D* g = static_cast<Grid3D*>(handle);
+  if (!g) return err(PFA_ESTATE, "pfa3d_read: null handle");
+  double* dst[4] = {conc_Cr, conc_Nb, phi_del, phi_lav};
+  return read3d(g, dst, true);
+}
+
+int pfa3d_read_async(void* handle, double* conc_Cr, double* conc_Nb, double* phi_del,
+                     double* phi_lav) {
+  Grid3D* g = static_cast<Grid3D*>(handle);
+  if (!g) return err(PFA_ESTATE, "pfa3d_read_async: null handle");
+  double* dst[4] = {conc_Cr, conc_Nb, phi_del, phi_lav};
+  return read3d(g, dst, false);
 }
 
 int pfa3d_upload(void* handle, const double* conc_Cr, const double* conc_Nb,
                  const double* phi_del, const double* phi_lav) {
   Grid3D* g = static_cast<Grid3D*>(handle);
   if (!g) return err(PFA_ESTATE, "pfa3d_upload: null handle");
+  if (!conc_Cr || !conc_Nb || !phi_del || !phi_lav) return err(PFA_EINVAL, "pfa3d_upload: null argument");
   const double* src[4] = {conc_Cr, conc_Nb, phi_del, phi_lav};
-  const size_t n = ghost_cells(g) * sizeof(double);
-  for (int k = 0; k < 4; k++)
-    CK3(cudaMemcpyAsync(g->f64[0][k], src[k], n, cudaMemcpyHostToDevice, g->st));
-  CK3(cudaStreamSynchronize(g->st));  // page-locked sources are read asynchronously
-  g->cur = 0;
-  g->f32_live = false;
-  return 0;
+  return upload3d(g, src, true);
+}
+
+int pfa3d_upload_async(void* handle, const double* conc_Cr, const double* conc_Nb,
+                       const double* phi_del, const double* phi_lav) {
+  Grid3D* g = static_cast<Grid3D*>(handle);
+  if (!g) return err(PFA_ESTATE, "pfa3d_upload_async: null handle");
+  if (!conc_Cr || !conc_Nb || !phi_del || !phi_lav)
+    return err(PFA_EINVAL, "pfa3d_upload_async: null argument");
+  const double* src[4] = {conc_Cr, conc_Nb, phi_del, phi_lav};
+  return upload3d(g, src, false);
 }
 
 int pfa3d_summarize(void* handle, double* out) {

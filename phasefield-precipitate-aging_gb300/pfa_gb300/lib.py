@@ -152,6 +152,8 @@ def load():
         "pfa3d_run_timed": (_i, [ctypes.c_void_p, _i, _fp]),
         "pfa3d_read": (_i, [ctypes.c_void_p, _dp, _dp, _dp, _dp]),
         "pfa3d_upload": (_i, [ctypes.c_void_p, _dp, _dp, _dp, _dp]),
+        "pfa3d_read_async": (_i, [ctypes.c_void_p, _dp, _dp, _dp, _dp]),
+        "pfa3d_upload_async": (_i, [ctypes.c_void_p, _dp, _dp, _dp, _dp]),
         "pfa3d_summarize": (_i, [ctypes.c_void_p, _dp]),
         "pfa3d_destroy": (_i, [ctypes.c_void_p]),
         "pfa3d_footprint": (ctypes.c_size_t, [_i, _i, _i, _i]),
@@ -462,14 +464,25 @@ class Grid3D:
             check(self.L.pfa_last_error(), "events")
         return [(cells[k], ph[k]) for k in range(min(n, cap))]
 
-    def read(self, out=None):
+    def read(self, out=None, wait=True):
+        """The fields into `out` (new arrays if None); wait=False only
+        enqueues the copies (`out` is filled once sync() returns)."""
         out = out or [np.empty(self.shape) for _ in range(4)]
-        check(self.L.pfa3d_read(self.h, *[_ptr(a) for a in out]), "pfa3d_read")
+        fn = self.L.pfa3d_read if wait else self.L.pfa3d_read_async
+        check(fn(self.h, *[_ptr(a) for a in out]), "pfa3d_read")
         return out
 
-    def upload(self, fields):
-        f = [np.ascontiguousarray(a, dtype=np.float64) for a in fields]
-        check(self.L.pfa3d_upload(self.h, *[_ptr(a) for a in f]), "pfa3d_upload")
+    def upload(self, fields, wait=True):
+        """Replace the fields; wait=False only enqueues the copies (C-contiguous
+        float64 arrays, unchanged until sync())."""
+        if wait:
+            f = [np.ascontiguousarray(a, dtype=np.float64) for a in fields]
+            check(self.L.pfa3d_upload(self.h, *[_ptr(a) for a in f]), "pfa3d_upload")
+            return
+        for a in fields:
+            if a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"]:
+                raise ValueError("upload(wait=False) needs C-contiguous float64 arrays")
+        check(self.L.pfa3d_upload_async(self.h, *[_ptr(a) for a in fields]), "pfa3d_upload")
 
     def summarize(self):
         out = np.zeros(5)

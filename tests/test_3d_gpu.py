@@ -119,3 +119,44 @@ def test_3d_graph_replay_equals_single_steps(pfa):
             assert np.array_equal(x, y), prec
         a.close()
         b.close()
+
+
+def test_3d_async_transfers_keep_order(pfa):
+    """pfa3d_read_async then pfa3d_upload_async and steps on one handle, and
+    jobs alternating over two handles: each read-out returns the state of its
+    own job, as the waiting calls give it."""
+    import torch
+    from pfa_gb300 import ic
+    p = _params(pfa)
+    jobs = [ic.grid3d(40, 33, 21, seed=s, slab=10, n_particles=2, radius=4.0) for s in range(4)]
+
+    def pinned(arrays):
+        out = []
+        for a in arrays:
+            h = torch.empty(a.shape, dtype=torch.float64, pin_memory=True).numpy()
+            h[...] = a
+            out.append(h)
+        return out
+
+    want = []
+    g = pfa.Grid3D(jobs[0], p, precision="fp32")
+    for f in jobs:
+        g.upload(f)
+        g.run(12)
+        want.append(g.read())
+    g.close()
+    host_in = [pinned(f) for f in jobs]
+    host_out = [pinned([np.zeros_like(a) for a in f]) for f in jobs]
+    h = [pfa.Grid3D(jobs[0], p, precision="fp32") for _ in range(2)]
+    h[0].upload(host_in[0], wait=False)
+    for k in range(len(jobs)):
+        d, o = h[k % 2], h[(k + 1) % 2]
+        if k + 1 < len(jobs):
+            o.upload(host_in[k + 1], wait=False)
+        d.run(12)
+        d.read(host_out[k], wait=False)
+    for x in h:
+        x.sync()
+        x.close()
+    for k in range(len(jobs)):
+        assert all(np.array_equal(a, b) for a, b in zip(host_out[k], want[k])), k
