@@ -125,3 +125,25 @@ def test_oracle_3d_reduces_to_2d(orc):
     o3 = orc.run3d(f3, prm, 20)
     for a, b in zip(o3, o2):
         assert np.max(np.abs(a[2, 1:-1, 1:-1] - b[1:-1, 1:-1])) <= 1e-12 * np.max(np.abs(b))
+
+
+def test_step_matches_reference_cuda_kernels(orc):
+    """The oracle's step against the reference's own CUDA step kernels
+    (src/discretization.cu, compiled here for sm_103a and run on a GB300 by
+    tests/golden/make_ref_gpu_golden.py, nucleation off): within 1e-12 of
+    each field's magnitude on the golden grid (1, 10, 100, 400 steps), with
+    the reference's dt rule (50 steps) and on the 256 x 256 workload (1000
+    steps); measured <= 3.2e-15."""
+    r = golden("ref_gpu_step2d.npz")
+    g = golden("step2d.npz")
+    prm = O.model_params()
+    cur, done = fields_of(g, "ic"), 0
+    for k in (1, 10, 100, 400):
+        cur = orc.run2d(cur, prm, k - done)
+        done = k
+        assert max(field_err(cur, fields_of(r, f"step_s{k}"))) <= 1e-12, k
+    g = golden("step2d_refdt.npz")
+    got = orc.run2d(fields_of(g, "ic"), O.model_params(dt_rule=0), 50)
+    assert max(field_err(got, fields_of(r, "refdt_s50"))) <= 1e-12
+    got = orc.run2d(fields_of(r, "config1_ic"), prm, 1000)
+    assert max(field_err(got, fields_of(r, "config1_s1000"))) <= 1e-12

@@ -1,5 +1,6 @@
-"""GPU parity of the 2D step (through the C ABI) against the oracle and the
-reference-generated golden vectors.
+"""GPU parity of the 2D step (through the C ABI) against the oracle, the
+reference-generated golden vectors and the steps of the reference's own CUDA
+kernels.
 
 Tolerances: the plain FP64 step within 1e-12 of the reference (per field,
 max|a - b| / max|b| over the interior and the ghost edges); the FP32
@@ -34,6 +35,55 @@ def test_fp64_matches_reference_golden(pfa):
         err = field_err(grid.read(), fields_of(g, f"s{k}"))
         assert max(err) <= FP64_TOL, (k, err)
     grid.close()
+
+
+def test_fp64_matches_reference_cuda_kernels(pfa):
+    """The fused FP64 step and the compat stage calls against the reference's
+    own CUDA step kernels, run on a GB300 from its src/discretization.cu
+    (tests/golden/make_ref_gpu_golden.py): golden grid after 1, 10, 100,
+    400 steps, the reference's dt rule after 50, the 256 x 256 workload after
+    1000."""
+    r = golden("ref_gpu_step2d.npz")
+    g = golden("step2d.npz")
+    p = _params(pfa)
+    fused = pfa.Grid2D(fields_of(g, "ic"), p)
+    stages = pfa.Grid2D(fields_of(g, "ic"), p, mode="compat")
+    done = 0
+    for k in (1, 10, 100, 400):
+        fused.run(k - done)
+        for _ in range(k - done):
+            stages.step_stages()
+        done = k
+        want = fields_of(r, f"step_s{k}")
+        assert max(field_err(fused.read(), want)) <= FP64_TOL, k
+        assert max(field_err(stages.read(), want)) <= FP64_TOL, k
+    fused.close()
+    stages.close()
+    g = golden("step2d_refdt.npz")
+    grid = pfa.Grid2D(fields_of(g, "ic"), pfa.model_params(dt_rule=0))
+    grid.run(50)
+    assert max(field_err(grid.read(), fields_of(r, "refdt_s50"))) <= FP64_TOL
+    grid.close()
+    grid = pfa.Grid2D(fields_of(r, "config1_ic"), p)
+    grid.run(1000)
+    err = field_err(grid.read(), fields_of(r, "config1_s1000"))
+    print("FP64 step vs the reference's CUDA kernels, 256^2 after 1000 steps", err)
+    assert max(err) <= FP64_TOL, err
+    grid.close()
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp32k"])
+def test_fp32_against_reference_cuda_kernels(pfa, precision):
+    """The FP32 form on the 256 x 256 workload after 1000 steps against the
+    reference's own CUDA step: within the bound the form holds against FP64."""
+    r = golden("ref_gpu_step2d.npz")
+    grid = pfa.Grid2D(fields_of(r, "config1_ic"), _params(pfa), precision=precision)
+    grid.run(1000)
+    got = grid.read()
+    grid.close()
+    err = [float(np.max(np.abs(interior(a) - interior(b))))
+           for a, b in zip(got, fields_of(r, "config1_s1000"))]
+    assert max(err) <= FP32_TOL_1000, err
 
 
 def test_fp64_reference_dt_rule_golden(pfa):
