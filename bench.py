@@ -152,6 +152,29 @@ def cpu_baseline(fields, params, steps, fast=True):
     return time.perf_counter() - t0
 
 
+def reference_gpu_baseline(fields, steps=10):
+    """The reference's own CUDA step (src/discretization.cu's kernels, built
+    from source for sm_103a into oracle/_ref/ref_step.cubin and launched in its
+    order and shapes by oracle/ref_gpu.py, nucleation off) on the same grid:
+    a baseline timed beside ours, never the measured path."""
+    import ref_gpu
+    if not os.path.exists(ref_gpu.CUBIN):
+        return {"unavailable": "oracle/_ref/ref_step.cubin not built "
+                               "(make -C oracle ref-gpu needs the reference checkout)"}
+    import oracle as O
+    drv = ref_gpu.Driver(ref_gpu.CUBIN)
+    try:
+        t = ref_gpu.time_reference(drv, fields, O.model_params(), steps)
+    finally:
+        drv.close()
+    ny, nx = fields[0].shape
+    return {"value": (nx - 2) * (ny - 2) / t, "unit": "cell-updates/s", "ms_per_step": 1e3 * t,
+            "kind": "the reference's own CUDA kernels (src/discretization.cu, "
+                    "src/parabola625.cu), FP64, launched in src/main.cpp's order on one stream "
+                    "without its host waits",
+            "sample": f"{steps} time steps of the same grid after 2 warm-up steps, nucleation off"}
+
+
 def run_reference(args, ws, rank):
     """--impl reference: the CPU path timed on this host's cores."""
     if rank != 0:
@@ -761,6 +784,9 @@ def main():
                    "cores": os.cpu_count(), "kind": "port", "cpu": cpu_model(),
                    "sample": f"{sample_steps} FP64 time steps of the {N_SIDE}^2 grid, "
                              f"OpenMP, reference host flags"}
+        ref_gpu = reference_gpu_baseline(fields)
+        if "value" in ref_gpu:
+            ref_gpu["speedup_fp32_over_reference_gpu"] = value / ws / ref_gpu["value"]
         line = {
             "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
@@ -788,6 +814,7 @@ def main():
                              "achieved": 32 * cells / (kms / 1e3) / 1e9,
                              "frac": 32 * cells / (kms / 1e3) / 1e9 / peak}},
             "cpu_baseline": cpu,
+            "reference_gpu": ref_gpu,
             "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": io_bytes,
                     "d2h_bytes_per_step": io_bytes,
                     "mode": "independent jobs on two alternating CudaData handles: job k+1's "

@@ -1,28 +1,11 @@
 """Golden time steps from the reference's own CUDA kernels (run on a GPU).
 
-oracle/Makefile's `ref-gpu` target compiles usnistgov/phasefield-precipitate-aging's
-src/parabola625.cu, src/nucleation.cu and src/discretization.cu where they lie
-into one sm_103a device module (oracle/_ref/ref_step.cubin; it needs the
-reference checkout, so it is built in the build container and carried to the
-GPU).  This script loads the module through the CUDA driver API (ctypes on
-libcuda), uploads the constants init_cuda uploads (src/data.cu:71-80: the
-5-point mask of src/mesh.cpp:187-196, D, kappa, omega, L) and runs the
-reference's update loop (src/main.cpp:289-321 with nucleation off) in its
-own launch order and shapes -- bx = by = 13, nm = 3 (src/main.cpp:229-231):
-
-  device_boundaries        src/discretization.cu:396-451 (10 fields)
-  device_fictitious        :128-173
-  fictitious_boundaries    :453-481
-  device_laplacian         :780-841 (shared tile (bx + nm) (by + nm) doubles)
-  device_laplacian_boundaries :524-548
-  device_evolution         :989-1020
-  swap of old / new        src/main.cpp:318-321
-
-The reference runs these on four streams ordered by events at every call;
-here they run in the same order on one stream, which computes the same
-values (the kernels of one call touch disjoint arrays).  Cases, all FP64
-(nucleation off), with the inputs of tests/golden/step2d.npz and
-step2d_refdt.npz and the 256 x 256 workload (ic.config1):
+The reference's kernels come from oracle/Makefile's `ref-gpu` target
+(oracle/_ref/ref_step.cubin) and run through oracle/ref_gpu.py, which
+launches them in the reference's own order and shapes (src/main.cpp:289-321,
+nucleation off).  Cases, all FP64, with the inputs of tests/golden/step2d.npz
+and step2d_refdt.npz and the 256 x 256 workload (ic.config1, stored with the
+output: host tanh differs in the last bits between machines):
 
   step   : step2d.npz's grid, KKS-stable dt, snapshots after 1, 10, 100, 400 steps
   refdt  : step2d_refdt.npz's grid, the reference's own dt rule, 50 steps
@@ -32,7 +15,6 @@ step2d_refdt.npz and the 256 x 256 workload (ic.config1):
                                                [--out tests/golden/ref_gpu_step2d.npz]
 """
 import argparse
-import ctypes
 import os
 import sys
 
@@ -44,170 +26,14 @@ sys.path.insert(0, os.path.join(REPO, "oracle"))
 sys.path.insert(0, os.path.join(REPO, "phasefield-precipitate-aging_gb300"))
 
 NAMES = ("cr", "nb", "pd", "pl")
-BX = BY = 13
-NM = 3
-
-# kernels of src/discretization.cu (C++ names; fp_t = double, src/type.h:23)
-K_BOUNDARY = b"_Z15boundary_kernelPdiii"
-K_FICT = (b"_Z21fictitious_gam_kernelPdS_S_S_S_S_iii", b"_Z21fictitious_del_kernelPdS_S_S_S_S_iii",
-          b"_Z21fictitious_lav_kernelPdS_S_S_S_S_iii")
-K_CONV = b"_Z18convolution_kernelPdS_iii"
-K_CH = b"_Z20cahn_hilliard_kernelPdS_S_S_iiid"
-K_AC = b"_Z17allen_cahn_kernelPdS_S_S_S_S_iiidd"
-
-
-class Driver:
-    """The few CUDA driver calls the script needs, through ctypes."""
-
-    def __init__(self, cubin):
-        cu = ctypes.CDLL("libcuda.so.1")
-        u64, sz, vp = ctypes.c_uint64, ctypes.c_size_t, ctypes.c_void_p
-        cu.cuModuleGetGlobal_v2.argtypes = [ctypes.POINTER(u64), ctypes.POINTER(sz), vp, ctypes.c_char_p]
-        cu.cuMemAlloc_v2.argtypes = [ctypes.POINTER(u64), sz]
-        cu.cuMemFree_v2.argtypes = [u64]
-        cu.cuMemsetD8_v2.argtypes = [u64, ctypes.c_ubyte, sz]
-        cu.cuMemcpyHtoD_v2.argtypes = [u64, vp, sz]
-        cu.cuMemcpyDtoH_v2.argtypes = [vp, u64, sz]
-        cu.cuModuleGetFunction.argtypes = [ctypes.POINTER(vp), vp, ctypes.c_char_p]
-        cu.cuLaunchKernel.argtypes = [vp] + [ctypes.c_uint] * 7 + [vp, ctypes.POINTER(vp), vp]
-        self.cu = cu
-        self.ck(cu.cuInit(0), "cuInit")
-        dev = ctypes.c_int()
-        self.ck(cu.cuDeviceGet(ctypes.byref(dev), 0), "cuDeviceGet")
-        self.ctx = vp()
-        self.ck(cu.cuDevicePrimaryCtxRetain(ctypes.byref(self.ctx), dev), "cuDevicePrimaryCtxRetain")
-        self.ck(cu.cuCtxSetCurrent(self.ctx), "cuCtxSetCurrent")
-        self.mod = vp()
-        self.ck(cu.cuModuleLoad(ctypes.byref(self.mod), cubin.encode()), "cuModuleLoad")
-        self.fn = {}
-
-    @staticmethod
-    def ck(r, what):
-        if r != 0:
-            raise RuntimeError(f"{what}: CUresult {r}")
-
-    def function(self, name):
-        if name not in self.fn:
-            f = ctypes.c_void_p()
-            self.ck(self.cu.cuModuleGetFunction(ctypes.byref(f), self.mod, name), name.decode())
-            self.fn[name] = f
-        return self.fn[name]
-
-    def set_constant(self, name, values):
-        ptr, size = ctypes.c_uint64(), ctypes.c_size_t()
-        self.ck(self.cu.cuModuleGetGlobal_v2(ctypes.byref(ptr), ctypes.byref(size), self.mod, name),
-                name.decode())
-        a = np.ascontiguousarray(values, dtype=np.float64).ravel()
-        if a.nbytes > size.value:
-            raise ValueError(f"{name.decode()} holds {size.value} bytes, not {a.nbytes}")
-        self.ck(self.cu.cuMemcpyHtoD_v2(ptr, a.ctypes.data, a.nbytes), "cuMemcpyHtoD")
-
-    def alloc(self, nbytes):
-        p = ctypes.c_uint64()
-        self.ck(self.cu.cuMemAlloc_v2(ctypes.byref(p), nbytes), "cuMemAlloc")
-        self.ck(self.cu.cuMemsetD8_v2(p, 0, nbytes), "cuMemsetD8")
-        return p
-
-    def free(self, p):
-        self.ck(self.cu.cuMemFree_v2(p), "cuMemFree")
-
-    def put(self, p, a):
-        a = np.ascontiguousarray(a, dtype=np.float64)
-        self.ck(self.cu.cuMemcpyHtoD_v2(p, a.ctypes.data, a.nbytes), "cuMemcpyHtoD")
-
-    def get(self, p, shape):
-        a = np.empty(shape, dtype=np.float64)
-        self.ck(self.cu.cuMemcpyDtoH_v2(a.ctypes.data, p, a.nbytes), "cuMemcpyDtoH")
-        return a
-
-    def launch(self, name, grid, block, shmem, args):
-        vals = []
-        for a in args:
-            if isinstance(a, ctypes.c_uint64):
-                vals.append(ctypes.c_uint64(a.value))
-            elif isinstance(a, int):
-                vals.append(ctypes.c_int(a))
-            else:
-                vals.append(ctypes.c_double(a))
-        params = (ctypes.c_void_p * len(vals))(*[ctypes.cast(ctypes.pointer(v), ctypes.c_void_p)
-                                                 for v in vals])
-        self.ck(self.cu.cuLaunchKernel(self.function(name), grid[0], grid[1], 1, block[0], block[1],
-                                       1, shmem, None, params, None), name.decode())
-
-    def sync(self):
-        self.ck(self.cu.cuCtxSynchronize(), "cuCtxSynchronize")
-
-
-def n_tiles(n, tile, nm):
-    """nTiles, src/discretization.cu:45-48 (float arithmetic as there)."""
-    return int(np.ceil(np.float32(n) / np.float32(tile - nm + 1)))
-
-
-def five_point_mask(dx, dy):
-    """five_point_Laplacian_stencil, src/mesh.cpp:187-196."""
-    m = np.zeros((3, 3))
-    m[0][1] = 1. / (dy * dy)
-    m[1][0] = 1. / (dx * dx)
-    m[1][1] = -2. * (dx * dx + dy * dy) / (dx * dx * dy * dy)
-    m[1][2] = 1. / (dx * dx)
-    m[2][1] = 1. / (dy * dy)
-    return m
-
-
-def run_reference(drv, fields, prm, steps):
-    """Snapshots of the reference's update loop after each count in `steps`."""
-    ny, nx = fields[0].shape
-    nb = nx * ny * 8
-    drv.set_constant(b"d_mask", five_point_mask(prm.dx, prm.dy))
-    drv.set_constant(b"d_DCr", list(prm.D_Cr))
-    drv.set_constant(b"d_DNb", list(prm.D_Nb))
-    drv.set_constant(b"d_Kapp", list(prm.kappa))
-    drv.set_constant(b"d_Omeg", list(prm.omega))
-    drv.set_constant(b"d_Lmob", list(prm.Lmob))
-    old = [drv.alloc(nb) for _ in range(4)]
-    new = [drv.alloc(nb) for _ in range(4)]
-    fict = [drv.alloc(nb) for _ in range(6)]  # Cr/Nb of gamma, delta, laves
-    for p, a in zip(old, fields):
-        drv.put(p, a)
-    grid = (n_tiles(nx, BX, NM), n_tiles(ny, BY, NM))
-    block = (BX, BY)
-    shmem = (BX + NM) * (BY + NM) * 8
-
-    def bc(p):
-        drv.launch(K_BOUNDARY, grid, block, 0, [p, nx, ny, NM])
-
-    out = {}
-    done = 0
-    for target in steps:
-        for _ in range(target - done):
-            for p in old + fict:  # device_boundaries
-                bc(p)
-            for k in range(3):  # device_fictitious
-                drv.launch(K_FICT[k], grid, block, 0, old + fict[2 * k:2 * k + 2] + [nx, ny, NM])
-            for p in fict:  # fictitious_boundaries
-                bc(p)
-            for src, dst in ((old[2], new[2]), (old[3], new[3]), (fict[0], new[0]),
-                             (fict[1], new[1])):  # device_laplacian
-                drv.launch(K_CONV, grid, block, shmem, [src, dst, nx, ny, NM])
-            for p in new:  # device_laplacian_boundaries
-                bc(p)
-            drv.launch(K_CH, grid, block, 0, [old[0], old[1], new[0], new[1], nx, ny, NM, prm.dt])
-            drv.launch(K_AC, grid, block, 0, [old[0], old[1], old[2], old[3], new[2], new[3],
-                                              nx, ny, NM, prm.alpha, prm.dt])
-            old, new = new, old
-        done = target
-        drv.sync()
-        out[target] = [drv.get(p, (ny, nx)) for p in old]
-    for p in old + new + fict:
-        drv.free(p)
-    return out
 
 
 def main():
     import oracle as O
+    from ref_gpu import CUBIN, Driver, run_reference
     from pfa_gb300 import ic
     ap = argparse.ArgumentParser()
-    ap.add_argument("--cubin", default=os.path.join(REPO, "oracle", "_ref", "ref_step.cubin"))
+    ap.add_argument("--cubin", default=CUBIN)
     ap.add_argument("--out", default=os.path.join(HERE, "ref_gpu_step2d.npz"))
     args = ap.parse_args()
     drv = Driver(args.cubin)
