@@ -43,6 +43,9 @@ K_FICT = (b"_Z21fictitious_gam_kernelPdS_S_S_S_S_iii", b"_Z21fictitious_del_kern
 K_CONV = b"_Z18convolution_kernelPdS_iii"
 K_CH = b"_Z20cahn_hilliard_kernelPdS_S_S_iiid"
 K_AC = b"_Z17allen_cahn_kernelPdS_S_S_S_S_iiidd"
+K_INIT_PRNG = b"_Z16init_prng_kernelP17curandStateXORWOWii"
+K_NUC = b"_Z17nucleation_kernelPdS_S_S_P17curandStateXORWOWiiidddddddd"
+PRNG_STATE_BYTES = 64  # >= sizeof(curandStateXORWOW) (48)
 
 
 class Driver:
@@ -229,3 +232,26 @@ def time_reference(drv, fields, prm, steps, warmup=2):
     for p in state[0] + state[1] + fict:
         drv.free(p)
     return t
+
+
+def run_reference_nucleation(drv, fields, sigma, unit_a, d, dt):
+    """One call of the reference's nucleation (device_init_prng, then
+    nucleation_kernel on the fields, src/discretization.cu:1022-1043,1079-1177)
+    with the spacing d = (dx, dy, dz) passed to the kernel as given; returns
+    the fields after it.  init_prng_kernel seeds each cell's XORWOW state from
+    clock(), so the draws differ from call to call: only statistics compare."""
+    ny, nx = fields[0].shape
+    nb = nx * ny * 8
+    f = [drv.alloc(nb) for _ in range(4)]
+    for p, a in zip(f, fields):
+        drv.put(p, a)
+    prng = drv.alloc(nx * ny * PRNG_STATE_BYTES)
+    grid = (n_tiles(nx, BX, NM), n_tiles(ny, BY, NM))
+    drv.launch(K_INIT_PRNG, grid, (BX, BY), 0, [prng, nx, ny])
+    drv.launch(K_NUC, grid, (BX, BY), 0, f + [prng, nx, ny, NM, sigma[0], sigma[1], unit_a, 0.0,
+                                              d[0], d[1], d[2], dt])
+    drv.sync()
+    out = [drv.get(p, (ny, nx)) for p in f]
+    for p in f + [prng]:
+        drv.free(p)
+    return out

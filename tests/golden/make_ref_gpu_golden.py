@@ -11,8 +11,14 @@ output: host tanh differs in the last bits between machines):
   refdt  : step2d_refdt.npz's grid, the reference's own dt rule, 50 steps
   config1: 256 x 256 (one stripe, four particles), KKS-stable dt, 1000 steps
 
+and, in ref_gpu_nucleation.npz, the event counts of the reference's own
+nucleation kernel (src/discretization.cu:1079-1177, clock-seeded curand) in
+four independent calls on a uniform enriched 512 x 512 grid whose nuclei
+cover one cell each.
+
     python tests/golden/make_ref_gpu_golden.py [--cubin oracle/_ref/ref_step.cubin]
                                                [--out tests/golden/ref_gpu_step2d.npz]
+                                               [--nuc-out tests/golden/ref_gpu_nucleation.npz]
 """
 import argparse
 import os
@@ -26,15 +32,24 @@ sys.path.insert(0, os.path.join(REPO, "oracle"))
 sys.path.insert(0, os.path.join(REPO, "phasefield-precipitate-aging_gb300"))
 
 NAMES = ("cr", "nb", "pd", "pl")
+# nucleation case: uniform enriched grid, P ~ 1e-3 per cell and phase
+NUC_SIDE = 512
+NUC_COMP = (0.2720, 0.1692)
+NUC_SIGMA = (0.05, 0.06)
+NUC_UNIT_A = 0.352e-9
+NUC_D = (2e-9, 2e-9, 1e-3)
+NUC_DT = 1e7
+NUC_CALLS = 4
 
 
 def main():
     import oracle as O
-    from ref_gpu import CUBIN, Driver, run_reference
+    from ref_gpu import CUBIN, Driver, run_reference, run_reference_nucleation
     from pfa_gb300 import ic
     ap = argparse.ArgumentParser()
     ap.add_argument("--cubin", default=CUBIN)
     ap.add_argument("--out", default=os.path.join(HERE, "ref_gpu_step2d.npz"))
+    ap.add_argument("--nuc-out", default=os.path.join(HERE, "ref_gpu_nucleation.npz"))
     args = ap.parse_args()
     drv = Driver(args.cubin)
     res = {}
@@ -55,6 +70,20 @@ def main():
             res[f"config1_s{k}_{n}"] = snap[j]
     np.savez_compressed(args.out, **res)
     print("reference GPU steps written to", args.out)
+    # nucleation: event counts of the reference's own kernel on a uniform
+    # enriched grid, single-cell nuclei (critical radius and scan radius
+    # below one cell), independent calls
+    f = ic.grid2d(NUC_SIDE, NUC_SIDE, seed=5, matrix=NUC_COMP, enrich=NUC_COMP, noise=0.0,
+                  stripes=[], n_particles=0)
+    counts = []
+    for _ in range(NUC_CALLS):
+        out = run_reference_nucleation(drv, f, NUC_SIGMA, NUC_UNIT_A, NUC_D, NUC_DT)
+        counts.append([int(np.count_nonzero(out[2] == 1.0)), int(np.count_nonzero(out[3] == 1.0))])
+    np.savez_compressed(args.nuc_out, counts=np.array(counts, dtype=np.int64),
+                        cells=np.array([f[0].size]), comp=np.array(NUC_COMP),
+                        sigma=np.array(NUC_SIGMA), unit_a=np.array([NUC_UNIT_A]),
+                        d=np.array(NUC_D), dt=np.array([NUC_DT]))
+    print("reference GPU nucleation counts", counts, "written to", args.nuc_out)
 
 
 if __name__ == "__main__":

@@ -1,6 +1,7 @@
 """GPU nucleation: Philox known answers, bit-exact event sets against the CPU
 replica, the reference-generated golden events, and the event rate against
-the reference's nucleation probability."""
+the reference's nucleation probability and its own nucleation kernel's
+event counts."""
 import numpy as np
 import pytest
 
@@ -122,6 +123,36 @@ def test_event_rate_matches_reference_probability(pfa, orc):
         k = sum(1 for e in events[0] if e[1] == ph)
         mean, sd = N * P[ph], np.sqrt(N * P[ph] * (1 - P[ph]))
         assert abs(k - mean) < 5 * sd, (ph, k, mean, sd)
+
+
+def test_event_rate_matches_reference_nucleation_kernel(pfa, orc):
+    """The same case the reference's own nucleation kernel ran on a GB300
+    (tests/golden/ref_gpu_nucleation.npz: uniform enriched grid, single-cell
+    nuclei): the event rate per phase is binomial with the oracle's P_nuc and
+    agrees with the reference kernel's rate over its four calls, within 5
+    sigma.  The reference also decides its ghost ring (514^2 cells); this
+    library decides interior cells only (512^2)."""
+    from pfa_gb300 import ic
+    from test_oracle import _ref_nuc_probabilities
+    g = golden("ref_gpu_nucleation.npz")
+    comp = tuple(float(v) for v in g["comp"])
+    side = int(round(np.sqrt(int(g["cells"][0])))) - 2
+    f = ic.grid2d(side, side, seed=5, matrix=comp, enrich=comp, noise=0.0, stripes=[],
+                  n_particles=0)
+    nuc = dict(sigma=tuple(float(v) for v in g["sigma"]), unit_a=float(g["unit_a"][0]),
+               d=tuple(float(v) for v in g["d"]), dt=float(g["dt"][0]))
+    P = _ref_nuc_probabilities(orc, g)
+    n_ours, n_ref = side * side, int(g["cells"][0])
+    calls = g["counts"].shape[0]
+    for seed in (3, 4):
+        _, events = _nucleate_once(pfa, f, nuc, seed=seed)
+        for ph in range(2):
+            k = sum(1 for e in events[0] if e[1] == ph)
+            m = n_ours * P[ph]
+            assert abs(k - m) < 5 * np.sqrt(m * (1 - P[ph])), (ph, k, m)
+            ref_rate = g["counts"][:, ph].sum() / (calls * n_ref)
+            sd = np.sqrt(P[ph] * (1 - P[ph]) * (1 / n_ours + 1 / (calls * n_ref)))
+            assert abs(k / n_ours - ref_rate) < 5 * sd, (ph, k / n_ours, ref_rate)
 
 
 def test_nucleation_in_the_step_loop(pfa):

@@ -147,3 +147,32 @@ def test_step_matches_reference_cuda_kernels(orc):
     assert max(field_err(got, fields_of(r, "refdt_s50"))) <= 1e-12
     got = orc.run2d(fields_of(r, "config1_ic"), prm, 1000)
     assert max(field_err(got, fields_of(r, "config1_s1000"))) <= 1e-12
+
+
+def _ref_nuc_probabilities(orc, g):
+    """The oracle's P_nuc (pinned to the reference's
+    nucleation_probability_sphere) for the reference-kernel nucleation case."""
+    x, y = (float(v) for v in g["comp"])
+    dx, dy, dz = (float(v) for v in g["d"])
+    dV = dx * dy * dz
+    va = 0.25 * float(g["unit_a"][0]) ** 3
+    dG = orc.g(0, [x], [y])[0]
+    dcc, dnn = orc.D(0, 0, [x], [y])[0], orc.D(1, 1, [x], [y])[0]
+    return [orc.nucleation_probability_sphere(x, y, dG, dcc, dnn, float(s), va, dV / va, dV,
+                                              float(g["dt"][0]))[1] for s in g["sigma"]]
+
+
+def test_reference_nucleation_kernel_rate_matches_oracle_probability(orc):
+    """Event counts of the reference's own nucleation kernel (clock-seeded
+    curand, run on a GB300 by tests/golden/make_ref_gpu_golden.py: uniform
+    enriched grid, single-cell nuclei, four calls) are binomial with the
+    oracle's P_nuc: each call and their sum within 5 sigma."""
+    g = golden("ref_gpu_nucleation.npz")
+    n = int(g["cells"][0])
+    P = _ref_nuc_probabilities(orc, g)
+    counts = g["counts"]
+    for ph in range(2):
+        assert 1e-4 < P[ph] < 1e-2, P
+        for k in list(counts[:, ph]) + [int(counts[:, ph].sum())]:
+            m = n * P[ph] * (len(counts) if k == counts[:, ph].sum() else 1)
+            assert abs(k - m) < 5 * np.sqrt(m * (1 - P[ph])), (ph, k, m)
