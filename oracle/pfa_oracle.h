@@ -1,9 +1,9 @@
 /*
  * pfa_oracle.h -- CPU oracle for the KKS Cr-Nb-Ni explicit time step.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker: the tests, the
- * smoke check and the CPU-baseline leg of the benchmark load it to compare
- * against (or to time beside) the CUDA library.  The product never links,
+ * TEST INFRASTRUCTURE ONLY.  The tests, the smoke check and the
+ * CPU-baseline leg of the benchmark load it to check the CUDA library's
+ * results against it (or to time it beside the library).  The product never links,
  * loads or calls it.
  *
  * It restates, in plain FP64 C, the semantics of the reference's step
