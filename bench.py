@@ -105,6 +105,16 @@ class ClockSampler:
                 "samples": len(rows)}
 
 
+def spin_up(grid, seconds=1.5):
+    """Untimed steps until `seconds` have passed, after the warm-up steps, so
+    that the timed region starts at steady clocks (a first run on a GPU fresh
+    from idle sampled 1987 MHz, the next one 2070)."""
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        grid.run(STEPS_PER_BENCH_STEP)
+        grid.sync()
+
+
 def measured_peak_hbm():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -726,6 +736,7 @@ def main():
     g.set_nucleation(**nuc_kw)
     g.run(args.warmup * STEPS_PER_BENCH_STEP)
     g.sync()
+    spin_up(g)
     barrier()
     with ClockSampler(local) as clk:
         ms = g.run_timed(args.steps * STEPS_PER_BENCH_STEP)
