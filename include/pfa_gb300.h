@@ -272,8 +272,11 @@ int pfa_summarize(struct CudaData* dev, double* out);
  * Allocates nothing: its scratch is a static device array holding one row of
  * partial sums per grid row, at most 16384 interior rows (ny - 2 <= 16384,
  * else PFA_EINVAL).  The first call on a device looks up that array's device
- * address (cudaGetSymbolAddress), so make it before any stream capture.
- * Calls share the array: calls that overlap on the GPU race. */
+ * address (cudaGetSymbolAddress), so make it before any stream capture; the
+ * address is kept for the life of the process, so do not call it on a device
+ * after a cudaDeviceReset of that device.  Calls share the array: calls that
+ * overlap on the GPU race.  A CUDA error already pending on the calling
+ * thread is reported (PFA_ECUDA) and left pending; nothing is launched. */
 int pfa_summarize_fields_noalloc(const double* conc_Cr, const double* conc_Nb,
                                  const double* phi_del, const double* phi_lav, int nx, int ny,
                                  double* out, void* stream);

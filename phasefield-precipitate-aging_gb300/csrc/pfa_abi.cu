@@ -337,24 +337,29 @@ static int run_chunk(CudaData* dev, State* s, int len, bool nuc_first, double al
   const int cur0 = s->cur;
   const uint64_t calls0 = s->calls;
   if (!exec) {
-    cudaGraph_t graph;
+    cudaGraph_t graph = nullptr;
     CK(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal));
     const int r = launch_chunk(dev, s, len, nuc_first, alpha, dt);
     const cudaError_t e = cudaStreamEndCapture(s->st, &graph);
-    if (r) return r;
-    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
-    CK(cudaGraphInstantiate(&exec, graph, 0));
-    cudaGraphDestroy(graph);
-    key.exec = exec;
-    if (s->graphs.size() >= 8) drop_graphs(s);
-    s->graphs.push_back(key);
     // capture only recorded the launches: restore the host-side bookkeeping
+    // (the ping-pong pointers and counters launch_chunk advanced), on every
+    // exit, so the handle still names the live fields when capture failed
     double** slots[8] = {&dev->conc_Cr_old, &dev->conc_Cr_new, &dev->conc_Nb_old,
                          &dev->conc_Nb_new, &dev->phi_del_old, &dev->phi_del_new,
                          &dev->phi_lav_old, &dev->phi_lav_new};
     for (int k = 0; k < 8; k++) *slots[k] = const_cast<double*>(static_cast<const double*>(p[k]));
     s->cur = cur0;
     s->calls = calls0;
+    if (r || e != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      return r ? r : cuda_fail(e, "cudaStreamEndCapture");
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ei != cudaSuccess) return cuda_fail(ei, "cudaGraphInstantiate");
+    key.exec = exec;
+    if (s->graphs.size() >= 8) drop_graphs(s);
+    s->graphs.push_back(key);
   }
   CK(cudaGraphLaunch(exec, s->st));
   // an even number of steps returns every ping-pong pointer to its place

@@ -15,6 +15,11 @@
 // The array is shared by every call: calls whose kernels overlap on the GPU
 // (different streams without ordering) race on it.  Nothing needs clearing
 // between calls: each call writes every row slot it later reads.
+//
+// The device address of the array is looked up once per device and kept for
+// the life of the process.  cudaDeviceReset unloads the library's device code
+// with the context, so the kept address is no longer valid: a process that
+// resets a device must not call this entry point on that device afterwards.
 #include <mutex>
 
 #include "pfa_device.cuh"
@@ -99,8 +104,15 @@ extern "C" int pfa_summarize_fields_noalloc(const double* conc_Cr, const double*
               "scratch holds one row of partial sums per grid row)");
     return PFA_EINVAL;
   }
+  // an error still pending from earlier work on this thread is not this
+  // call's: report it as such and leave before launching anything
+  cudaError_t e = cudaPeekAtLastError();
+  if (e != cudaSuccess) {
+    set_error(PFA_ECUDA, "pfa_summarize_fields_noalloc: a CUDA error was pending before the call");
+    return PFA_ECUDA;
+  }
   int device = 0;
-  cudaError_t e = cudaGetDevice(&device);
+  e = cudaGetDevice(&device);
   if (e != cudaSuccess || device < 0 || device >= kMaxDevices) {
     set_error(PFA_ECUDA, "pfa_summarize_fields_noalloc: no current device");
     return PFA_ECUDA;

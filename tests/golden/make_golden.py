@@ -171,7 +171,8 @@ def abi_symbols(refdir):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("PFA_REFERENCE") or
+                    os.path.join(os.path.dirname(REPO), "reference"))
     ap.add_argument("--only", nargs="*", help="write only these sets (e.g. energy summary)")
     args = ap.parse_args()
     subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "ref", f"REF={args.ref}"],
