@@ -146,11 +146,12 @@ def config1(seed=1):
     return grid2d(256, 256, seed)
 
 
-def config2(seed=2, n=4096):
-    """4096 x 4096, 16 stripes 64 wide at seeded columns, 64 particles R = 8."""
+def config2(seed=2, n=4096, n_particles=4):
+    """4096 x 4096 with config1's recipe (4 particles R = 8) and 16 stripes
+    64 wide at seeded columns; n_particles=64 gives the denser variant."""
     rng = np.random.default_rng(seed + 1000)
     stripes = sorted(int(v) for v in rng.integers(0, n - 64, 16))
-    return grid2d(n, n, seed, stripes=stripes, n_particles=64)
+    return grid2d(n, n, seed, stripes=stripes, n_particles=n_particles)
 
 
 def batch_sides(count=64, seed=3, lo=128, hi=2048):
