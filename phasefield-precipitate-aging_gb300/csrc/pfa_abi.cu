@@ -279,6 +279,7 @@ static int nucleate(CudaData* dev, State* s, double sig_d, double sig_l, double 
   a.seed = s->seed;
   a.call_ptr = s->call_dev;
   a.events = s->ev;
+  a.keys = reinterpret_cast<unsigned long long*>(s->ev + kNucCap);
   a.count = s->ev_count;
   a.status = s->ev_status;
   a.cap = kNucCap;
@@ -542,7 +543,7 @@ static int init_core(CudaData* dev, int nx, int ny, int nm, const double* mask,
                         &dev->phi_lav_old, &dev->phi_lav_new};
   for (auto p : main_f)
     if (alloc_field(p, n)) return PFA_ECUDA;
-  CK(cudaMalloc(reinterpret_cast<void**>(&s->ev), sizeof(NucEvent) * kNucCap));
+  CK(cudaMalloc(reinterpret_cast<void**>(&s->ev), nucleation_event_bytes()));
   CK(cudaMalloc(reinterpret_cast<void**>(&s->ev_count), 2 * sizeof(unsigned)));
   s->cand_cap = nucleation_cand_cap(n);
   CK(cudaMalloc(reinterpret_cast<void**>(&s->cand), sizeof(long long) * size_t(s->cand_cap)));

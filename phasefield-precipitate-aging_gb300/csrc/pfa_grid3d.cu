@@ -183,6 +183,7 @@ int nucleate(Grid3D* g) {
   a.seed = g->seed;
   a.call_ptr = g->call_dev;
   a.events = g->ev;
+  a.keys = reinterpret_cast<unsigned long long*>(g->ev + kNucCap);
   a.count = g->ev_count;
   a.status = g->ev_status;
   a.cap = kNucCap;
@@ -344,7 +345,7 @@ static int create3d(void** handle, int nx, int ny, int nz, const double* params,
   }
   CK3(cudaMalloc(reinterpret_cast<void**>(&g->sum_partial), sizeof(double) * kSumBlocks * 5));
   CK3(cudaMalloc(reinterpret_cast<void**>(&g->sum_out), sizeof(double) * 5));
-  CK3(cudaMalloc(reinterpret_cast<void**>(&g->ev), sizeof(NucEvent) * kNucCap));
+  CK3(cudaMalloc(reinterpret_cast<void**>(&g->ev), nucleation_event_bytes()));
   CK3(cudaMalloc(reinterpret_cast<void**>(&g->ev_count), 2 * sizeof(unsigned)));
   g->cand_cap = nucleation_cand_cap(size_t(g->Nx) * g->Ny * g->Nz);
   CK3(cudaMalloc(reinterpret_cast<void**>(&g->cand), sizeof(long long) * size_t(g->cand_cap)));

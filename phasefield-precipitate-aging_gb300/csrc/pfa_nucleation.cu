@@ -25,6 +25,7 @@
 #include <cstdint>
 
 #include "pfa_device.cuh"
+#include "pfa_nucleation.cuh"
 #include "pfa_nucleation.h"
 
 namespace pfa {
@@ -34,201 +35,9 @@ using namespace dev;
 namespace {
 
 template <class T>
-__device__ __forceinline__ double ld(const void* p, size_t i) {
-  return double(static_cast<const T*>(p)[i]);
-}
-
-// Storage index of reference cell (xx, yy, zz) (ghost-ring coordinates; zz
-// = 0 in 2D).  The FP32 form stores the interior only: a ghost cell reads its
-// mirror.
-__device__ __forceinline__ size_t stor(const NucArgs& a, int xx, int yy, int zz = 0) {
-  if (a.compact) {
-    const int cx = min(max(xx - 1, 0), a.Nx - 1), cy = min(max(yy - 1, 0), a.Ny - 1);
-    const int cz = a.is3d ? min(max(zz - 1, 0), a.Nz - 1) : 0;
-    return (size_t(cz) * a.Ny + cy) * a.pitch + cx;
-  }
-  return (size_t(zz) * (a.Ny + 2) + yy) * a.pitch + xx;
-}
-
-// Kahan compensation of field k at a cell of the FP32 form (value = f - c)
-__device__ __forceinline__ float comp_get(const NucArgs& a, size_t cell, int k) {
-  if (!a.comp) return 0.0f;
-  float4 c;
-  if (a.pack)
-    c = cq_unpack(static_cast<const uint2*>(a.comp)[cell]);
-  else
-    c = static_cast<const float4*>(a.comp)[cell];
-  return k == 0 ? c.x : (k == 1 ? c.y : (k == 2 ? c.z : c.w));
-}
-
-__device__ __forceinline__ void comp_set(const NucArgs& a, size_t cell, int k, float c) {
-  if (!a.comp) return;
-  if (a.pack)
-    static_cast<short*>(a.comp)[4 * cell + k] = short(cq_count(c, k < 2 ? kCqX : kCqP));
-  else
-    static_cast<float*>(a.comp)[4 * cell + k] = c;
-}
-
-// a field's value as stored (FP64, or the FP32 form's hi - c), exact
-template <class T>
-__device__ __forceinline__ double ldval(const NucArgs& a, int k, size_t cell) {
-  return ld<T>(a.f[k], cell * a.stride) - double(comp_get(a, cell, k));
-}
-
-// a phase field rounded to FP32 without touching the FP64 pipe in the FP32 form
-template <class T>
-__device__ __forceinline__ float ldphi_f(const NucArgs& a, int k, size_t cell) {
-  return float(static_cast<const T*>(a.f[k])[cell * a.stride]);
-}
-
-// composition-dependent diffusivities D_CrCr, D_NbNb (thermo/parabola625.c:1860-1894)
-__device__ void diffusivities(double X, double Y, double& dcc, double& dnn) {
-  const double xni = -X - Y + 1;
-  const double mNb = kMobPreNb * exp(-34.982563536715503 * Y * xni + 14.437947842988088 * Y);
-  const double mCr = kMobPreCr * exp(-7.1543718172640256 * X * xni + 3.3541967644499233 * X);
-  const double mNi = kMobPreNi * exp(-8.5221193705645018 * X * xni + 4.0036674816806448 * X -
-                                     442.62877981749585 * Y * xni - 0.82164267100913768 * Y);
-  const double s0 = -kHCrCr * X - kHCrNb * Y;  // column Cr
-  const double s1 = -kHCrNb * X - kHNbNb * Y;  // column Nb
-  dcc = -mNb * X * Y * (s0 + kHCrNbAddA) + mCr * X * (1 - X) * (s0 + kHCrCrAdd) - mNi * X * s0 * xni;
-  dnn = -mCr * X * Y * (s1 + kHCrNbAddB) + mNb * Y * (1 - Y) * (s1 + kHNbNbAdd) - mNi * Y * s1 * xni;
-}
-
-// nucleation_probability_sphere, thermo/nucleation.c:30-69 (src/nucleation.cu:30-70)
-__device__ void probability_sphere(double xCr, double xNb, double dG, double dcc, double dnn,
-                                   double sigma, double Vatom, double n_gam, double dV, double dt,
-                                   double& Rstar, double& P) {
-  const double sigma_cubed = sigma * sigma * sigma;
-  const double Zeldov = (Vatom * dG * dG) / (8. * kPi * sqrt(kKT * sigma_cubed));
-  const double Gstar = (16. * kPi * sigma_cubed) / (3. * dG * dG);
-  constexpr double a2 = kLatticeConst * kLatticeConst;
-  const double a4 = a2 * a2;
-  const double BstarCr = (3. * Gstar * dcc * xCr) / (sigma * a4);
-  const double BstarNb = (3. * Gstar * dnn * xNb) / (sigma * a4);
-  const double k1Cr = BstarCr * Zeldov * n_gam;
-  const double k1Nb = BstarNb * Zeldov * n_gam;
-  const double k2 = Gstar / kKT;
-  const double dc_Cr = -xCr + kXe[0][0];
-  const double dc_Nb = xNb - kXe[0][1];
-  const double JCr = k1Cr * exp(-k2 / dc_Cr);
-  const double JNb = k1Nb * exp(-k2 / dc_Nb);
-  const double P0 = exp(-dt * dV * (JCr + JNb));
-  P = 1. - P0;
-  Rstar = (2. * sigma) / dG;
-}
-
-// Upper bound, in FP32, of ln z with z = dt dV (J_Cr + J_Nb) for each phase;
-// +inf where no bound is attempted (compositions outside the simplex, or
-// above the gamma equilibrium composition, where the exponents change sign).
-// The diffusivities are bounded by the magnitudes of their three mobility
-// terms, so the bound holds whatever the signs of D_CrCr and D_NbNb:
-//   |D| <= 3 x 1.5e-20 x exp(max e) x 2.5e6     (prefactors, |s| + add)
-//   k1  <= 3 G* |D| / (sigma a^4) x Zeldovich x n_gam      (x <= 1)
-//   J_Cr + J_Nb <= 2 k1 exp(-k2 / max(dc_Cr, dc_Nb)),  k2 = G* / kT.
-// With G* = 16 pi sigma^3 / (3 dG^2) and Zeldovich ~ dG^2 the dG factors of
-// k1 cancel, so ln z <= lnC1 + max e - C2 / (dG^2 max dc) with the per-phase
-// constants lnC1, C2 of the host (NucArgs).
-__device__ void ln_z_bound(float X, float Y, const NucArgs& a, float lnz[2]) {
-  lnz[0] = lnz[1] = INFINITY;
-  const float dcCr = float(kXe[0][0]) - X, dcNb = Y - float(kXe[0][1]);
-  if (!(dcCr > 0.0f && dcNb > 0.0f && X > 0.0f && Y > 0.0f && X + Y < 1.0f)) return;
-  const float u = X - float(kXe[0][0]), v = Y - float(kXe[0][1]);
-  const float dG = float(kG[0][0]) * u * u + (float(kG[0][1]) * X - float(kG[0][2])) * v +
-                   float(kG[0][3]) * v * v;
-  if (!(dG > 1.0f)) return;
-  const float xni = 1.0f - X - Y;
-  const float eNb = -34.982563536715503f * Y * xni + 14.437947842988088f * Y;
-  const float eCr = -7.1543718172640256f * X * xni + 3.3541967644499233f * X;
-  const float eNi = -8.5221193705645018f * X * xni + 4.0036674816806448f * X -
-                    442.62877981749585f * Y * xni - 0.82164267100913768f * Y;
-  const float emax = fmaxf(eNb, fmaxf(eCr, eNi));
-  const float inv = __fdividef(1.0f, dG * dG * fmaxf(dcCr, dcNb));
-#pragma unroll
-  for (int ph = 0; ph < 2; ph++) {
-    const float l = a.lnC1[ph] + emax - a.C2[ph] * inv;
-    if (l == l) lnz[ph] = l;  // NaN stays +inf
-  }
-}
-
-// p(phi_del) + p(phi_lav) < 1e-10 as the reference's FP64 test decides it:
-// in FP32 when the FP32 sum is farther from the threshold than its error
-// bound (1e-6 of |p_del| + |p_lav|; p < 0 for phi < 0 allows cancellation),
-// in FP64 from the exact stored values otherwise.
-template <class T>
-__device__ __forceinline__ bool clear_at(const NucArgs& a, size_t s) {
-  const float fa = p32(ldphi_f<T>(a, 2, s)), fb = p32(ldphi_f<T>(a, 3, s));
-  const float q = fa + fb, err = 1e-6f * (fabsf(fa) + fabsf(fb)) + 1e-20f;
-  if (q - err > 1e-10f) return false;
-  if (q + err < 1e-10f) return true;
-  // the reference takes max(phi_pre, sum), which skips a NaN sum
-  return !(p64(ldval<T>(a, 2, s)) + p64(ldval<T>(a, 3, s)) >= 1e-10);
-}
-
-// Philox draw of a cell in a call: counter (cell, call), key = seed
-__device__ __forceinline__ uint4 nuc_draw(const NucArgs& a, long long idx) {
-  const unsigned long long call = *a.call_ptr;
-  return philox4x32_10(make_uint4(uint32_t(idx), uint32_t(uint64_t(idx) >> 32), uint32_t(call),
-                                  uint32_t(call >> 32)),
-                       make_uint2(uint32_t(a.seed), uint32_t(a.seed >> 32)));
-}
-
-// The FP64 decision of one clear cell (reference linear index idx, storage
-// index s) with its draw w: classical nucleation probability of each phase
-// against the draw; fills e and returns true on an event.
-template <class T>
-__device__ bool decide64(const NucArgs& a, long long idx, size_t s, uint4 w, NucEvent& e) {
-  const double X = ldval<T>(a, 0, s), Y = ldval<T>(a, 1, s);
-  const double u[2] = {u53(w.x, w.y), u53(w.z, w.w)};
-  const double dG = g64<0>(X, Y);
-  double dcc, dnn;
-  diffusivities(X, Y, dcc, dnn);
-  int mask = 0;
-  double rp[2] = {0.0, 0.0};
-#pragma unroll
-  for (int ph = 0; ph < 2; ph++) {
-    double Rstar = 0.0, P = 0.0;
-    probability_sphere(X, Y, dG, dcc, dnn, a.sigma[ph], a.Vatom, a.n_gam, a.dV, a.dt, Rstar, P);
-    if (Rstar > 0.) {
-      rp[ph] = Rstar / a.dx;
-      if (P - u[ph] > 0) {
-        if (rp[ph] <= kNucMaxRadius)
-          mask |= 1 << ph;
-        else
-          atomicExch(a.status, 2);  // nucleus wider than the paint limit: reported
-      }
-    }
-  }
-  if (!mask) return false;
-  e.cell = idx;
-  e.mask = mask;
-  e.pad = 0;
-  e.xcr = X;
-  e.xnb = Y;
-  e.r[0] = rp[0];
-  e.r[1] = rp[1];
-  return true;
-}
-
-// warp-aggregated append of the lanes' events (whole warp)
-__device__ __forceinline__ void append_events(const NucArgs& a, bool ev, const NucEvent& e) {
-  const unsigned bal = __ballot_sync(0xffffffffu, ev);
-  if (bal == 0) return;
-  const int lane = threadIdx.x & 31;
-  const int leader = __ffs(bal) - 1;
-  unsigned base = 0;
-  if (lane == leader) base = atomicAdd(a.count, unsigned(__popc(bal)));
-  base = __shfl_sync(0xffffffffu, base, leader);
-  if (ev) {
-    const unsigned slot = base + __popc(bal & ((1u << lane) - 1u));
-    if (slot < unsigned(a.cap)) a.events[slot] = e;
-  }
-}
-
-template <class T>
 __global__ void __launch_bounds__(256) k_nuc_decide(NucArgs a) {
   const int gx = blockIdx.x * 32 + (threadIdx.x & 31);
   const int gy = blockIdx.y * 8 + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
   const int nxr = a.Nx + 2, nyr = a.Ny + 2;
   bool need = false;  // the FP32 screen leaves this cell to the FP64 decision
   long long idx = 0;
@@ -274,64 +83,52 @@ __global__ void __launch_bounds__(256) k_nuc_decide(NucArgs a) {
     }
     if (clear) {
       s = stor(a, x, y, z);
-      const T Xs = static_cast<const T*>(a.f[0])[s * a.stride];
-      const T Ys = static_cast<const T*>(a.f[1])[s * a.stride];
-      // Screen in FP32 on the bound z_up of z = dt dV (J_Cr + J_Nb), which
-      // carries several nats of analytic slack; kMargin covers the FP32
-      // evaluation error many times over:
-      //  * z < 2^-55: FP64 exp(-z) is 1 or 1 - 2^-53, so P_nuc <= 2^-53 <= u for
-      //    every draw -- no event, no draw needed;
-      //  * else draw, and skip the FP64 path when u >= hi32 2^-32 (rounded
-      //    toward zero) >= P_up >= P_nuc.
-      constexpr float kMargin = 2.0f;
-      float lnz[2];
-      ln_z_bound(float(Xs), float(Ys), a, lnz);
-      const float lnz_max = fmaxf(lnz[0], lnz[1]) + kMargin;
-      if (!(lnz_max < -38.8f)) {  // ln 2^-56
-        w = nuc_draw(a, idx);
-        const float ulo[2] = {__uint2float_rz(w.x) * 0x1p-32f, __uint2float_rz(w.z) * 0x1p-32f};
-#pragma unroll
-        for (int ph = 0; ph < 2; ph++) {
-          const bool bounded = lnz[ph] + kMargin < 80.0f;
-          const float pup = 2.0f * __expf(fminf(lnz[ph] + kMargin, 80.0f)) + 0x1p-52f;
-          if (!bounded || !(ulo[ph] >= pup)) need = true;
-        }
-      }
+      need = nuc_screen(a, float(static_cast<const T*>(a.f[0])[s * a.stride]),
+                        float(static_cast<const T*>(a.f[1])[s * a.stride]), idx, w);
     }
   }
-  // Cells the screen cannot settle go to k_nuc_fp64 as a compact list: a warp
-  // issues the FP64 path if any of its lanes needs it, so in place a few such
-  // cells would cost whole warps.  Cells past the list's capacity decide here.
-  const unsigned nb = __ballot_sync(0xffffffffu, need);
-  if (nb == 0) return;
-  {
-    const int leader = __ffs(nb) - 1;
-    unsigned base = 0;
-    if (lane == leader) base = atomicAdd(a.count + 1, unsigned(__popc(nb)));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (need) {
-      const unsigned slot = base + __popc(nb & ((1u << lane) - 1u));
-      if (slot < unsigned(a.cand_cap)) {
-        a.cand[slot] = idx;
-        need = false;
-      }
-    }
-  }
-  bool ev = false;
-  NucEvent e;
-  if (need) ev = decide64<T>(a, idx, s, w, e);
-  append_events(a, ev, e);
+  nuc_list_or_decide<T>(a, need, idx, s, w);
 }
 
-// The FP64 decisions of the listed cells, 32 per warp.
+// The decisions of a call whose neighbourhood scan covers each cell alone
+// (R_scan <= 1 cell, as in the reference's geometry): one cell per thread,
+// one coalesced load of its values, the clear test and the first tier of the
+// screen inline (the rest of the screen, the FP64 path and the lists are
+// calls the few open lanes take), so the kernel stays small enough for high
+// occupancy, which hides the loads' latency.
+template <class T>
+__global__ void __launch_bounds__(256, 6) k_nuc_decide_own(NucArgs a) {
+  const int gx = blockIdx.x * 32 + (threadIdx.x & 31);
+  const int gy = blockIdx.y * 8 + (threadIdx.x >> 5);
+  bool need = false;
+  long long idx = 0;
+  size_t s = 0;
+  uint4 w = make_uint4(0, 0, 0, 0);
+  if (gx < a.Nx && gy < a.Ny) {
+    const int x = gx + 1, y = gy + 1, z = a.is3d ? int(blockIdx.z) + 1 : 0;
+    idx = ((long long)z * (a.Ny + 2) + y) * (a.Nx + 2) + x;
+    s = stor(a, x, y, z);
+    float v[4];
+    own_values<T>(a, s, v);
+    int clear = clear_fp32(v[2], v[3]);
+    if (clear < 0) clear = clear_exact(ldval<T>(a, 2, s), ldval<T>(a, 3, s));
+    if (clear) need = nuc_screen(a, v[0], v[1], idx, w);
+  }
+  nuc_list_or_decide<T>(a, need, idx, s, w);
+}
+
+// The FP64 decisions of the listed cells, 32 per warp.  Consecutive chunks
+// of 32 go to different CTAs (chunk c to CTA c mod gridDim.x): a short list
+// then spreads over the SMs instead of queueing on one SM's FP64 unit.
 template <class T>
 __global__ void __launch_bounds__(256) k_nuc_fp64(NucArgs a) {
   const unsigned n = min(a.count[1], unsigned(a.cand_cap));
   const int lane = threadIdx.x & 31;
-  const unsigned step = gridDim.x * blockDim.x;  // a multiple of 32: warps stay whole
+  const unsigned chunks = (n + 31) / 32;
+  const unsigned step = gridDim.x * (blockDim.x >> 5);
   const long long nxr = a.Nx + 2, nyr = a.Ny + 2;
-  for (unsigned b = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); b < n; b += step) {
-    const unsigned i = b + lane;
+  for (unsigned c = blockIdx.x + gridDim.x * (threadIdx.x >> 5); c < chunks; c += step) {
+    const unsigned i = 32 * c + lane;
     bool ev = false;
     NucEvent e;
     if (i < n) {
@@ -426,9 +223,27 @@ __device__ void paint(const NucArgs& a, const NucEvent& e, int ph) {
   }
 }
 
+// paint() of an event whose nuclei lie within its own cell (radius < 1
+// cell: the box is the cell, at distance 0 <= R): the precipitate's
+// composition and phase, delta before laves
+template <class T>
+__device__ void paint_own(const NucArgs& a, const NucEvent& e) {
+  const long long nxr = a.Nx + 2, nyr = a.Ny + 2;
+  const int x = int(e.cell % nxr);
+  const long long t = e.cell / nxr;
+  const int y = int(t % nyr), z = int(t / nyr);
+  const size_t s = stor(a, x, y, a.is3d ? z : 0);
+  constexpr double xdCr = kXe[1][0], xdNb = kXe[1][1], xlCr = kXe[2][0], xlNb = kXe[2][1];
+  for (int ph = 0; ph < 2; ph++)
+    if (e.mask & (1 << ph)) {
+      put<T>(a, 0, s, ph == 0 ? xdCr : xlCr);
+      put<T>(a, 1, s, ph == 0 ? xdNb : xlNb);
+      put<T>(a, 2 + ph, s, 1.0);
+    }
+}
+
 template <class T>
 __global__ void __launch_bounds__(1024) k_nuc_apply(NucArgs a) {
-  extern __shared__ unsigned long long s_key[];
   const unsigned n = *a.count;
   __syncthreads();
   // the decision kernel of this call has read the counter: advance it
@@ -438,29 +253,45 @@ __global__ void __launch_bounds__(1024) k_nuc_apply(NucArgs a) {
     if (threadIdx.x == 0) *a.status = 1;  // overflow: nothing painted
     return;
   }
+  // When every nucleus of the call has a radius below one cell, paint's box
+  // is the event's own cell, and events come from distinct cells: they touch
+  // disjoint cells, so they are painted at once, one thread each.
+  bool own = true;
+  for (unsigned t = threadIdx.x; t < n; t += blockDim.x) {
+    const NucEvent& e = a.events[t];
+    for (int ph = 0; ph < 2; ph++)
+      if ((e.mask & (1 << ph)) && !(e.r[ph] < 1.0)) own = false;
+  }
+  if (__syncthreads_and(own)) {
+    for (unsigned t = threadIdx.x; t < n; t += blockDim.x) paint_own<T>(a, a.events[t]);
+    return;
+  }
+  // bitonic sort of (cell, event index) keys, ascending, in the global
+  // scratch beside the events (no shared memory, so the launch asks for no
+  // large shared allocation on the calls, most of them, with few events)
+  unsigned long long* key = a.keys;
   unsigned m = 1;
   while (m < n) m <<= 1;
   for (unsigned t = threadIdx.x; t < m; t += blockDim.x)
-    s_key[t] = t < n ? ((unsigned long long)a.events[t].cell << kNucIdxBits) | t : ~0ull;
+    key[t] = t < n ? ((unsigned long long)a.events[t].cell << kNucIdxBits) | t : ~0ull;
   __syncthreads();
-  // bitonic sort, ascending
   for (unsigned k = 2; k <= m; k <<= 1)
     for (unsigned j = k >> 1; j > 0; j >>= 1) {
       for (unsigned t = threadIdx.x; t < m; t += blockDim.x) {
         const unsigned p = t ^ j;
         if (p > t) {
-          const unsigned long long u = s_key[t], v = s_key[p];
+          const unsigned long long u = key[t], v = key[p];
           const bool up = (t & k) == 0;
           if ((u > v) == up) {
-            s_key[t] = v;
-            s_key[p] = u;
+            key[t] = v;
+            key[p] = u;
           }
         }
       }
       __syncthreads();
     }
   for (unsigned q = 0; q < n; q++) {
-    const NucEvent e = a.events[s_key[q] & ((1ull << kNucIdxBits) - 1)];
+    const NucEvent e = a.events[key[q] & ((1ull << kNucIdxBits) - 1)];
     for (int ph = 0; ph < 2; ph++) {
       if (e.mask & (1 << ph)) paint<T>(a, e, ph);
       __syncthreads();
@@ -474,16 +305,23 @@ cudaError_t launch_nucleation(const NucArgs& a, cudaStream_t s) {
   cudaError_t err = cudaMemsetAsync(a.count, 0, 2 * sizeof(unsigned), s);
   if (err != cudaSuccess) return err;
   dim3 grid((a.Nx + 31) / 32, (a.Ny + 7) / 8, a.is3d ? a.Nz : 1);
-  const size_t smem = sizeof(unsigned long long) * size_t(kNucCap);
-  const int fp64_blocks = 152 * 4;  // grid-stride over the list (its length is on the device)
+  const bool own = a.scan_lo == 0 && a.scan_hi == 1;  // the scan covers each cell alone
+  // grid-stride over the FP64 list (its length is on the device): a CTA per SM
+  const int fp64_blocks = 152;
   if (a.is_f32) {
-    k_nuc_decide<float><<<grid, 256, 0, s>>>(a);
+    if (own)
+      k_nuc_decide_own<float><<<grid, 256, 0, s>>>(a);
+    else
+      k_nuc_decide<float><<<grid, 256, 0, s>>>(a);
     k_nuc_fp64<float><<<fp64_blocks, 256, 0, s>>>(a);
-    k_nuc_apply<float><<<1, 1024, smem, s>>>(a);
+    k_nuc_apply<float><<<1, 1024, 0, s>>>(a);
   } else {
-    k_nuc_decide<double><<<grid, 256, 0, s>>>(a);
+    if (own)
+      k_nuc_decide_own<double><<<grid, 256, 0, s>>>(a);
+    else
+      k_nuc_decide<double><<<grid, 256, 0, s>>>(a);
     k_nuc_fp64<double><<<fp64_blocks, 256, 0, s>>>(a);
-    k_nuc_apply<double><<<1, 1024, smem, s>>>(a);
+    k_nuc_apply<double><<<1, 1024, 0, s>>>(a);
   }
   return cudaGetLastError();
 }
@@ -517,27 +355,24 @@ const char* nucleation_constants(NucArgs& a, double dx, double dy, double dz, do
   long long m = (long long)std::floor(R2);
   if (double(m) >= R2) m--;  // strictly below R^2
   a.scan_r2 = int(m);
-  // constants of the FP32 screening bound (ln_z_bound):
-  // ln z <= lnC1 + max e - C2 / (dG^2 max dc)
+  // constants of the FP32 screen (ln_z_tier1, ln_z_tier2):
+  // ln k1_k = lnK + ln(D_kk x_k) (ln(dt dV) folded in), k2 = C2 / dG^2
   for (int ph = 0; ph < 2; ph++) {
     const double sg = a.sigma[ph], s3 = sg * sg * sg;
     const double a4 = std::pow(kLatticeConst, 4);
-    const double lnDpre = std::log(3.0 * 1.5e-20 * 2.5e6);            // |D| prefactor bound
-    const double lnG = std::log(16.0 * kPi * s3 / 3.0);                  // G* dG^2
+    const double lnG = std::log(16.0 * kPi * s3 / 3.0);                        // G* dG^2
     const double lnZ = std::log(a.Vatom / (8.0 * kPi * std::sqrt(kKT * s3)));  // Zeldovich / dG^2
-    a.lnC1[ph] = float(std::log(3.0) + lnG - std::log(sg) - std::log(a4) + lnDpre + lnZ +
-                       a.ln_ngam + std::log(2.0) + a.ln_dtdV);
+    const double lnK = std::log(3.0) + lnG - std::log(sg) - std::log(a4) + lnZ + a.ln_ngam +
+                       a.ln_dtdV;
+    a.lnK[ph] = float(lnK);
+    // |D_kk| <= 3 x 1.5e-20 x 2.5e6 exp(max e); two terms at most twice one
+    a.lnC1[ph] = float(lnK + std::log(3.0 * 1.5e-20 * 2.5e6) + std::log(2.0));
     a.C2[ph] = float(16.0 * kPi * s3 / (3.0 * kKT));
   }
   return nullptr;
 }
 
-cudaError_t nucleation_setup() {
-  const int smem = int(sizeof(unsigned long long) * kNucCap);
-  cudaError_t e = cudaFuncSetAttribute(k_nuc_apply<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_nuc_apply<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-}
+cudaError_t nucleation_setup() { return cudaSuccess; }
 
 // The FP32-form split exposed for its test (one block of doubles).
 __global__ void k_split_block(const double* in, float* hi, float* c, int n) {

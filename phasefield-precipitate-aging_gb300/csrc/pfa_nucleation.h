@@ -20,6 +20,11 @@ struct NucEvent {
   double r[2];     // nucleus radius in cells (delta, laves)
 };
 
+// bytes of a nucleation handle's event buffer: kNucCap events and their sort keys
+constexpr size_t nucleation_event_bytes() {
+  return (sizeof(NucEvent) + sizeof(unsigned long long)) * size_t(kNucCap);
+}
+
 struct NucArgs {
   void* f[4];          // x_Cr, x_Nb, phi_del, phi_lav (halo layout, row pitch `pitch`)
   void* comp;          // FP32 form: compensation records (value = f - c; set where
@@ -35,12 +40,13 @@ struct NucArgs {
   double dx;           // kernel spacing (the reference passes dx * nx here)
   double dV, Vatom, n_gam, dt, R_scan;
   double ln_dtdV, ln_ngam;
-  float lnC1[2], C2[2];  // per-phase constants of the FP32 screening bound
+  float lnK[2], lnC1[2], C2[2];  // per-phase constants of the FP32 screen (ln_z_tier1/2)
   int scan_lo, scan_hi;  // scan offsets i in [scan_lo, scan_hi) (from R_scan)
   int scan_r2;           // largest integer below R_scan^2
   uint64_t seed;
   unsigned long long* call_ptr;  // scratch: nucleation call counter (Philox counter word)
-  NucEvent* events;    // scratch: kNucCap events
+  NucEvent* events;    // scratch: kNucCap events, then kNucCap sort keys
+  unsigned long long* keys;  // = (unsigned long long*)(events + kNucCap)
   unsigned* count;     // scratch: [0] events, [1] cells listed for the FP64 decision
   int* status;         // scratch: 1 = overflow
   int cap;
@@ -57,7 +63,7 @@ inline int nucleation_cand_cap(size_t cells) {
 
 // Device scratch of a nucleation handle: events, counters, status, list.
 inline size_t nucleation_scratch_bytes(size_t cells) {
-  return sizeof(NucEvent) * kNucCap + 2 * sizeof(unsigned) + sizeof(int) +
+  return nucleation_event_bytes() + 2 * sizeof(unsigned) + sizeof(int) +
          sizeof(unsigned long long) + sizeof(long long) * size_t(nucleation_cand_cap(cells));
 }
 

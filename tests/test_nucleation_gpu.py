@@ -212,3 +212,85 @@ def test_fp32_nucleation_runs_and_paints(pfa):
     for cell, ph in events[0]:
         y, x = divmod(cell, out[0].shape[1])
         assert abs(out[2 + ph][y, x] - 1.0) < 1e-7
+
+
+# NUC_A's probabilities at a spacing where the neighbourhood scan covers each
+# cell alone (1.75 nm / dx <= 1, the decision kernel's one-load path): dx = dy
+# = 2 nm, dz scaled so that dV = dx dy dz is NUC_A's.  The nuclei are then
+# narrower than a cell, so the paint takes its parallel path as well.
+NUC_F = dict(sigma=(0.05, 0.05), unit_a=0.352e-9, d=(2e-9, 2e-9, 0.01), dt=1e6)
+
+
+def _enriched(nx, ny, seed):
+    from pfa_gb300 import ic
+    return ic.grid2d(nx, ny, seed=seed, matrix=(0.2720, 0.1692), enrich=(0.2720, 0.1692),
+                     stripes=[], n_particles=0)
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+@pytest.mark.parametrize("shape", [(48, 64), (131, 97)])
+def test_one_cell_scan_matches_replica(pfa, orc, shape, precision):
+    """A nucleation call after a step (pfa_run with a nucleation interval)
+    whose neighbourhood scan covers each cell alone: the same events as the
+    step followed by device_nucleation, bit-identical fields, and the events
+    and painted fields of the CPU replica run on the state after the step.
+    On these enriched grids most cells need the FP64 decision, more than the
+    list holds, so cells are also decided in place."""
+    from golden.make_golden import nuc_struct
+    ny, nx = shape
+    f = _enriched(nx, ny, seed=nx + ny)
+    p = pfa.model_params()
+    a = pfa.Grid2D(f, p, precision=precision)
+    a.set_nucleation(seed=9, geometry=pfa.NUC_FIXED_GEOMETRY, interval=1, **_nuc_kwargs(NUC_F))
+    a.run(1)
+    ev_a, out_a = a.events(), a.read()
+    a.close()
+    b = pfa.Grid2D(f, p, precision=precision)
+    b.set_nucleation(seed=9, geometry=pfa.NUC_FIXED_GEOMETRY)
+    pfa.check(b.L.pfa_device_evolution(b.ref, b.nx, b.ny, 3, 13, 13, p["alpha"], p["dt"]),
+              "device_evolution")
+    b.nucleate(**_nuc_kwargs(NUC_F))  # FP64: on *_new, before the caller's swap
+    if precision == "fp64":
+        b.swap()
+    ev_b, out_b = b.events(), b.read()
+    b.close()
+    assert len(ev_a) > nx * ny // 100
+    assert ev_a == ev_b
+    for x, y in zip(out_a, out_b):
+        assert np.array_equal(x, y)
+    c = pfa.Grid2D(f, p, precision=precision)
+    c.run(1)
+    state = c.read()
+    c.close()
+    want, ev, n = orc.nucleation2d(state, nuc_struct(NUC_F), 9, 0)
+    assert ev_a == [(e[0], e[1]) for e in ev]
+    tol = 2.0 ** -39 if precision == "fp32" else 0.0  # FP32: a 16-bit compensation count
+    for x, y in zip(out_a, want):
+        assert np.max(np.abs(x[1:-1, 1:-1] - y[1:-1, 1:-1])) <= tol
+
+
+def test_one_cell_scan_in_the_step_loop(pfa):
+    """pfa_run with a nucleation interval (replayed from a graph) equals the
+    per-step loop with device_nucleation calls, bit for bit, over 35 steps
+    and 4 calls, in the FP32 form."""
+    from pfa_gb300 import ic
+    f = ic.grid2d(96, 64, seed=5, matrix=(0.2600, 0.1680), enrich=(0.2720, 0.1692),
+                  stripes=[30], stripe_width=24, n_particles=1, radius=5.0)
+    p = pfa.model_params()
+    a = pfa.Grid2D(f, p, precision="fp32")
+    a.set_nucleation(seed=5, geometry=pfa.NUC_FIXED_GEOMETRY, interval=10, **_nuc_kwargs(NUC_F))
+    a.run(35)
+    b = pfa.Grid2D(f, p, precision="fp32")
+    b.set_nucleation(seed=5, geometry=pfa.NUC_FIXED_GEOMETRY)
+    calls = 0
+    for k in range(35):
+        pfa.check(b.L.pfa_device_evolution(b.ref, b.nx, b.ny, 3, 13, 13, p["alpha"], p["dt"]),
+                  "device_evolution")
+        if k % 10 == 0:
+            b.nucleate(**_nuc_kwargs(NUC_F))
+            calls += len(b.events())
+    assert calls > 0
+    for x, y in zip(a.read(), b.read()):
+        assert np.array_equal(x, y, equal_nan=True)
+    a.close()
+    b.close()
