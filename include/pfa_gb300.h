@@ -164,6 +164,14 @@ int pfa3d_set_nucleation(void* handle, uint64_t seed, int interval, double sigma
  * cell = (z ny + y) nx + x in the ghost-ring layout; returns the count */
 int pfa3d_last_nucleation_events(void* handle, int64_t* cells, int32_t* phases, int cap);
 int pfa3d_destroy(void* handle);
+/* For tests of the failure path only: in the next pfa3d_run of this FP32
+ * handle, the first CTA of the step kernel neither arms nor issues the
+ * staging copy of interior plane `plane`, so its bounded wait runs out
+ * (after about a second); the CTA then stops and drains its other copies,
+ * and pfa3d_sync / pfa3d_read report PFA_ECUDA ("a TMA staging wait gave
+ * up") once and clear it.  That run's result is not meaningful; later runs
+ * are normal.  No counterpart in the reference. */
+int pfa3d_test_skip_plane(void* handle, int plane);
 
 /* ---- batches of 2D grids (continuous batching) ----
  * No counterpart in the reference, which runs one grid per process

@@ -20,6 +20,33 @@ extern "C" {
 
 double ref_p(double x) { return p(x); }
 double ref_pprime(double x) { return pPrime(x); }
+double ref_tanh_interp(double r, double w) { return tanh_interp(r, w); }
+
+/* embed_OPC (src/alloy625.cpp:262-294) on a 2D grid in the ghost-ring layout
+ * (rows of nx doubles, f = x_Cr, x_Nb, phi_del, phi_lav), seed centre
+ * (cx, cy) in array coordinates, restated without MMSP: over the box
+ * |i|, |j| <= int(R + 4 w / meshres), phi = tanh_interp(meshres (r - R), w / 2)
+ * with the reference's compiled tanh_interp and p, phase field pid (2 or 3)
+ * set to phi, compositions blended toward (par_cr, par_nb) by p(phi). */
+void ref_embed_opc(double* f[4], int nx, int ny, int cx, int cy, double par_cr, double par_nb,
+                   double R_precip, int pid, double meshres, double ifce_width)
+{
+	const int R = (int)(R_precip + 4 * ifce_width / meshres);
+	for (int i = -R; i < R + 1; i++)
+		for (int j = -R; j < R + 1; j++) {
+			const int x = cx + i, y = cy + j;
+			if (x < 0 || x >= nx || y < 0 || y >= ny) continue;
+			const size_t k = (size_t)y * nx + x;
+			const double xCr = f[0][k], xNb = f[1][k];
+			const double r = sqrt((double)(i * i + j * j));
+			const double z = meshres * (r - R_precip);
+			const double phi = tanh_interp(z, ifce_width / 2);
+			const double pgam = 1.0 - p(phi);
+			f[pid][k] = phi;
+			f[0][k] = p(phi) * par_cr + pgam * xCr;
+			f[1][k] = p(phi) * par_nb + pgam * xNb;
+		}
+}
 
 double ref_fict(int phase, int comp, double a, double b, double c, double d, double e)
 {

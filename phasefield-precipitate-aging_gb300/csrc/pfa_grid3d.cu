@@ -52,6 +52,7 @@ struct Grid3D {
   unsigned long long* call_dev = nullptr;  // Philox call counter
   long long* cand = nullptr;               // cells left to the FP64 nucleation decision
   int cand_cap = 0;
+  int skip_plane = -1;  // tests only (pfa3d_test_skip_plane): the next run's skipped plane
 };
 
 int err(int code, const char* what) {
@@ -125,6 +126,7 @@ int step(Grid3D* g) {
     a.out[1] = g->B[n];
     a.pitch = g->pitch32;
     a.status = g->ev_status;
+    a.skip_plane = g->skip_plane;
     CK3(launch_step3d(a, false, &g->tm[c], g->st));
   }
   g->cur = n;
@@ -211,14 +213,22 @@ int graph_chunk(Grid3D* g, int len, bool nuc_first) {
     if (e.len == len && e.nuc_first == int(nuc_first) && e.cur == g->cur) exec = e.exec;
   if (!exec) {
     const int cur0 = g->cur;
-    cudaGraph_t graph;
+    cudaGraph_t graph = nullptr;
     CK3(cudaStreamBeginCapture(g->st, cudaStreamCaptureModeThreadLocal));
     const int r = chunk(g, len, nuc_first);
     const cudaError_t e = cudaStreamEndCapture(g->st, &graph);
-    if (r) return r;
-    if (e != cudaSuccess) return cuda_err(e, "cudaStreamEndCapture");
-    CK3(cudaGraphInstantiate(&exec, graph, 0));
+    if (r || e != cudaSuccess) {
+      // nothing ran: the ping-pong index goes back to the live buffers
+      g->cur = cur0;
+      if (graph) cudaGraphDestroy(graph);
+      return r ? r : cuda_err(e, "cudaStreamEndCapture");
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
     cudaGraphDestroy(graph);
+    if (ei != cudaSuccess) {
+      g->cur = cur0;
+      return cuda_err(ei, "cudaGraphInstantiate");
+    }
     if (g->graphs.size() >= 8) {
       cudaGraphExecDestroy(g->graphs.front().exec);
       g->graphs.erase(g->graphs.begin());
@@ -255,6 +265,14 @@ int run(Grid3D* g, int nsteps) {
     } else {
       len = std::min(nsteps, 100);
     }
+    if (g->skip_plane >= 0) {
+      // a test run with a skipped plane goes outside the graphs, which are
+      // kept for normal runs
+      if (int r = chunk(g, len, nuc_first)) return r;
+      g->step_counter += uint64_t(len);
+      nsteps -= len;
+      continue;
+    }
     if (len % 2) {
       // one step outside the graphs, so that they see an even count
       if (int r = chunk(g, 1, nuc_first)) return r;
@@ -269,6 +287,7 @@ int run(Grid3D* g, int nsteps) {
       nsteps -= len;
     }
   }
+  g->skip_plane = -1;
   return g->nuc_interval > 0 ? check_status(g) : 0;
 }
 
@@ -458,6 +477,15 @@ int pfa3d_run_timed(void* handle, int nsteps, float* ms) {
   cudaEventDestroy(b);
   if (ms) *ms = t;
   return r;
+}
+
+int pfa3d_test_skip_plane(void* handle, int plane) {
+  Grid3D* g = static_cast<Grid3D*>(handle);
+  if (!g) return err(PFA_ESTATE, "pfa3d_test_skip_plane: null handle");
+  if (g->precision == PFA_FP64) return err(PFA_EINVAL, "pfa3d_test_skip_plane: FP32 form only");
+  if (plane < 0 || plane >= g->Nz) return err(PFA_EINVAL, "pfa3d_test_skip_plane: plane");
+  g->skip_plane = plane;
+  return 0;
 }
 
 int pfa3d_sync(void* handle) {

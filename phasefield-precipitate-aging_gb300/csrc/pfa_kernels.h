@@ -108,6 +108,9 @@ struct Step3DArgs {
   FastCoef k;
   float dtD[2][2], dtL[2], om2[2], alpha2, kap[2], idx2f[3];
   int* status;          // FP32 form: set to 3 when a staging wait gave up (may be null)
+  int skip_plane;       // tests only: CTA (0, 0, 0) neither arms nor issues the
+                        // copies of this interior plane (>= 0), so its wait runs
+                        // out; negative: none (plane -1 is the ring's lower halo)
 };
 
 // TMA descriptors of one FP32-form record pair (A: the float4 records as an

@@ -284,6 +284,8 @@ static_assert(kSlotA % 128 == 0 && kSlotB % 128 == 0 && (kRing3 * kSlotA) % 128 
               "ring slots must stay 128-byte aligned");
 constexpr size_t kSmem3 = sizeof(Smem3) + 128;  // + slack to align the base to 128 B
 
+// SKIP: the instantiation with the test hook (Step3DArgs::skip_plane)
+template <bool SKIP>
 __global__ void __launch_bounds__(32 * kW)
     k_stream3d_f32(Step3DArgs a, const __grid_constant__ Tma3 t) {
   extern __shared__ unsigned char smem_raw[];
@@ -314,8 +316,17 @@ __global__ void __launch_bounds__(32 * kW)
   // phase (p - z0 + 1) >> 2; planes past z1 are never issued.  The slot
   // arguments below are compile-time constants.
   int last[kRing3] = {-2, -2, -2, -2};  // thread 0: last plane issued into each slot
+  // A thread whose wait gave up stops waiting (later waits give up after
+  // their first polls; it computes from whatever the ring holds and the
+  // handle reports the failure); thread 0, once its own wait gave up, issues
+  // nothing more, so the copies in flight are exactly those its final drain
+  // waits for.  SKIP: the test hook that withholds one plane's copies in
+  // the first CTA.
+  bool gave_up = false;
+  const bool skip =
+      SKIP && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && a.skip_plane >= 0;
   auto issue = [&](int p, int sl) {
-    if (tid == 0 && p <= z1) {
+    if (tid == 0 && p <= z1 && !gave_up && !(skip && p == a.skip_plane)) {
       const int zc = min(max(p, 0), a.Nz - 1);
       tma::proxy_fence();  // the slot's earlier reads (ordered by the barrier) come first
       tma::bar_arrive_tx(bar0 + 8 * sl, kTxPlane);
@@ -324,9 +335,10 @@ __global__ void __launch_bounds__(32 * kW)
       last[sl] = p;
     }
   };
-  bool gave_up = false;
   auto wait = [&](int p, int sl) {
-    if (!tma::bar_wait(bar0 + 8 * sl, uint32_t((p - z0 + 1) >> 2) & 1u)) gave_up = true;
+    if (!tma::bar_wait(bar0 + 8 * sl, uint32_t((p - z0 + 1) >> 2) & 1u,
+                       gave_up ? 0ull : tma::kWaitNs))
+      gave_up = true;
   };
   auto fetch = [&](int sl) {
     const float4 v = sm.ra[sl][by][bx];
@@ -465,7 +477,7 @@ cudaError_t query3() {
     if (F64)
       e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_stream3d<true>, 32 * kW, 0);
     else
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_stream3d_f32, 32 * kW, kSmem3);
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_stream3d_f32<false>, 32 * kW, kSmem3);
   }
   g_resident3[F64] = sms * (per > 0 ? per : 1);
   return e;
@@ -474,8 +486,11 @@ cudaError_t query3() {
 }  // namespace
 
 cudaError_t prepare_step3d() {
-  cudaError_t e = cudaFuncSetAttribute(k_stream3d_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaError_t e = cudaFuncSetAttribute(k_stream3d_f32<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        int(kSmem3));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_stream3d_f32<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             int(kSmem3));
   if (e == cudaSuccess) e = query3<true>();
   return e == cudaSuccess ? query3<false>() : e;
 }
@@ -523,7 +538,10 @@ cudaError_t launch_step3d(Step3DArgs a, bool f64, const Tma3* t, cudaStream_t s)
     k_stream3d<true><<<grid, 32 * kW, 0, s>>>(a);
   } else {
     if (!t) return cudaErrorInvalidValue;
-    k_stream3d_f32<<<grid, 32 * kW, kSmem3, s>>>(a, *t);
+    if (a.skip_plane >= 0)
+      k_stream3d_f32<true><<<grid, 32 * kW, kSmem3, s>>>(a, *t);
+    else
+      k_stream3d_f32<false><<<grid, 32 * kW, kSmem3, s>>>(a, *t);
   }
   return cudaGetLastError();
 }

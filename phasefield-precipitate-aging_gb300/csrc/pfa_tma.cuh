@@ -3,8 +3,9 @@
 //
 // One thread of a CTA arms a barrier with the bytes a plane's copies deliver
 // and issues the tiled copies; every thread that reads the plane waits on
-// the barrier's phase.  Waits are bounded: after kWaitLimit polls the wait
-// gives up and reports it, so a copy that never lands cannot hold the GPU.
+// the barrier's phase.  Waits are bounded: after kWaitNs (one second of the
+// global timer) or kWaitLimit polls the wait gives up and reports it, so a
+// copy that never lands cannot hold the GPU.
 #pragma once
 
 #include <cstdint>
@@ -12,7 +13,8 @@
 namespace pfa {
 namespace tma {
 
-constexpr uint32_t kWaitLimit = 1u << 22;  // polls of mbarrier.try_wait before giving up
+constexpr uint32_t kWaitLimit = 1u << 22;       // polls of mbarrier.try_wait before giving up
+constexpr uint64_t kWaitNs = 1000000000ull;     // or this long (ns), whichever comes first
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
   return uint32_t(__cvta_generic_to_shared(p));
@@ -39,21 +41,41 @@ __device__ __forceinline__ void bar_arrive_tx(uint32_t bar, uint32_t bytes) {
                : "memory");
 }
 
-// true once the phase with this parity has completed; false after
-// kWaitLimit polls
-__device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity) {
+// nanoseconds of the GPU's global timer
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ bool bar_try(uint32_t bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n"
+      ".reg .pred P;\n"
+      "mbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2;\n"
+      "selp.u32 %0, 1, 0, P;\n"
+      "}\n"
+      : "=r"(done)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
+// true once the phase with this parity has completed; false when it has not
+// after limit_ns of the global timer or kWaitLimit polls, whichever comes
+// first (limit_ns 0: after the first 64 polls)
+__device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity,
+                                         uint64_t limit_ns = kWaitNs) {
+  // a copy in flight usually lands within these polls: the clock is read
+  // only for waits that outlast them
+  for (int i = 0; i < 64; i++)
+    if (bar_try(bar, parity)) return true;
+  if (limit_ns == 0) return false;
+  const uint64_t t0 = global_ns();
   for (uint32_t i = 0; i < kWaitLimit; i++) {
-    uint32_t done;
-    asm volatile(
-        "{\n"
-        ".reg .pred P;\n"
-        "mbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2;\n"
-        "selp.u32 %0, 1, 0, P;\n"
-        "}\n"
-        : "=r"(done)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    if (done) return true;
+    if (bar_try(bar, parity)) return true;
+    if (global_ns() - t0 > limit_ns) return false;
   }
   return false;
 }

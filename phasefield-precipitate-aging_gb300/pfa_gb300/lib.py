@@ -156,6 +156,7 @@ def load():
         "pfa3d_upload_async": (_i, [ctypes.c_void_p, _dp, _dp, _dp, _dp]),
         "pfa3d_summarize": (_i, [ctypes.c_void_p, _dp]),
         "pfa3d_destroy": (_i, [ctypes.c_void_p]),
+        "pfa3d_test_skip_plane": (_i, [ctypes.c_void_p, _i]),
         "pfa3d_footprint": (ctypes.c_size_t, [_i, _i, _i, _i]),
         "pfa3d_sync": (_i, [ctypes.c_void_p]),
         "pfa3d_summarize_energy": (_i, [ctypes.c_void_p, _d, _dp]),

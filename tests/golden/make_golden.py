@@ -140,6 +140,57 @@ def free_energy(ref):
                                          prm.omega[0], prm.omega[1], 1.07e11]))
 
 
+IC_RECIPES = [
+    # particles embedded with embed_OPC's box and overwrite (particle_mode 1),
+    # integer centres as the reference's (MMSP grid positions), boxes inside
+    # the interior; overlapping boxes test the order of embedding
+    dict(nx=60, ny=44, nz=0, matrix=(0.3041, 0.0235), enrich=(0.2720, 0.1692), noise=0.002,
+         seed=7, bands=[(20, 36)], dx=5e-9, width=10e-9, particle_mode=1,
+         particles=[(16.0, 14.0, 0.0, 4.0, 0), (30.0, 22.0, 0.0, 5.5, 1),
+                    (42.0, 28.0, 0.0, 3.0, 0)]),
+    dict(nx=50, ny=50, nz=0, matrix=(0.2900, 0.0220), enrich=(0.2600, 0.1700), noise=0.0,
+         seed=8, bands=[], dx=2e-9, width=10e-9, particle_mode=1,
+         particles=[(25.0, 25.0, 0.0, 6.0, 1)]),
+]
+
+
+def initial_conditions(ref):
+    """embed_OPC (src/alloy625.cpp:262-294) with the reference's compiled
+    tanh_interp (thermo/nucleation.c:12-16) and p (thermo/parabola625.c),
+    applied to the recipe's particle-free fields, for the recipes above; and
+    tanh_interp itself on a set of distances and widths."""
+    import ctypes
+    out = {}
+    dp = ctypes.POINTER(ctypes.c_double)
+    emb = ref.lib.ref_embed_opc
+    emb.restype = None
+    emb.argtypes = [dp * 4] + [ctypes.c_int] * 4 + [ctypes.c_double] * 3 + [ctypes.c_int] + \
+        [ctypes.c_double] * 2
+    rxe = ref.lib.ref_xe  # the reference's equilibrium compositions (phase 1 delta, 2 laves)
+    rxe.restype = ctypes.c_double
+    rxe.argtypes = [ctypes.c_int, ctypes.c_int]
+    xe = [(rxe(1, 0), rxe(1, 1)), (rxe(2, 0), rxe(2, 1))]
+    for n, rec in enumerate(IC_RECIPES):
+        base = dict(rec, particles=[])
+        f = [np.ascontiguousarray(a) for a in O.ic_fields(base)]
+        ny, nx = f[0].shape
+        for (x, y, _z, R, ph) in rec["particles"]:
+            emb((dp * 4)(*[a.ctypes.data_as(dp) for a in f]), nx, ny, int(x) + 1, int(y) + 1,
+                xe[ph][0], xe[ph][1], R, 2 + ph, rec["dx"], rec["width"])
+        for a in f:  # the recipe's ghost ring: the mirror of the interior
+            ic.mirror_halo(a)
+        for j, name in enumerate(("cr", "nb", "pd", "pl")):
+            out[f"r{n}_{name}"] = f[j]
+    ti = ref.lib.ref_tanh_interp
+    ti.restype = ctypes.c_double
+    ti.argtypes = [ctypes.c_double, ctypes.c_double]
+    r = np.linspace(-3e-8, 3e-8, 241)
+    w = np.array([2.5e-9, 5e-9, 1e-8])
+    out["tanh_r"], out["tanh_w"] = r, w
+    out["tanh_v"] = np.array([[ti(a, b) for a in r] for b in w])
+    np.savez_compressed(os.path.join(HERE, "ic_embed.npz"), **out)
+
+
 def abi_symbols(refdir):
     """Mangled names the reference's caller links against: compile a stub
     that calls every host entry point through the reference's own headers."""
@@ -181,7 +232,8 @@ def main():
     rng = np.random.default_rng(20261203)
     sets = {"energies": lambda: energies(ref, rng), "steps": lambda: steps(ref),
             "nucleation": lambda: nucleation(ref), "summary": lambda: summary(ref),
-            "energy": lambda: free_energy(ref), "abi": lambda: abi_symbols(args.ref)}
+            "energy": lambda: free_energy(ref), "abi": lambda: abi_symbols(args.ref),
+            "ic": lambda: initial_conditions(ref)}
     for name, fn in sets.items():
         if not args.only or name in args.only:
             fn()

@@ -160,3 +160,31 @@ def test_3d_async_transfers_keep_order(pfa):
         x.close()
     for k in range(len(jobs)):
         assert all(np.array_equal(a, b) for a, b in zip(host_out[k], want[k])), k
+
+
+def test_staging_wait_that_runs_out_is_reported(pfa):
+    """The bounded wait of the FP32 3D step's TMA ring: with one plane's copy
+    withheld (pfa3d_test_skip_plane: the first CTA neither arms nor issues
+    it), that CTA's wait runs out after about a second, the CTA stops and
+    drains its other copies, and the handle reports PFA_ECUDA once (a TMA
+    staging wait gave up).  The context stays usable: the same handle, given
+    its fields again, then runs bit for bit like a fresh one."""
+    from pfa_gb300 import ic
+    f = ic.grid3d(64, 48, 40, seed=21, slab=12, n_particles=2, radius=4.0)
+    p = pfa.model_params(dim=3)
+    L = pfa.load()
+    g = pfa.Grid3D(f, p, precision="fp32")
+    pfa.check(L.pfa3d_test_skip_plane(g.h, 1), "pfa3d_test_skip_plane")
+    g.run(1)
+    with pytest.raises(pfa.PfaError, match="gave up"):
+        g.sync()
+    L.pfa_clear_error()
+    g.sync()  # reported once
+    g.upload(f)
+    g.run(6)
+    ref = pfa.Grid3D(f, p, precision="fp32")
+    ref.run(6)
+    for a, b in zip(g.read(), ref.read()):
+        assert np.array_equal(a, b)
+    g.close()
+    ref.close()

@@ -135,3 +135,26 @@ def test_oracle_reference_profile_and_embedding(orc):
     r2 = dict(r, particles=r["particles"] + [(300.0, 30.0, 0.0, 1.0, 0)])
     g = O.ic_fields(r2)
     assert g[2][1 + 30, 1 + 306] < f[2][1 + 30, 1 + 306]
+
+
+def test_oracle_embedding_matches_reference_code(orc):
+    """The oracle's particles in embed_OPC's mode against embed_OPC's loop
+    (src/alloy625.cpp:262-294) run with the reference's own compiled
+    tanh_interp (thermo/nucleation.c:12-16), p and equilibrium compositions
+    (thermo/parabola625.c) on the same particle-free fields
+    (tests/golden/ic_embed.npz, tests/golden/make_golden.py): overlapping
+    boxes, two spacings.  The oracle evaluates p in another order of
+    operations, hence a few ulps."""
+    import oracle as O
+    from conftest import golden
+    from golden.make_golden import IC_RECIPES
+    g = golden("ic_embed.npz")
+    for n, rec in enumerate(IC_RECIPES):
+        got = O.ic_fields(rec, orc)
+        for j, name in enumerate(("cr", "nb", "pd", "pl")):
+            want = g[f"r{n}_{name}"]
+            assert np.max(np.abs(got[j] - want)) <= 1e-15, (n, name)
+            assert np.array_equal(got[j] == 0.0, want == 0.0)
+    # the profile itself: tanh_interp(r, w) = 0.5 - 0.5 tanh(r / w)
+    prof = 0.5 - 0.5 * np.tanh(g["tanh_r"][None, :] / g["tanh_w"][:, None])
+    assert np.max(np.abs(prof - g["tanh_v"])) <= 2.3e-16

@@ -150,3 +150,20 @@ def test_served_recipe_equals_served_fields(pfa):
     for k in a:
         for x, y in zip(a[k], b[k]):
             assert np.max(np.abs(x - y)) <= 1e-12, k
+
+
+def test_device_embedding_matches_reference_code(pfa):
+    """The device's particles in embed_OPC's mode against embed_OPC's loop run
+    with the reference's compiled tanh_interp, p and equilibrium compositions
+    (tests/golden/ic_embed.npz): within device tanh / p rounding."""
+    import torch
+    from conftest import golden
+    from golden.make_golden import IC_RECIPES
+    g = golden("ic_embed.npz")
+    for n, rec in enumerate(IC_RECIPES):
+        shape = g[f"r{n}_cr"].shape
+        dev = [torch.full(shape, -1.0, dtype=torch.float64, device="cuda") for _ in range(4)]
+        pfa.ic_generate(rec, [t.data_ptr() for t in dev])
+        torch.cuda.synchronize()
+        for t, name in zip(dev, ("cr", "nb", "pd", "pl")):
+            assert np.max(np.abs(t.cpu().numpy() - g[f"r{n}_{name}"])) <= TANH_TOL, (n, name)
