@@ -45,6 +45,9 @@ enum { PFA_MODE_FUSED = 0, PFA_MODE_COMPAT = 1 };
  * PFA_FP32_KPHI: the same with FP32 compensations (64 bytes per cell). */
 enum { PFA_FP64 = 0, PFA_FP32 = 1, PFA_FP32_KPHI = 2 };
 enum { PFA_NUC_REFERENCE_GEOMETRY = 0, PFA_NUC_FIXED_GEOMETRY = 1 };
+/* Cahn-Hilliard: the reference's constant diffusivity matrix (its loop's
+ * form), or its disabled variable-mobility form (see pfa_set_mobility) */
+enum { PFA_MOBILITY_CONSTANT = 0, PFA_MOBILITY_VARIABLE = 1 };
 
 /* ---- errors (replaces checkCuda's assert, src/discretization.cu:23-30) ---- */
 int pfa_last_error(void);
@@ -59,6 +62,20 @@ int pfa_device_count(void);
 int pfa_set_mode(struct CudaData* dev, int mode);
 int pfa_set_precision(struct CudaData* dev, int precision);
 int pfa_set_nucleation(struct CudaData* dev, uint64_t seed, int geometry);
+/* PFA_MOBILITY_VARIABLE: the variable-mobility Cahn-Hilliard the reference
+ * wrote and left disabled (mobility_Cr/Nb_kernel src/discretization.cu:175-358,
+ * chemical_convolution_Cr/Nb_kernel :618-778, the commented update of
+ * composition_kernel :848-856): dx_k/dt = div of 8 coefficient-weighted
+ * gradients per component (those of the three phases' fictitious
+ * compositions, and of phi_del and phi_lav -- these two along x only, as
+ * the reference has them).  Its mobility matrix (d_M_CrCr ..., never
+ * defined by the reference) is M = D(x) H_gam^-1 with D(x) the
+ * composition-dependent D_CrCr ... D_NbNb and H_gam the gamma curvatures,
+ * so that pure gamma diffuses with D(x).  FP64 only; the fused step needs
+ * the 5-point mask; in compat mode device_mobilities / mobility_boundaries
+ * (and device_laplacian, for a loop that does not call them) compute the
+ * coefficients.  No counterpart in the reference's running code. */
+int pfa_set_mobility(struct CudaData* dev, int model);
 
 /* ---- mirrors of the reference entry points ---- */
 /* init_cuda, src/data.cuh:21-25 / src/data.cu:10-92; mask is nm*nm doubles */
@@ -92,6 +109,11 @@ int pfa_fictitious_boundaries(struct CudaData* dev, int nx, int ny, int nm, int 
 int pfa_device_laplacian(struct CudaData* dev, int nx, int ny, int nm, int bx, int by,
                          double dx, double dy);
 int pfa_device_laplacian_boundaries(struct CudaData* dev, int nx, int ny, int nm, int bx, int by);
+/* device_mobilities / mobility_boundaries, src/discretization.cuh:46,67
+ * (declared, never defined by the reference): compat mode with the variable
+ * mobility only, otherwise they return at once */
+int pfa_device_mobilities(struct CudaData* dev, int nx, int ny, int nm, int bx, int by);
+int pfa_mobility_boundaries(struct CudaData* dev, int nx, int ny, int nm, int bx, int by);
 int pfa_device_evolution(struct CudaData* dev, int nx, int ny, int nm, int bx, int by,
                          double alpha, double dt);
 int pfa_device_init_prng(struct CudaData* dev, int nx, int ny, int nm, int bx, int by);

@@ -129,14 +129,18 @@ float nTiles(int domain_size, int tile_loc, int mask_size);
  * (pfa_set_mode) each stage reproduces its own post-condition. */
 void device_fictitious(struct CudaData* dev, const int nx, const int ny, const int nm,
                        const int bx, const int by);
+/* Declared and never defined by the reference (its variable-mobility form is
+ * disabled); defined here: in compat mode with pfa_set_mobility's variable
+ * mobility they compute the flux coefficients and fill their ghost ring,
+ * otherwise they return at once. */
 void device_mobilities(struct CudaData* dev, const int nx, const int ny, const int nm,
-                       const int bx, const int by); /* declared, never defined (as in the reference) */
+                       const int bx, const int by);
 void device_boundaries(struct CudaData* dev, const int nx, const int ny, const int nm,
                        const int bx, const int by);
 void fictitious_boundaries(struct CudaData* dev, const int nx, const int ny, const int nm,
                            const int bx, const int by);
 void mobility_boundaries(struct CudaData* dev, const int nx, const int ny, const int nm,
-                         const int bx, const int by); /* declared, never defined */
+                         const int bx, const int by);
 void device_laplacian_boundaries(struct CudaData* dev, const int nx, const int ny, const int nm,
                                  const int bx, const int by);
 void device_laplacian(struct CudaData* dev, const int nx, const int ny, const int nm,

@@ -100,6 +100,21 @@ class Oracle:
         self._run2d.restype = None
         self._run2d.argtypes = [ctypes.POINTER(_dbl_p), ctypes.POINTER(_dbl_p), i, i,
                                 ctypes.POINTER(OrcParams), _dbl_p, i]
+        self._run2d_vm = getattr(L, P + "run2d_varmob")
+        self._run2d_vm.restype = None
+        self._run2d_vm.argtypes = [ctypes.POINTER(_dbl_p), ctypes.POINTER(_dbl_p), i, i,
+                                   ctypes.POINTER(OrcParams), _dbl_p, i]
+        self._mob2d = getattr(L, P + "mobility2d")
+        self._mob2d.restype = None
+        self._mob2d.argtypes = [ctypes.POINTER(_dbl_p), i, i, ctypes.POINTER(_dbl_p),
+                                ctypes.POINTER(_dbl_p)]
+        self._cdiv = getattr(L, P + "chem_div2d")
+        self._cdiv.restype = None
+        self._cdiv.argtypes = [ctypes.POINTER(_dbl_p), i, i, d, d, ctypes.POINTER(_dbl_p)]
+        self._dg = getattr(L, P + ("dg" if P == "orc_" else "dg_phase"))
+        self._dg.restype, self._dg.argtypes = d, [i, i, d, d]
+        self._d2g = getattr(L, P + ("d2g" if P == "orc_" else "d2g_phase"))
+        self._d2g.restype, self._d2g.argtypes = d, [i, i, i]
         self._step3d = getattr(L, P + "step3d")
         self._step3d.restype = None
         self._step3d.argtypes = [ctypes.POINTER(_dbl_p), ctypes.POINTER(_dbl_p), i, i, i,
@@ -161,6 +176,46 @@ class Oracle:
         self._run2d(pa, pb, nx, ny, ctypes.byref(prm), _ptr(work), int(nsteps))
         by_addr = {x.ctypes.data: x for x in a + b}
         return [by_addr[ctypes.cast(pa[k], ctypes.c_void_p).value] for k in range(4)]
+
+    def run2d_varmob(self, fields, params, nsteps):
+        """run2d with the variable-mobility Cahn-Hilliard (step2d_varmob)."""
+        a = [np.array(f, dtype=np.float64, copy=True) for f in fields]
+        b = [np.empty_like(x) for x in a]
+        ny, nx = a[0].shape
+        work = np.empty(22 * nx * ny, dtype=np.float64)
+        pa = (_dbl_p * 4)(*[_ptr(x) for x in a])
+        pb = (_dbl_p * 4)(*[_ptr(x) for x in b])
+        prm = params if isinstance(params, OrcParams) else OrcParams.from_dict(params)
+        self._run2d_vm(pa, pb, nx, ny, ctypes.byref(prm), _ptr(work), int(nsteps))
+        by_addr = {x.ctypes.data: x for x in a + b}
+        return [by_addr[ctypes.cast(pa[k], ctypes.c_void_p).value] for k in range(4)]
+
+    def mobility2d(self, fields):
+        """(fict[6], mob[16]) of a state: x_gam, x_del, x_lav (Cr, Nb) and the
+        Cr and Nb rows of the mobility coefficients, ghost ring mirrored."""
+        f = [np.ascontiguousarray(x, dtype=np.float64) for x in fields]
+        ny, nx = f[0].shape
+        fict = [np.zeros((ny, nx)) for _ in range(6)]
+        mob = [np.zeros((ny, nx)) for _ in range(16)]
+        self._mob2d((_dbl_p * 4)(*[_ptr(x) for x in f]), nx, ny,
+                    (_dbl_p * 6)(*[_ptr(x) for x in fict]), (_dbl_p * 16)(*[_ptr(x) for x in mob]))
+        return fict, mob
+
+    def chem_div2d(self, fields, dx, dy):
+        """The variable-mobility divergences (Cr, Nb) at the interior cells."""
+        f = [np.ascontiguousarray(x, dtype=np.float64) for x in fields]
+        ny, nx = f[0].shape
+        out = [np.zeros((ny, nx)) for _ in range(2)]
+        self._cdiv((_dbl_p * 4)(*[_ptr(x) for x in f]), nx, ny, dx, dy,
+                   (_dbl_p * 2)(*[_ptr(x) for x in out]))
+        return out
+
+    def dg(self, phase, comp, x, y):
+        return np.array([self._dg(phase, comp, float(a), float(b))
+                         for a, b in zip(np.ravel(x), np.ravel(y))])
+
+    def d2g(self, phase, i, j):
+        return self._d2g(phase, i, j)
 
     def run3d(self, fields, params, nsteps):
         a = [np.array(f, dtype=np.float64, copy=True) for f in fields]

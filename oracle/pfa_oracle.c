@@ -167,6 +167,30 @@ double orc_dg_gam(int comp, double xcr, double xnb)
 	return DGGAM[comp][0] * xcr + DGGAM[comp][1] * xnb + DGGAM[comp][2];
 }
 
+/* d g_<phase> / d x_<comp> and the (constant) curvatures d2 g / dx_i dx_j of
+ * the paraboloids (thermo/parabola625.c:655-706, 1305-1410), derived here
+ * from the energy parameters above: with u = XCR - xe_Cr, v = XNB - xe_Nb,
+ *   g = A u^2 + (B XCR - C) v + E v^2,
+ *   dg/dXCR = 2 A u + B v,  dg/dXNB = B XCR - C + 2 E v,
+ *   d2g = [[2 A, B], [B, 2 E]]. */
+double orc_dg(int phase, int comp, double xcr, double xnb)
+{
+	const double* g = GPAR[phase];
+	const double ucr = xcr - XE[phase][0];
+	const double unb = xnb - XE[phase][1];
+	if (comp == 0)
+		return 2.0 * g[0] * ucr + g[1] * unb;
+	return g[1] * xcr - g[2] + 2.0 * g[3] * unb;
+}
+
+double orc_d2g(int phase, int i, int j)
+{
+	const double* g = GPAR[phase];
+	if (i != j)
+		return g[1];
+	return i == 0 ? 2.0 * g[0] : 2.0 * g[3];
+}
+
 /* D[row][col]: row 0 = Cr, 1 = Nb; col 0 = Cr, 1 = Nb. */
 double orc_D(int row, int col, double XCR, double XNB)
 {
@@ -359,7 +383,11 @@ double orc_u53(uint32_t hi, uint32_t lo)
 #define E_DG_GAM_CR(a, b) orc_dg_gam(0, a, b)
 #define E_DG_GAM_NB(a, b) orc_dg_gam(1, a, b)
 #define E_D_CRCR(a, b) orc_D(0, 0, a, b)
+#define E_D_CRNB(a, b) orc_D(0, 1, a, b)
+#define E_D_NBCR(a, b) orc_D(1, 0, a, b)
 #define E_D_NBNB(a, b) orc_D(1, 1, a, b)
+#define E_DG(ph, c, a, b) orc_dg(ph, c, a, b)
+#define E_D2G(ph, i, j) orc_d2g(ph, i, j)
 #define E_NUC_PROB orc_nucleation_probability_sphere
 #define E_XE_GAM_CR XE[0][0]
 #define E_XE_GAM_NB XE[0][1]

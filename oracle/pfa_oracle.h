@@ -67,6 +67,8 @@ double orc_fict(int phase, int comp, double xcr, double xnb,
 double orc_g(int phase, double xcr, double xnb);
 double orc_dg_gam(int comp, double xcr, double xnb);
 double orc_D(int row, int col, double xcr, double xnb);
+double orc_dg(int phase, int comp, double xcr, double xnb);
+double orc_d2g(int phase, int i, int j);
 void orc_nucleation_probability_sphere(double xcr, double xnb, double dG_chem,
                                        double D_CrCr, double D_NbNb, double sigma,
                                        double Vatom, double n_gam, double dV, double dt,
@@ -86,6 +88,16 @@ void orc_step2d(double* old_f[4], double* new_f[4], int nx, int ny,
                 const orc_params* prm, double* work /* 2*nx*ny doubles */);
 void orc_run2d(double* a[4], double* b[4], int nx, int ny, const orc_params* prm,
                double* work, int nsteps);
+/* variable-mobility Cahn-Hilliard (the reference's disabled mobility kernels),
+ * work = 22*nx*ny doubles; orc_mobility2d: the 6 fictitious compositions and
+ * the 16 mobility coefficients of a state (after its boundary fill) */
+void orc_step2d_varmob(double* old_f[4], double* new_f[4], int nx, int ny,
+                       const orc_params* prm, double* work);
+void orc_run2d_varmob(double* a[4], double* b[4], int nx, int ny, const orc_params* prm,
+                      double* work, int nsteps);
+void orc_mobility2d(const double* const f[4], int nx, int ny, double* fict[6], double* mob[16]);
+void orc_chem_div2d(const double* const f[4], int nx, int ny, double dx, double dy,
+                    double* out[2]);
 void orc_step3d(double* old_f[4], double* new_f[4], int nx, int ny, int nz,
                 const orc_params* prm, double* work /* 2*nx*ny*nz doubles */);
 

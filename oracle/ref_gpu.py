@@ -43,6 +43,8 @@ K_FICT = (b"_Z21fictitious_gam_kernelPdS_S_S_S_S_iii", b"_Z21fictitious_del_kern
 K_CONV = b"_Z18convolution_kernelPdS_iii"
 K_CH = b"_Z20cahn_hilliard_kernelPdS_S_S_iiid"
 K_AC = b"_Z17allen_cahn_kernelPdS_S_S_S_S_iiidd"
+K_CHEM = (b"_Z30chemical_convolution_Cr_kernelPdS_S_S_S_S_S_S_S_S_S_S_S_S_S_S_S_iiidd",
+          b"_Z30chemical_convolution_Nb_kernelPdS_S_S_S_S_S_S_S_S_S_S_S_S_S_S_S_iiidd")
 K_INIT_PRNG = b"_Z16init_prng_kernelP17curandStateXORWOWii"
 K_NUC = b"_Z17nucleation_kernelPdS_S_S_P17curandStateXORWOWiiidddddddd"
 PRNG_STATE_BYTES = 64  # >= sizeof(curandStateXORWOW) (48)
@@ -255,3 +257,29 @@ def run_reference_nucleation(drv, fields, sigma, unit_a, d, dt):
     for p in f + [prng]:
         drv.free(p)
     return out
+
+
+def run_reference_chem_div(drv, fields, fict, mob, dx, dy):
+    """The reference's chemical_convolution_Cr_kernel and _Nb_kernel
+    (src/discretization.cu:618-778, compiled but never launched by its loop)
+    on a state: fields (x_Cr, x_Nb, phi_del, phi_lav), its six fictitious
+    compositions and 16 mobility coefficients (Cr row, Nb row, in the
+    kernels' argument order), in the launch shape its commented launches
+    use (bx = by = 13).  Returns the two divergence arrays."""
+    ny, nx = fields[0].shape
+    nb = nx * ny * 8
+    pf = [drv.alloc(nb) for _ in range(4)]
+    pc = [drv.alloc(nb) for _ in range(6)]
+    pm = [drv.alloc(nb) for _ in range(16)]
+    out = [drv.alloc(nb) for _ in range(2)]
+    for p, a in zip(pf + pc + pm, list(fields) + list(fict) + list(mob)):
+        drv.put(p, a)
+    grid = (n_tiles(nx, BX, NM), n_tiles(ny, BY, NM))
+    for k in range(2):
+        drv.launch(K_CHEM[k], grid, (BX, BY), 0,
+                   pc + pm[8 * k:8 * k + 8] + [pf[2], pf[3], out[k], nx, ny, NM, dx, dy])
+    drv.sync()
+    res = [drv.get(p, (ny, nx)) for p in out]
+    for p in pf + pc + pm + out:
+        drv.free(p)
+    return res

@@ -22,6 +22,38 @@ double ref_p(double x) { return p(x); }
 double ref_pprime(double x) { return pPrime(x); }
 double ref_tanh_interp(double r, double w) { return tanh_interp(r, w); }
 
+/* the reference's dg_<phase>_dx<comp> and d2g_<phase>_dx<i><j> by index
+ * (phase 0 gamma, 1 delta, 2 laves; comp 0 Cr, 1 Nb) */
+double ref_dg_phase(int phase, int comp, double a, double b)
+{
+	switch (phase * 2 + comp) {
+	case 0: return dg_gam_dxCr(a, b);
+	case 1: return dg_gam_dxNb(a, b);
+	case 2: return dg_del_dxCr(a, b);
+	case 3: return dg_del_dxNb(a, b);
+	case 4: return dg_lav_dxCr(a, b);
+	default: return dg_lav_dxNb(a, b);
+	}
+}
+
+double ref_d2g_phase(int phase, int i, int j)
+{
+	switch (phase * 4 + i * 2 + j) {
+	case 0: return d2g_gam_dxCrCr();
+	case 1: return d2g_gam_dxCrNb();
+	case 2: return d2g_gam_dxNbCr();
+	case 3: return d2g_gam_dxNbNb();
+	case 4: return d2g_del_dxCrCr();
+	case 5: return d2g_del_dxCrNb();
+	case 6: return d2g_del_dxNbCr();
+	case 7: return d2g_del_dxNbNb();
+	case 8: return d2g_lav_dxCrCr();
+	case 9: return d2g_lav_dxCrNb();
+	case 10: return d2g_lav_dxNbCr();
+	default: return d2g_lav_dxNbNb();
+	}
+}
+
 /* embed_OPC (src/alloy625.cpp:262-294) on a 2D grid in the ghost-ring layout
  * (rows of nx doubles, f = x_Cr, x_Nb, phi_del, phi_lav), seed centre
  * (cx, cy) in array coordinates, restated without MMSP: over the box
@@ -138,7 +170,11 @@ extern "C" {
 #define E_DG_GAM_CR dg_gam_dxCr
 #define E_DG_GAM_NB dg_gam_dxNb
 #define E_D_CRCR D_CrCr
+#define E_D_CRNB D_CrNb
+#define E_D_NBCR D_NbCr
 #define E_D_NBNB D_NbNb
+#define E_DG(ph, c, a, b) ref_dg_phase(ph, c, a, b)
+#define E_D2G(ph, i, j) ref_d2g_phase(ph, i, j)
 #define E_NUC_PROB nuc_prob_ref
 #define E_XE_GAM_CR xe_gam_Cr()
 #define E_XE_GAM_NB xe_gam_Nb()

@@ -11,7 +11,10 @@
  *   E_FICT_GAM_CR(...), E_FICT_GAM_NB, E_FICT_DEL_CR, E_FICT_DEL_NB,
  *   E_FICT_LAV_CR, E_FICT_LAV_NB  -- (XCR, XNB, pDel, pGam, pLav)
  *   E_G_GAM, E_G_DEL, E_G_LAV, E_DG_GAM_CR, E_DG_GAM_NB  -- (XCR, XNB)
- *   E_D_CRCR, E_D_NBNB   -- composition-dependent diffusivities
+ *   E_D_CRCR, E_D_CRNB, E_D_NBCR, E_D_NBNB -- composition-dependent diffusivities
+ *   E_DG(ph, c, XCR, XNB), E_D2G(ph, i, j) -- dg_<phase>_dx<c> and the constant
+ *                          curvatures d2g_<phase>_dx<i><j> (0 gamma, 1 delta,
+ *                          2 laves; 0 Cr, 1 Nb)
  *   E_NUC_PROB(...)      -- nucleation_probability_sphere
  *   E_XE_GAM_CR ... E_XE_LAV_NB -- equilibrium compositions (no parentheses)
  * Compiles as C99 and as C++.
@@ -181,6 +184,235 @@ void SFN(step2d)(double* old_f[4], double* new_f[4], int nx, int ny,
 		                 new_f[0][i], new_f[1][i], new_f[2][i], new_f[3][i],
 		                 &new_f[0][i], &new_f[1][i], &new_f[2][i], &new_f[3][i]);
 	}
+}
+
+/* ---- variable-mobility Cahn-Hilliard ----
+ * The reference's disabled form (mobility_Cr_kernel / mobility_Nb_kernel,
+ * src/discretization.cu:175-358, chemical_convolution_Cr/Nb_kernel
+ * :618-778, the commented update of composition_kernel :848-856), restated
+ * term by term.  The reference never defines the mobility matrix its
+ * kernels call (d_M_CrCr ...); here M = D(x) H_gam^-1, with D(x) the
+ * composition-dependent diffusivities (thermo/parabola625.c:1860-1894) and
+ * H_gam the gamma curvatures, so that in pure gamma the flux is
+ * D(x) grad x^gamma.  Per component k the 8 coefficients are, in the
+ * reference's order,
+ *   gam_k0 = pGam (M_k0 H_gam[0][0] + M_k1 H_gam[.][.]) ... (see below),
+ *   phi_del_k = p'(phi_del) (M_k0 (dg_del_Cr - dg_gam_Cr) + M_k1 (dg_del_Nb - dg_gam_Nb)),
+ * and the divergence sums, for terms 1-6, the 1D variable-coefficient
+ * differences along x and along y, for terms 7-8 along x only (as the
+ * reference does).  mob[16]: Cr row gamCrCr gamCrNb delCrCr delCrNb
+ * lavCrCr lavCrNb phiDelCr phiLavCr, then the Nb row likewise; fict[6]:
+ * x_gam Cr Nb, x_del Cr Nb, x_lav Cr Nb.  All cells of the array. */
+static void SFN(mobility_fields)(double* const* f, double* const* fict, double* const* mob,
+                                 size_t n)
+{
+	const double hg00 = E_D2G(0, 0, 0), hg01 = E_D2G(0, 0, 1), hg10 = E_D2G(0, 1, 0),
+	             hg11 = E_D2G(0, 1, 1);
+	const double det = hg00 * hg11 - hg01 * hg10;
+	long long i;
+	#pragma omp parallel for schedule(static)
+	for (i = 0; i < (long long)n; i++) {
+		const double X = f[0][i], Y = f[1][i], phd = f[2][i], phl = f[3][i];
+		const double pDel = E_P(phd), pLav = E_P(phl), pGam = 1.0 - pDel - pLav;
+		const double xg[2] = {E_FICT_GAM_CR(X, Y, pDel, pGam, pLav), E_FICT_GAM_NB(X, Y, pDel, pGam, pLav)};
+		const double xd[2] = {E_FICT_DEL_CR(X, Y, pDel, pGam, pLav), E_FICT_DEL_NB(X, Y, pDel, pGam, pLav)};
+		const double xl[2] = {E_FICT_LAV_CR(X, Y, pDel, pGam, pLav), E_FICT_LAV_NB(X, Y, pDel, pGam, pLav)};
+		fict[0][i] = xg[0];
+		fict[1][i] = xg[1];
+		fict[2][i] = xd[0];
+		fict[3][i] = xd[1];
+		fict[4][i] = xl[0];
+		fict[5][i] = xl[1];
+		const double D[2][2] = {{E_D_CRCR(X, Y), E_D_CRNB(X, Y)}, {E_D_NBCR(X, Y), E_D_NBNB(X, Y)}};
+		double M[2][2];
+		for (int k = 0; k < 2; k++) {
+			M[k][0] = (D[k][0] * hg11 - D[k][1] * hg10) / det;
+			M[k][1] = (D[k][1] * hg00 - D[k][0] * hg01) / det;
+		}
+		const double pw[3] = {pGam, pDel, pLav};
+		const double dgg[2] = {E_DG(0, 0, xg[0], xg[1]), E_DG(0, 1, xg[0], xg[1])};
+		const double dgd[2] = {E_DG(1, 0, xd[0], xd[1]), E_DG(1, 1, xd[0], xd[1])};
+		const double dgl[2] = {E_DG(2, 0, xl[0], xl[1]), E_DG(2, 1, xl[0], xl[1])};
+		const double ppd = E_PPRIME(phd), ppl = E_PPRIME(phl);
+		/* Cr row, mobility_Cr_kernel (terms 1-8) */
+		for (int ph = 0; ph < 3; ph++) {
+			mob[2 * ph][i] = pw[ph] * (M[0][0] * E_D2G(ph, 0, 0) + M[0][1] * E_D2G(ph, 0, 1));
+			mob[2 * ph + 1][i] = pw[ph] * (M[0][0] * E_D2G(ph, 1, 0) + M[0][1] * E_D2G(ph, 1, 1));
+		}
+		mob[6][i] = ppd * (M[0][0] * (dgd[0] - dgg[0]) + M[0][1] * (dgd[1] - dgg[1]));
+		mob[7][i] = ppl * (M[0][0] * (dgl[0] - dgg[0]) + M[0][1] * (dgl[1] - dgg[1]));
+		/* Nb row, mobility_Nb_kernel (its terms 1-6 read d2g_..._dxNbCr where
+		 * the Cr kernel reads ..._dxCrNb: equal, the matrices are symmetric) */
+		for (int ph = 0; ph < 3; ph++) {
+			mob[8 + 2 * ph][i] = pw[ph] * (M[1][0] * E_D2G(ph, 0, 0) + M[1][1] * E_D2G(ph, 1, 0));
+			mob[9 + 2 * ph][i] = pw[ph] * (M[1][0] * E_D2G(ph, 1, 0) + M[1][1] * E_D2G(ph, 1, 1));
+		}
+		mob[14][i] = ppd * (M[1][0] * (dgd[0] - dgg[0]) + M[1][1] * (dgd[1] - dgg[1]));
+		mob[15][i] = ppl * (M[1][0] * (dgl[0] - dgg[0]) + M[1][1] * (dgl[1] - dgg[1]));
+	}
+}
+
+/* discrete_laplacian, src/discretization.cu:605-616 */
+static double SFN(dlap)(double Dl, double Dm, double Dh, double cl, double cm, double ch, double d)
+{
+	return ((Dh + Dm) * (ch - cm) - (Dm + Dl) * (cm - cl)) / (2.0 * d * d);
+}
+
+/* chemical_convolution_<comp>_kernel (src/discretization.cu:618-778) at
+ * array cell (x, y): neighbours clamped at the array's edges as there */
+static double SFN(chem_div)(double* const* fict, double* const* mobk, const double* phd,
+                            const double* phl, int nx, int ny, int x, int y, double dx, double dy)
+{
+	const size_t mid = (size_t)nx * y + x;
+	const size_t lft = x == 0 ? mid : mid - 1;
+	const size_t rgt = x == nx - 1 ? mid : mid + 1;
+	const size_t bot = y == 0 ? mid : mid - nx;
+	const size_t top = y == ny - 1 ? mid : mid + nx;
+	/* terms 1-6: (coefficient, composition) pairs */
+	const int comp[6] = {0, 1, 2, 3, 4, 5};
+	double div = 0.0;
+	for (int t = 0; t < 6; t++) {
+		const double* D = mobk[t];
+		const double* c = fict[comp[t]];
+		div += SFN(dlap)(D[lft], D[mid], D[rgt], c[lft], c[mid], c[rgt], dx);
+		div += SFN(dlap)(D[bot], D[mid], D[top], c[bot], c[mid], c[top], dy);
+	}
+	/* terms 7-8: along x only */
+	div += SFN(dlap)(mobk[6][lft], mobk[6][mid], mobk[6][rgt], phd[lft], phd[mid], phd[rgt], dx);
+	div += SFN(dlap)(mobk[7][lft], mobk[7][mid], mobk[7][rgt], phl[lft], phl[mid], phl[rgt], dx);
+	return div;
+}
+
+/* One step with the variable-mobility Cahn-Hilliard, in the sequence the
+ * reference's loop would run with its mobility calls enabled
+ * (src/main.cpp:289-305 with device_mobilities / mobility_boundaries):
+ * boundaries, fictitious compositions and their boundaries, mobility
+ * coefficients and their boundaries, the divergences of Cr and Nb and the
+ * 5-point convolution of the phases into new_f, their boundaries, then the
+ * update: x_new = x_old + dt div (the commented form of composition_kernel,
+ * src/discretization.cu:848-856) and Allen-Cahn as in the constant form.
+ * work: 22 n doubles. */
+void SFN(step2d_varmob)(double* old_f[4], double* new_f[4], int nx, int ny,
+                        const orc_params* prm, double* work)
+{
+	const size_t n = (size_t)nx * ny;
+	double* fict[6];
+	double* mob[16];
+	for (int k = 0; k < 6; k++) fict[k] = work + (size_t)k * n;
+	for (int k = 0; k < 16; k++) mob[k] = work + (size_t)(6 + k) * n;
+	for (int k = 0; k < 4; k++)
+		SFN(bc2d)(old_f[k], nx, ny);
+	SFN(mobility_fields)(old_f, fict, mob, n);
+	for (int k = 0; k < 6; k++)
+		SFN(bc2d)(fict[k], nx, ny);
+	for (int k = 0; k < 16; k++)
+		SFN(bc2d)(mob[k], nx, ny);
+
+	const double dx = prm->dx, dy = prm->dy;
+	const double m_n = 1. / (dy * dy);
+	const double m_w = 1. / (dx * dx);
+	const double m_c = -2. * (dx * dx + dy * dy) / (dx * dx * dy * dy);
+	const double m_e = 1. / (dx * dx);
+	const double m_s = 1. / (dy * dy);
+	int y;
+	#pragma omp parallel for schedule(static)
+	for (y = 1; y < ny - 1; y++) {
+		for (int x = 1; x < nx - 1; x++) {
+			const size_t i = (size_t)y * nx + x;
+			new_f[0][i] = SFN(chem_div)(fict, mob, old_f[2], old_f[3], nx, ny, x, y, dx, dy);
+			new_f[1][i] = SFN(chem_div)(fict, mob + 8, old_f[2], old_f[3], nx, ny, x, y, dx, dy);
+			for (int k = 2; k < 4; k++) {
+				const double* s = old_f[k];
+				double v = 0.;
+				v += m_n * s[i - nx];
+				v += m_w * s[i - 1];
+				v += m_c * s[i];
+				v += m_e * s[i + 1];
+				v += m_s * s[i + nx];
+				new_f[k][i] = v;
+			}
+		}
+	}
+	for (int k = 0; k < 4; k++)
+		SFN(bc2d)(new_f[k], nx, ny);
+
+	long long i;
+	#pragma omp parallel for schedule(static)
+	for (i = 0; i < (long long)n; i++) {
+		const double divCr = new_f[0][i], divNb = new_f[1][i];
+		double oCr, oNb;
+		SFN(update_cell)(prm, old_f[0][i], old_f[1][i], old_f[2][i], old_f[3][i],
+		                 0.0, 0.0, new_f[2][i], new_f[3][i],
+		                 &oCr, &oNb, &new_f[2][i], &new_f[3][i]);
+		new_f[0][i] = old_f[0][i] + prm->dt * divCr;
+		new_f[1][i] = old_f[1][i] + prm->dt * divNb;
+	}
+}
+
+void SFN(run2d_varmob)(double* a[4], double* b[4], int nx, int ny, const orc_params* prm,
+                       double* work, int nsteps)
+{
+	for (int s = 0; s < nsteps; s++) {
+		SFN(step2d_varmob)(a, b, nx, ny, prm, work);
+		for (int k = 0; k < 4; k++) {
+			double* t = a[k];
+			a[k] = b[k];
+			b[k] = t;
+		}
+	}
+}
+
+/* The two divergences of the variable-mobility form (chemical_convolution
+ * of Cr and Nb) at the interior cells of a state, after its boundary fill;
+ * the ghost ring of out[] is left 0. */
+void SFN(chem_div2d)(const double* const f[4], int nx, int ny, double dx, double dy,
+                     double* out[2])
+{
+	const size_t n = (size_t)nx * ny;
+	double* fict[6];
+	double* mob[16];
+	double* g[4];
+	double* work = (double*)malloc(26 * n * sizeof(double));
+	for (int k = 0; k < 6; k++) fict[k] = work + (size_t)k * n;
+	for (int k = 0; k < 16; k++) mob[k] = work + (size_t)(6 + k) * n;
+	for (int k = 0; k < 4; k++) {
+		g[k] = work + (size_t)(22 + k) * n;
+		memcpy(g[k], f[k], n * sizeof(double));
+		SFN(bc2d)(g[k], nx, ny);
+	}
+	SFN(mobility_fields)(g, fict, mob, n);
+	for (int k = 0; k < 6; k++) SFN(bc2d)(fict[k], nx, ny);
+	for (int k = 0; k < 16; k++) SFN(bc2d)(mob[k], nx, ny);
+	memset(out[0], 0, n * sizeof(double));
+	memset(out[1], 0, n * sizeof(double));
+	for (int y = 1; y < ny - 1; y++)
+		for (int x = 1; x < nx - 1; x++) {
+			const size_t i = (size_t)y * nx + x;
+			out[0][i] = SFN(chem_div)(fict, mob, g[2], g[3], nx, ny, x, y, dx, dy);
+			out[1][i] = SFN(chem_div)(fict, mob + 8, g[2], g[3], nx, ny, x, y, dx, dy);
+		}
+	free(work);
+}
+
+/* The fictitious compositions and the 16 mobility coefficients of a state
+ * (after its boundary fill), for the golden divergences made with the
+ * reference's own chemical_convolution kernels.  f is not modified. */
+void SFN(mobility2d)(const double* const f[4], int nx, int ny, double* fict[6], double* mob[16])
+{
+	const size_t n = (size_t)nx * ny;
+	double* g[4];
+	for (int k = 0; k < 4; k++) {
+		g[k] = (double*)malloc(n * sizeof(double));
+		memcpy(g[k], f[k], n * sizeof(double));
+		SFN(bc2d)(g[k], nx, ny);
+	}
+	SFN(mobility_fields)(g, fict, mob, n);
+	for (int k = 0; k < 6; k++)
+		SFN(bc2d)(fict[k], nx, ny);
+	for (int k = 0; k < 16; k++)
+		SFN(bc2d)(mob[k], nx, ny);
+	for (int k = 0; k < 4; k++)
+		free(g[k]);
 }
 
 /* nsteps steps with the caller-side pointer swap of src/main.cpp:318-321;

@@ -101,6 +101,12 @@ struct State {
   cudaEvent_t xev[8] = {};  // chunked transfers (created on first use)
   cudaEvent_t xdone = nullptr;  // the read-out's last copy on str_B
   double* nrg_map[2] = {};  // per-node chemical / gradient energy (on request)
+  // variable-mobility Cahn-Hilliard (pfa_set_mobility): the compat stages'
+  // 16 coefficient arrays (allocated on first use) and the spacing of the
+  // divergence (the last device_laplacian call's, else from the mask)
+  int varmob = 0;
+  double* mob[16] = {};
+  double dxy[2] = {0.0, 0.0};
   std::vector<GraphEntry> graphs;
 };
 
@@ -198,6 +204,7 @@ static Step2DArgs step_args(State* s, double alpha, double dt) {
   a.m.dt = dt;
   std::memcpy(a.mask9, s->mask9, sizeof(a.mask9));
   a.nine = !s->five_point;
+  a.varmob = s->varmob;
   a.k = s->fk;
   for (int i = 0; i < 2; i++)
     for (int j = 0; j < 2; j++) a.dtD[i][j] = float(dt * s->m.D[i][j]);
@@ -430,6 +437,10 @@ static StageArgs stage_args(CudaData* dev, State* s) {
   a.ny = s->ny;
   a.m = s->m;
   std::memcpy(a.mask9, s->mask9, sizeof(a.mask9));
+  for (int k = 0; k < 16; k++) a.mob[k] = s->mob[k];
+  a.dxy[0] = s->dxy[0];
+  a.dxy[1] = s->dxy[1];
+  a.varmob = s->varmob;
   return a;
 }
 
@@ -457,10 +468,41 @@ static int st_fict_boundaries(CudaData* dev, State* s) {
   return 0;
 }
 
+// the variable-mobility coefficients at every cell from the old fields and
+// the fictitious compositions (device_mobilities, src/discretization.cu:297-358)
+static int st_mobilities(CudaData* dev, State* s) {
+  if (int r = ensure_fict(dev, s)) return r;
+  const size_t n = size_t(s->nx) * s->ny;
+  for (auto& p : s->mob)
+    if (!p && alloc_field(&p, n)) return PFA_ECUDA;
+  CK(launch_mobility(stage_args(dev, s), s->st));
+  return 0;
+}
+
+// mobility_boundaries (declared, never defined by the reference): the
+// zero-flux fill of the coefficients' ghost ring
+static int st_mob_boundaries(CudaData* dev, State* s) {
+  (void)dev;
+  for (double* p : s->mob)
+    if (p) CK(launch_bc(p, s->nx, s->ny, s->st));
+  return 0;
+}
+
+// device_laplacian (src/discretization.cu:780-841): the mask convolution of
+// the phases and of the gamma compositions, or, with the variable mobility,
+// of the phases and chemical_convolution_Cr/Nb (the reference's commented
+// launches) for the compositions -- with the coefficients computed here, so
+// that a loop that never calls device_mobilities still gets them
 static int st_laplacian(CudaData* dev, State* s) {
   if (int r = ensure_fict(dev, s)) return r;
   CK(launch_convolution(dev->phi_del_old, dev->phi_del_new, s->nx, s->ny, s->mask9, s->st));
   CK(launch_convolution(dev->phi_lav_old, dev->phi_lav_new, s->nx, s->ny, s->mask9, s->st));
+  if (s->varmob) {
+    if (int r = st_mobilities(dev, s)) return r;
+    if (int r = st_mob_boundaries(dev, s)) return r;
+    CK(launch_chem_convolution(stage_args(dev, s), s->st));
+    return 0;
+  }
   CK(launch_convolution(dev->conc_Cr_gam, dev->conc_Cr_new, s->nx, s->ny, s->mask9, s->st));
   CK(launch_convolution(dev->conc_Nb_gam, dev->conc_Nb_new, s->nx, s->ny, s->mask9, s->st));
   return 0;
@@ -522,6 +564,8 @@ static int init_core(CudaData* dev, int nx, int ny, int nm, const double* mask,
   s->m.mask[4] = mask[7];
   s->m.idx2[0] = mask[3];  // left: 1/dx^2 (src/mesh.cpp:191)
   s->m.idx2[1] = mask[1];  // upper: 1/dy^2 (src/mesh.cpp:190)
+  s->dxy[0] = mask[3] > 0.0 ? 1.0 / std::sqrt(mask[3]) : 0.0;
+  s->dxy[1] = mask[1] > 0.0 ? 1.0 / std::sqrt(mask[1]) : 0.0;
   s->m.idx2[2] = 0.0;
   model_fast_coef(&s->fk);
   {
@@ -558,6 +602,7 @@ static int init_core(CudaData* dev, int nx, int ny, int nm, const double* mask,
   if (!nuc_ready) {
     CK(nucleation_setup());
     CK(prepare_step2d_f32());
+    CK(prepare_step2d_f64());
     nuc_ready = true;
   }
   if (cr) {
@@ -599,6 +644,7 @@ static int free_core(CudaData* dev) {
   cudaFree(s->sum_out);
   cudaFree(s->nrg_map[0]);
   cudaFree(s->nrg_map[1]);
+  for (double* p : s->mob) cudaFree(p);
   for (cudaEvent_t e : s->xev)
     if (e) cudaEventDestroy(e);
   if (s->xdone) cudaEventDestroy(s->xdone);
@@ -788,8 +834,21 @@ void fictitious_boundaries(struct CudaData* dev, const int, const int, const int
   PFA_STAGE(st_fict_boundaries(dev, s))
 }
 void device_laplacian(struct CudaData* dev, const int, const int, const int, const int, const int,
-                      const fp_t, const fp_t) {
-  PFA_STAGE(st_laplacian(dev, s))
+                      const fp_t dx, const fp_t dy) {
+  PFA_STAGE((s->dxy[0] = dx, s->dxy[1] = dy, st_laplacian(dev, s)))
+}
+
+// Declared by the reference (src/discretization.cuh:46,67) for its disabled
+// variable-mobility form and never defined there.  Here, in compat mode with
+// the variable mobility (pfa_set_mobility), they compute the flux
+// coefficients and fill their ghost ring; otherwise they return at once.
+void device_mobilities(struct CudaData* dev, const int, const int, const int, const int,
+                       const int) {
+  PFA_STAGE(if (s->varmob) st_mobilities(dev, s))
+}
+void mobility_boundaries(struct CudaData* dev, const int, const int, const int, const int,
+                         const int) {
+  PFA_STAGE(if (s->varmob) st_mob_boundaries(dev, s))
 }
 void device_laplacian_boundaries(struct CudaData* dev, const int, const int, const int, const int,
                                  const int) {
@@ -869,6 +928,8 @@ int pfa_set_mode(struct CudaData* dev, int mode) {
   if (mode != PFA_MODE_FUSED && mode != PFA_MODE_COMPAT) return fail(PFA_EINVAL, "pfa_set_mode");
   if (mode == PFA_MODE_COMPAT && s->precision != PFA_FP64)
     return fail(PFA_EINVAL, "compat mode is FP64 only");
+  if (mode == PFA_MODE_FUSED && s->varmob && !s->five_point)
+    return fail(PFA_EINVAL, "the fused variable-mobility step needs the 5-point mask");
   s->mode = mode;
   return 0;
 }
@@ -879,6 +940,8 @@ int pfa_set_precision(struct CudaData* dev, int precision) {
   if (precision < PFA_FP64 || precision > PFA_FP32_KPHI) return fail(PFA_EINVAL, "pfa_set_precision");
   if (precision != PFA_FP64 && s->mode == PFA_MODE_COMPAT)
     return fail(PFA_EINVAL, "compat mode is FP64 only");
+  if (precision != PFA_FP64 && s->varmob)
+    return fail(PFA_EINVAL, "the variable mobility is an FP64 form");
   if (precision == s->precision) return 0;
   if (s->f32_live) {
     if (int r = f32_export(dev, s)) return r;
@@ -886,6 +949,22 @@ int pfa_set_precision(struct CudaData* dev, int precision) {
   }
   drop_graphs(s);
   s->precision = precision;
+  return 0;
+}
+
+int pfa_set_mobility(struct CudaData* dev, int model) {
+  State* s = lookup(dev);
+  if (!s) return fail(PFA_ESTATE, "pfa_set_mobility: unknown CudaData");
+  if (model != PFA_MOBILITY_CONSTANT && model != PFA_MOBILITY_VARIABLE)
+    return fail(PFA_EINVAL, "pfa_set_mobility: model");
+  if (model == PFA_MOBILITY_VARIABLE) {
+    if (s->precision != PFA_FP64)
+      return fail(PFA_EINVAL, "the variable mobility is an FP64 form (pfa_set_precision PFA_FP64)");
+    if (s->mode == PFA_MODE_FUSED && !s->five_point)
+      return fail(PFA_EINVAL, "the fused variable-mobility step needs the 5-point mask");
+  }
+  s->varmob = model == PFA_MOBILITY_VARIABLE;
+  drop_graphs(s);
   return 0;
 }
 
@@ -962,8 +1041,25 @@ int pfa_device_fictitious(struct CudaData* dev, int, int, int, int, int) { PFA_C
 int pfa_fictitious_boundaries(struct CudaData* dev, int, int, int, int, int) {
   PFA_CSTAGE(st_fict_boundaries)
 }
-int pfa_device_laplacian(struct CudaData* dev, int, int, int, int, int, double, double) {
-  PFA_CSTAGE(st_laplacian)
+int pfa_device_laplacian(struct CudaData* dev, int, int, int, int, int, double dx, double dy) {
+  State* s = lookup(dev);
+  if (!s) return fail(PFA_ESTATE, "st_laplacian: unknown CudaData");
+  if (s->mode != PFA_MODE_COMPAT) return 0;
+  s->dxy[0] = dx;
+  s->dxy[1] = dy;
+  return st_laplacian(dev, s);
+}
+int pfa_device_mobilities(struct CudaData* dev, int, int, int, int, int) {
+  State* s = lookup(dev);
+  if (!s) return fail(PFA_ESTATE, "pfa_device_mobilities: unknown CudaData");
+  if (s->mode != PFA_MODE_COMPAT || !s->varmob) return 0;
+  return st_mobilities(dev, s);
+}
+int pfa_mobility_boundaries(struct CudaData* dev, int, int, int, int, int) {
+  State* s = lookup(dev);
+  if (!s) return fail(PFA_ESTATE, "pfa_mobility_boundaries: unknown CudaData");
+  if (s->mode != PFA_MODE_COMPAT || !s->varmob) return 0;
+  return st_mob_boundaries(dev, s);
 }
 int pfa_device_laplacian_boundaries(struct CudaData* dev, int, int, int, int, int) {
   PFA_CSTAGE(st_lap_boundaries)

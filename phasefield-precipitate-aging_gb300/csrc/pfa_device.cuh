@@ -77,6 +77,95 @@ __device__ __forceinline__ double dg64(double X, double Y) {
   return a * X + b * Y + c;
 }
 
+// ---- variable-mobility Cahn-Hilliard (FP64) ----
+// d2g_<phase>_dx<i><j> as a compile-time constant
+template <int PH, int I, int J>
+__device__ __forceinline__ constexpr double d2g() {
+  return kD2g[PH][I][J];
+}
+
+// dg_<phase>_dx<comp>, thermo/parabola625.c:655-706
+template <int PH, int C>
+__device__ __forceinline__ double dgp64(double X, double Y) {
+  constexpr double a = kDgPh[PH][C][0], b = kDgPh[PH][C][1], c = kDgPh[PH][C][2];
+  return a * X + b * Y + c;
+}
+
+// The composition-dependent diffusivities D_CrCr, D_CrNb, D_NbCr, D_NbNb of
+// thermo/parabola625.c:1860-1894, term by term (mobility prefactors times
+// the exponentials of the mobility exponents, curvature weights).
+__device__ __forceinline__ void dmatrix64(double X, double Y, double D[2][2]) {
+  const double xni = -X - Y + 1;
+  const double eNb = exp(-34.982563536715503 * Y * xni + 14.437947842988088 * Y);
+  const double eCr = exp(-7.1543718172640256 * X * xni + 3.3541967644499233 * X);
+  const double eNi = exp(-8.5221193705645018 * X * xni + 4.0036674816806448 * X -
+                         442.62877981749585 * Y * xni - 0.82164267100913768 * Y);
+  const double s0 = -kHCrCr * X - kHCrNb * Y;  // curvature row of the Cr column
+  const double s1 = -kHCrNb * X - kHNbNb * Y;  // of the Nb column
+  D[0][0] = -kMobPreNb * X * Y * (s0 + kHCrNbAddA) * eNb + kMobPreCr * X * (1 - X) * (s0 + kHCrCrAdd) * eCr -
+            kMobPreNi * X * s0 * xni * eNi;
+  D[0][1] = -kMobPreNb * X * Y * (s1 + kHNbNbAdd) * eNb + kMobPreCr * X * (1 - X) * (s1 + kHCrNbAddB) * eCr -
+            kMobPreNi * X * s1 * xni * eNi;
+  D[1][0] = -kMobPreCr * X * Y * (s0 + kHCrCrAdd) * eCr + kMobPreNb * Y * (1 - Y) * (s0 + kHCrNbAddA) * eNb -
+            kMobPreNi * Y * s0 * xni * eNi;
+  D[1][1] = -kMobPreCr * X * Y * (s1 + kHCrNbAddB) * eCr + kMobPreNb * Y * (1 - Y) * (s1 + kHNbNbAdd) * eNb -
+            kMobPreNi * Y * s1 * xni * eNi;
+}
+
+// The 16 coefficients of the variable-mobility flux at one cell (the
+// reference's disabled mobility_Cr_kernel / mobility_Nb_kernel,
+// src/discretization.cu:175-296).  The reference never defines the mobility
+// matrix those kernels call; here M = D(x) H_gam^-1 (H_gam the gamma
+// curvatures), so that in pure gamma the flux is D(x) grad x^gamma.
+// o[0..7]: Cr row gam_CrCr gam_CrNb del_CrCr del_CrNb lav_CrCr lav_CrNb
+// phi_del_Cr phi_lav_Cr; o[8..15] the Nb row likewise.  xg, xd, xl: the
+// cell's fictitious compositions (Cr, Nb).
+__device__ __forceinline__ void mobility64(double X, double Y, double phd, double phl, double pD,
+                                           double pG, double pL, const double xg[2],
+                                           const double xd[2], const double xl[2], double o[16]) {
+  constexpr double hg00 = d2g<0, 0, 0>(), hg01 = d2g<0, 0, 1>(), hg10 = d2g<0, 1, 0>(),
+                   hg11 = d2g<0, 1, 1>();
+  constexpr double det = hg00 * hg11 - hg01 * hg10;
+  double D[2][2];
+  dmatrix64(X, Y, D);
+  double M[2][2];
+#pragma unroll
+  for (int k = 0; k < 2; k++) {
+    M[k][0] = (D[k][0] * hg11 - D[k][1] * hg10) / det;
+    M[k][1] = (D[k][1] * hg00 - D[k][0] * hg01) / det;
+  }
+  const double dgg0 = dgp64<0, 0>(xg[0], xg[1]), dgg1 = dgp64<0, 1>(xg[0], xg[1]);
+  const double dgd0 = dgp64<1, 0>(xd[0], xd[1]) - dgg0, dgd1 = dgp64<1, 1>(xd[0], xd[1]) - dgg1;
+  const double dgl0 = dgp64<2, 0>(xl[0], xl[1]) - dgg0, dgl1 = dgp64<2, 1>(xl[0], xl[1]) - dgg1;
+  const double ppd = pp64(phd), ppl = pp64(phl);
+  // Cr row (mobility_Cr_kernel, terms 1-8)
+  o[0] = pG * (M[0][0] * d2g<0, 0, 0>() + M[0][1] * d2g<0, 0, 1>());
+  o[1] = pG * (M[0][0] * d2g<0, 1, 0>() + M[0][1] * d2g<0, 1, 1>());
+  o[2] = pD * (M[0][0] * d2g<1, 0, 0>() + M[0][1] * d2g<1, 0, 1>());
+  o[3] = pD * (M[0][0] * d2g<1, 1, 0>() + M[0][1] * d2g<1, 1, 1>());
+  o[4] = pL * (M[0][0] * d2g<2, 0, 0>() + M[0][1] * d2g<2, 0, 1>());
+  o[5] = pL * (M[0][0] * d2g<2, 1, 0>() + M[0][1] * d2g<2, 1, 1>());
+  o[6] = ppd * (M[0][0] * dgd0 + M[0][1] * dgd1);
+  o[7] = ppl * (M[0][0] * dgl0 + M[0][1] * dgl1);
+  // Nb row (mobility_Nb_kernel: its terms 1-6 read d2g_..._dxNbCr where the
+  // Cr kernel reads ..._dxCrNb -- equal, the curvature matrices are symmetric)
+  o[8] = pG * (M[1][0] * d2g<0, 0, 0>() + M[1][1] * d2g<0, 1, 0>());
+  o[9] = pG * (M[1][0] * d2g<0, 1, 0>() + M[1][1] * d2g<0, 1, 1>());
+  o[10] = pD * (M[1][0] * d2g<1, 0, 0>() + M[1][1] * d2g<1, 1, 0>());
+  o[11] = pD * (M[1][0] * d2g<1, 1, 0>() + M[1][1] * d2g<1, 1, 1>());
+  o[12] = pL * (M[1][0] * d2g<2, 0, 0>() + M[1][1] * d2g<2, 1, 0>());
+  o[13] = pL * (M[1][0] * d2g<2, 1, 0>() + M[1][1] * d2g<2, 1, 1>());
+  o[14] = ppd * (M[1][0] * dgd0 + M[1][1] * dgd1);
+  o[15] = ppl * (M[1][0] * dgl0 + M[1][1] * dgl1);
+}
+
+// discrete_laplacian, src/discretization.cu:605-616: the 1D difference of a
+// variable coefficient D times the gradient of c; r2 = 1 / (2 d^2)
+__device__ __forceinline__ double dlap64(double Dl, double Dm, double Dh, double cl, double cm,
+                                         double ch, double r2) {
+  return ((Dh + Dm) * (ch - cm) - (Dm + Dl) * (cm - cl)) * r2;
+}
+
 // ---- FP32 fast forms ----
 __device__ __forceinline__ float p32(float x) {
   const float x2 = x * x;

@@ -19,6 +19,7 @@ struct Step2DArgs {
   void* out[4];
   int Nx, Ny, pitch;    // interior size and row pitch (elements)
   int write_halo;       // also write the mirrored ghost ring
+  int varmob;           // FP64: variable-mobility Cahn-Hilliard (5-point mask)
   int nine;             // 3x3 mask has non-zero corners
   int full_comp;        // FP32 form: compensations as FP32 (16-byte B records)
                         // instead of packed 16-bit counts (8-byte B records)
@@ -57,6 +58,12 @@ struct StageArgs {
   int nx, ny;           // full array extent including the ghost ring
   ModelConst m;
   double mask9[9];
+  // variable-mobility Cahn-Hilliard: the 16 coefficient arrays (Cr row, Nb
+  // row; see dev::mobility64), the spacing of the divergence, and whether
+  // the evolution takes the divergence (x + dt div) instead of D lap x^gamma
+  double* mob[16];
+  double dxy[2];
+  int varmob;
 };
 
 // A batch of 2D grids in the FP32 form (packed compensations) stepped by one
@@ -141,6 +148,12 @@ cudaError_t launch_fictitious(const StageArgs& a, cudaStream_t s);
 cudaError_t launch_convolution(const double* in, double* out, int nx, int ny,
                                const double* mask9, cudaStream_t s);
 cudaError_t launch_evolution(const StageArgs& a, cudaStream_t s);
+// variable mobility: the 16 coefficients at every cell (a.gam/del/lav hold the
+// fictitious compositions), and the divergences of Cr and Nb into a.o[0], a.o[1]
+cudaError_t launch_mobility(const StageArgs& a, cudaStream_t s);
+cudaError_t launch_chem_convolution(const StageArgs& a, cudaStream_t s);
+// the fused FP64 variable-mobility step's one-time set-up (shared memory)
+cudaError_t prepare_step2d_f64();
 cudaError_t launch_dataviz(const double* cr, const double* nb, const double* pd,
                            const double* pl, double* ni, double* phi, int nx, int ny,
                            cudaStream_t s);

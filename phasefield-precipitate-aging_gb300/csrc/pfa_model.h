@@ -48,6 +48,23 @@ constexpr double kDg[2][3] = {
     {15095482346.486225, 110386166481.37187, -9347516202.3169327},
 };
 
+// d g_<phase> / d x_<comp> = a XCR + b XNB + c for every phase (gamma, delta,
+// laves), and the constant curvatures d2 g_<phase> / d x_i d x_j
+// (thermo/parabola625.c:655-706, 1305-1410)
+constexpr double kDgPh[3][2][3] = {
+    {{4534264425.5240498, 15095482346.486225, -2573067053.9739881},
+     {15095482346.486225, 110386166481.37187, -9347516202.3169327}},
+    {{42692985981.597771, 16906497386.287418, -5204511070.9175282},
+     {16906497386.287418, 6170738265863.7695, -1542120310850.303}},
+    {{17733460569.613991, 24191004361.532181, -12878550648.781645},
+     {24191004361.532181, 196588620559.76782, -59817023476.78421}},
+};
+constexpr double kD2g[3][2][2] = {
+    {{4534264425.5240498, 15095482346.486225}, {15095482346.486225, 110386166481.37187}},
+    {{42692985981.597771, 16906497386.287418}, {16906497386.287418, 6170738265863.7695}},
+    {{17733460569.613991, 24191004361.532181}, {24191004361.532181, 196588620559.76782}},
+};
+
 // shared denominator of the fictitious compositions over the monomials
 // [pD^2, pD pG, pD pL, pG^2, pG pL, pL^2]
 constexpr double kDen[6] = {0.001036042775998007, 0.12229015747171917, 0.041785936156220213,

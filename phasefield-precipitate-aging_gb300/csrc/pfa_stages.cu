@@ -7,6 +7,10 @@
 //   device_laplacian  -> 3x3 mask convolution into the *_new arrays (:550-603)
 //   device_evolution  -> CH + AC from those Laplacians (:843-1020)
 //   device_dataviz    -> x_Ni and p(phi_del) + p(phi_lav) (:1211-1229)
+// and, with the variable-mobility Cahn-Hilliard, the reference's disabled
+//   device_mobilities -> the 16 flux coefficients (:175-358)
+//   device_laplacian  -> chemical_convolution_Cr/Nb (:618-778) for x_Cr, x_Nb
+//   device_evolution  -> x + dt div (the commented composition_kernel, :848-856)
 // The fused path (pfa_step2d.cu) is the production form; these kernels let a
 // caller observe every intermediate the reference exposes.
 #include "pfa_device.cuh"
@@ -91,8 +95,13 @@ __global__ void k_evolution(StageArgs a) {
   const ModelConst& M = a.m;
   const double X = a.f[0][i], Y = a.f[1][i], phd = a.f[2][i], phl = a.f[3][i];
   const double lapCr = a.o[0][i], lapNb = a.o[1][i], lapD = a.o[2][i], lapL = a.o[3][i];
-  a.o[0][i] = X + M.dt * (M.D[0][0] * lapCr + M.D[0][1] * lapNb);
-  a.o[1][i] = Y + M.dt * (M.D[1][0] * lapCr + M.D[1][1] * lapNb);
+  if (a.varmob) {  // lapCr, lapNb hold the divergences
+    a.o[0][i] = X + M.dt * lapCr;
+    a.o[1][i] = Y + M.dt * lapNb;
+  } else {
+    a.o[0][i] = X + M.dt * (M.D[0][0] * lapCr + M.D[0][1] * lapNb);
+    a.o[1][i] = Y + M.dt * (M.D[1][0] * lapCr + M.D[1][1] * lapNb);
+  }
   const double pD = p64(phd), pL = p64(phl), pG = 1.0 - pD - pL;
   Poly64 m;
   poly64(pD, pG, pL, m);
@@ -114,6 +123,52 @@ __global__ void k_evolution(StageArgs a) {
     const double dF = -pp64(phl) * gp + 2.0 * M.omega[1] * phl * (phl - 1.0) * (2.0 * phl - 1.0) +
                       2.0 * M.alpha * phl * phd * phd - M.kappa[1] * lapL;
     a.o[3][i] = phl - M.dt * M.L[1] * dF;
+  }
+}
+
+// Every cell, ghost ring included (mobility_Cr/Nb_kernel run over the whole
+// array); the fictitious compositions come from k_fictitious.
+__global__ void k_mobility(StageArgs a) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= a.nx || y >= a.ny) return;
+  const size_t i = size_t(y) * a.nx + x;
+  const double X = a.f[0][i], Y = a.f[1][i], phd = a.f[2][i], phl = a.f[3][i];
+  const double pD = p64(phd), pL = p64(phl), pG = 1.0 - pD - pL;
+  const double xg[2] = {a.gam[0][i], a.gam[1][i]};
+  const double xd[2] = {a.del[0][i], a.del[1][i]};
+  const double xl[2] = {a.lav[0][i], a.lav[1][i]};
+  double o[16];
+  mobility64(X, Y, phd, phl, pD, pG, pL, xg, xd, xl, o);
+#pragma unroll
+  for (int k = 0; k < 16; k++) a.mob[k][i] = o[k];
+}
+
+// chemical_convolution_Cr_kernel / _Nb_kernel at the interior cells (the
+// ghost ring is left to the boundary stage): for the coefficient / field
+// pairs of terms 1-6 the differences along x and along y, for terms 7-8
+// along x only, in the reference's order.
+__global__ void k_chem_convolution(StageArgs a) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (x > a.nx - 2 || y > a.ny - 2) return;
+  const size_t mid = size_t(y) * a.nx + x, lft = mid - 1, rgt = mid + 1, bot = mid - a.nx,
+               top = mid + a.nx;
+  const double r2x = 1.0 / (2.0 * a.dxy[0] * a.dxy[0]), r2y = 1.0 / (2.0 * a.dxy[1] * a.dxy[1]);
+  const double* c[6] = {a.gam[0], a.gam[1], a.del[0], a.del[1], a.lav[0], a.lav[1]};
+#pragma unroll
+  for (int k = 0; k < 2; k++) {
+    double* const* mob = a.mob + 8 * k;
+    double div = 0.0;
+#pragma unroll
+    for (int t = 0; t < 6; t++) {
+      const double* D = mob[t];
+      div += dlap64(D[lft], D[mid], D[rgt], c[t][lft], c[t][mid], c[t][rgt], r2x);
+      div += dlap64(D[bot], D[mid], D[top], c[t][bot], c[t][mid], c[t][top], r2y);
+    }
+    div += dlap64(mob[6][lft], mob[6][mid], mob[6][rgt], a.f[2][lft], a.f[2][mid], a.f[2][rgt], r2x);
+    div += dlap64(mob[7][lft], mob[7][mid], mob[7][rgt], a.f[3][lft], a.f[3][mid], a.f[3][rgt], r2x);
+    a.o[k][mid] = div;
   }
 }
 
@@ -152,6 +207,16 @@ cudaError_t launch_convolution(const double* in, double* out, int nx, int ny, co
 
 cudaError_t launch_evolution(const StageArgs& a, cudaStream_t s) {
   k_evolution<<<grid2(a.nx, a.ny), dim3(32, 8), 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mobility(const StageArgs& a, cudaStream_t s) {
+  k_mobility<<<grid2(a.nx, a.ny), dim3(32, 8), 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_chem_convolution(const StageArgs& a, cudaStream_t s) {
+  k_chem_convolution<<<grid2(a.nx - 2, a.ny - 2), dim3(32, 8), 0, s>>>(a);
   return cudaGetLastError();
 }
 

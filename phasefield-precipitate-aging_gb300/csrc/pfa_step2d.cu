@@ -167,10 +167,141 @@ __global__ void __launch_bounds__(kTX* kBY) k_step2d_f64(Step2DArgs a) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Plain FP64 step with the variable-mobility Cahn-Hilliard (5-point mask):
+// the reference's disabled mobility kernels, chemical_convolution_Cr/Nb
+// (src/discretization.cu:175-358, 618-778) and the commented update of
+// composition_kernel (:848-856), fused.  Each CTA stages its tile and halo:
+// per cell the phases, the six fictitious compositions and the 16 flux
+// coefficients (dev::mobility64, three FP64 exponentials), then forms the
+// divergences (terms 7-8 along x only, as the reference) and the Laplacians
+// of the phases, and updates its interior cells.  Staged arrays are laid out
+// one after another in dynamic shared memory (kVmArrays x kVmCells doubles).
+constexpr int kVmTY = 8;                      // tile height (one row per thread row)
+constexpr int kVmCells = kEX * (kVmTY + 2);   // staged cells (tile + halo)
+constexpr int kVmArrays = 27;                 // phd phl fict[6] mob[16] pD pL rden
+constexpr size_t kVmSmem = sizeof(double) * kVmArrays * kVmCells;
+
+__global__ void __launch_bounds__(kTX* kVmTY) k_step2d_f64_varmob(Step2DArgs a) {
+  extern __shared__ double vm[];
+  auto S = [&](int k, int ex, int ey) -> double& { return vm[k * kVmCells + ey * kEX + ex]; };
+  const double* __restrict__ icr = static_cast<const double*>(a.in[0]);
+  const double* __restrict__ inb = static_cast<const double*>(a.in[1]);
+  const double* __restrict__ ipd = static_cast<const double*>(a.in[2]);
+  const double* __restrict__ ipl = static_cast<const double*>(a.in[3]);
+  const int x0 = blockIdx.x * kTX, y0 = blockIdx.y * kVmTY;
+  const int tid = threadIdx.y * kTX + threadIdx.x;
+  for (int e = tid; e < kVmCells; e += kTX * kVmTY) {
+    const int ex = e % kEX, ey = e / kEX;
+    const int gx = clampi(x0 + ex - 1, 0, a.Nx - 1);
+    const int gy = clampi(y0 + ey - 1, 0, a.Ny - 1);
+    const size_t i = size_t(gy + 1) * a.pitch + gx + 1;
+    const double X = icr[i], Y = inb[i], phd = ipd[i], phl = ipl[i];
+    const double pD = p64(phd), pL = p64(phl), pG = 1.0 - pD - pL;
+    Poly64 m;
+    poly64(pD, pG, pL, m);
+    const double xg[2] = {fict64<0, 0>(X, Y, m), fict64<0, 1>(X, Y, m)};
+    const double xd[2] = {fict64<1, 0>(X, Y, m), fict64<1, 1>(X, Y, m)};
+    const double xl[2] = {fict64<2, 0>(X, Y, m), fict64<2, 1>(X, Y, m)};
+    double mob[16];
+    mobility64(X, Y, phd, phl, pD, pG, pL, xg, xd, xl, mob);
+    S(0, ex, ey) = phd;
+    S(1, ex, ey) = phl;
+    S(2, ex, ey) = xg[0];
+    S(3, ex, ey) = xg[1];
+    S(4, ex, ey) = xd[0];
+    S(5, ex, ey) = xd[1];
+    S(6, ex, ey) = xl[0];
+    S(7, ex, ey) = xl[1];
+#pragma unroll
+    for (int k = 0; k < 16; k++) S(8 + k, ex, ey) = mob[k];
+    S(24, ex, ey) = pD;
+    S(25, ex, ey) = pL;
+    S(26, ex, ey) = m.rden;
+  }
+  __syncthreads();
+
+  const ModelConst& M = a.m;
+  const int gx = x0 + threadIdx.x, gy = y0 + threadIdx.y;
+  if (gx >= a.Nx || gy >= a.Ny) return;
+  const int ex = threadIdx.x + 1, ey = threadIdx.y + 1;
+  const double r2x = 0.5 * M.idx2[0], r2y = 0.5 * M.idx2[1];  // 1 / (2 d^2)
+  double div[2];
+#pragma unroll
+  for (int k = 0; k < 2; k++) {
+    const int mb = 8 + 8 * k;  // this component's coefficients
+    double d = 0.0;
+#pragma unroll
+    for (int t = 0; t < 6; t++) {
+      const int D = mb + t, c = 2 + t;
+      d += dlap64(S(D, ex - 1, ey), S(D, ex, ey), S(D, ex + 1, ey), S(c, ex - 1, ey), S(c, ex, ey),
+                  S(c, ex + 1, ey), r2x);
+      d += dlap64(S(D, ex, ey - 1), S(D, ex, ey), S(D, ex, ey + 1), S(c, ex, ey - 1), S(c, ex, ey),
+                  S(c, ex, ey + 1), r2y);
+    }
+    d += dlap64(S(mb + 6, ex - 1, ey), S(mb + 6, ex, ey), S(mb + 6, ex + 1, ey), S(0, ex - 1, ey),
+                S(0, ex, ey), S(0, ex + 1, ey), r2x);
+    d += dlap64(S(mb + 7, ex - 1, ey), S(mb + 7, ex, ey), S(mb + 7, ex + 1, ey), S(1, ex - 1, ey),
+                S(1, ex, ey), S(1, ex + 1, ey), r2x);
+    div[k] = d;
+  }
+  auto lap = [&](int k) {
+    double v = M.mask[0] * S(k, ex, ey - 1);
+    v = fma(M.mask[1], S(k, ex - 1, ey), v);
+    v = fma(M.mask[2], S(k, ex, ey), v);
+    v = fma(M.mask[3], S(k, ex + 1, ey), v);
+    return fma(M.mask[4], S(k, ex, ey + 1), v);
+  };
+  const double lapD = lap(0), lapL = lap(1);
+  const size_t i = size_t(gy + 1) * a.pitch + gx + 1;
+  const double X = icr[i], Y = inb[i];
+  const double phd = S(0, ex, ey), phl = S(1, ex, ey);
+  const double ocr = X + M.dt * div[0];
+  const double onb = Y + M.dt * div[1];
+  // Allen-Cahn, src/discretization.cu:888-980, as in k_step2d_f64
+  const double gam_Cr = S(2, ex, ey), gam_Nb = S(3, ex, ey);
+  const double gam_nrg = g64<0>(gam_Cr, gam_Nb);
+  const double dgGdxCr = dg64<0>(gam_Cr, gam_Nb);
+  const double dgGdxNb = dg64<1>(gam_Cr, gam_Nb);
+  double od, ol;
+  {
+    const double del_Cr = S(4, ex, ey), del_Nb = S(5, ex, ey);
+    const double del_nrg = g64<1>(del_Cr, del_Nb);
+    const double gp = gam_nrg - del_nrg - dgGdxCr * (gam_Cr - del_Cr) - dgGdxNb * (gam_Nb - del_Nb);
+    const double dF = -pp64(phd) * gp + 2.0 * M.omega[0] * phd * (phd - 1.0) * (2.0 * phd - 1.0) +
+                      2.0 * M.alpha * phd * phl * phl - M.kappa[0] * lapD;
+    od = phd - M.dt * M.L[0] * dF;
+  }
+  {
+    const double lav_Cr = S(6, ex, ey), lav_Nb = S(7, ex, ey);
+    const double lav_nrg = g64<2>(lav_Cr, lav_Nb);
+    const double gp = gam_nrg - lav_nrg - dgGdxCr * (gam_Cr - lav_Cr) - dgGdxNb * (gam_Nb - lav_Nb);
+    const double dF = -pp64(phl) * gp + 2.0 * M.omega[1] * phl * (phl - 1.0) * (2.0 * phl - 1.0) +
+                      2.0 * M.alpha * phl * phd * phd - M.kappa[1] * lapL;
+    ol = phl - M.dt * M.L[1] * dF;
+  }
+  const bool h = a.write_halo;
+  store_with_halo(static_cast<double*>(a.out[0]), a.pitch, gx, gy, a.Nx, a.Ny, ocr, h);
+  store_with_halo(static_cast<double*>(a.out[1]), a.pitch, gx, gy, a.Nx, a.Ny, onb, h);
+  store_with_halo(static_cast<double*>(a.out[2]), a.pitch, gx, gy, a.Nx, a.Ny, od, h);
+  store_with_halo(static_cast<double*>(a.out[3]), a.pitch, gx, gy, a.Nx, a.Ny, ol, h);
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
+cudaError_t prepare_step2d_f64() {
+  return cudaFuncSetAttribute(k_step2d_f64_varmob, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              int(kVmSmem));
+}
+
 cudaError_t launch_step2d_f64(const Step2DArgs& a, cudaStream_t s) {
+  if (a.varmob) {
+    if (a.nine) return cudaErrorInvalidValue;
+    dim3 grid((a.Nx + kTX - 1) / kTX, (a.Ny + kVmTY - 1) / kVmTY);
+    k_step2d_f64_varmob<<<grid, dim3(kTX, kVmTY), kVmSmem, s>>>(a);
+    return cudaGetLastError();
+  }
   dim3 grid((a.Nx + kTX - 1) / kTX, (a.Ny + kTY - 1) / kTY);
   dim3 block(kTX, kBY);
   if (a.nine)

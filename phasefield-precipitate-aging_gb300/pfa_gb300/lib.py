@@ -15,6 +15,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "libpfa_gb300.so")
 
 FP64, FP32, FP32_KPHI = 0, 1, 2
+MOBILITY_CONSTANT, MOBILITY_VARIABLE = 0, 1
 MODE_FUSED, MODE_COMPAT = 0, 1
 NUC_REFERENCE_GEOMETRY, NUC_FIXED_GEOMETRY = 0, 1
 PRECISIONS = {"fp64": FP64, "fp32": FP32, "fp32k": FP32_KPHI}
@@ -116,6 +117,9 @@ def load():
         "pfa_set_mode": (_i, [P, _i]),
         "pfa_set_precision": (_i, [P, _i]),
         "pfa_set_nucleation": (_i, [P, ctypes.c_uint64, _i]),
+        "pfa_set_mobility": (_i, [P, _i]),
+        "pfa_device_mobilities": (_i, [P, _i, _i, _i, _i, _i]),
+        "pfa_mobility_boundaries": (_i, [P, _i, _i, _i, _i, _i]),
         "pfa_set_nucleation_args": (_i, [P, _i, _d, _d, _d, _d, _d, _d, _d]),
         "pfa_init_cuda": (_i, [P, _i, _i, _i, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
         "pfa_free_cuda": (_i, [P]),
@@ -252,7 +256,8 @@ def model_params(dx=5e-9, ifce_width=10e-9, xcr0=0.30, xnb0=0.02, meshres=None, 
 class Grid2D:
     """One 2D grid behind the reference's CudaData interface."""
 
-    def __init__(self, fields, params, precision="fp64", mode="fused", mask=None):
+    def __init__(self, fields, params, precision="fp64", mode="fused", mask=None,
+                 mobility="constant"):
         L = load()
         self.L = L
         f = [np.ascontiguousarray(a, dtype=np.float64) for a in fields]
@@ -272,6 +277,9 @@ class Grid2D:
         if mode == "compat":
             check(L.pfa_set_mode(ctypes.byref(self.dev), MODE_COMPAT), "pfa_set_mode")
         self.set_precision(precision)
+        if mobility != "constant":
+            check(L.pfa_set_mobility(ctypes.byref(self.dev),
+                                     {"variable": MOBILITY_VARIABLE}[mobility]), "pfa_set_mobility")
 
     @property
     def ref(self):
@@ -309,6 +317,8 @@ class Grid2D:
         check(L.pfa_device_boundaries(*a), "device_boundaries")
         check(L.pfa_device_fictitious(*a), "device_fictitious")
         check(L.pfa_fictitious_boundaries(*a), "fictitious_boundaries")
+        check(L.pfa_device_mobilities(*a), "device_mobilities")
+        check(L.pfa_mobility_boundaries(*a), "mobility_boundaries")
         check(L.pfa_device_laplacian(*a, self.params["dx"], self.params.get("dy", self.params["dx"])),
               "device_laplacian")
         check(L.pfa_device_laplacian_boundaries(*a), "device_laplacian_boundaries")

@@ -140,6 +140,38 @@ def free_energy(ref):
                                          prm.omega[0], prm.omega[1], 1.07e11]))
 
 
+def varmob(ref):
+    """The variable-mobility form with the reference's compiled energies,
+    diffusivities, chemical-potential derivatives and curvatures
+    (thermo/parabola625.c) through ref_shim.cpp: the derivatives at sample
+    compositions, and the steps of step2d_varmob from two grids."""
+    out = {}
+    rng = np.random.default_rng(7)
+    x = rng.uniform(0.0, 0.6, 200)
+    y = rng.uniform(0.0, 0.3, 200)
+    out["x"], out["y"] = x, y
+    for ph in range(3):
+        for c in range(2):
+            out[f"dg_{ph}_{c}"] = ref.dg(ph, c, x, y)
+        out[f"d2g_{ph}"] = np.array([[ref.d2g(ph, i, j) for j in range(2)] for i in range(2)])
+    grids = [ic.grid2d(30, 22, seed=11, stripe_width=10, n_particles=4, radius=4.0),
+             ic.grid2d(41, 37, seed=12, stripe_width=12, n_particles=2, radius=5.0)]
+    p = O.model_params()
+    for g, f0 in enumerate(grids):
+        for j, n in enumerate(("cr", "nb", "pd", "pl")):
+            out[f"g{g}_ic_{n}"] = f0[j]
+        done, f = 0, f0
+        for k in (1, 10, 60):
+            f = ref.run2d_varmob(f, p, k - done)
+            done = k
+            for j, n in enumerate(("cr", "nb", "pd", "pl")):
+                out[f"g{g}_s{k}_{n}"] = f[j]
+        dv = ref.chem_div2d(f0, p.dx, p.dy)
+        out[f"g{g}_div_cr"], out[f"g{g}_div_nb"] = dv
+    out["params"] = np.array([p.dt, p.dx])
+    np.savez_compressed(os.path.join(HERE, "step2d_varmob.npz"), **out)
+
+
 IC_RECIPES = [
     # particles embedded with embed_OPC's box and overwrite (particle_mode 1),
     # integer centres as the reference's (MMSP grid positions), boxes inside
@@ -233,7 +265,7 @@ def main():
     sets = {"energies": lambda: energies(ref, rng), "steps": lambda: steps(ref),
             "nucleation": lambda: nucleation(ref), "summary": lambda: summary(ref),
             "energy": lambda: free_energy(ref), "abi": lambda: abi_symbols(args.ref),
-            "ic": lambda: initial_conditions(ref)}
+            "ic": lambda: initial_conditions(ref), "varmob": lambda: varmob(ref)}
     for name, fn in sets.items():
         if not args.only or name in args.only:
             fn()

@@ -11,6 +11,12 @@ output: host tanh differs in the last bits between machines):
   refdt  : step2d_refdt.npz's grid, the reference's own dt rule, 50 steps
   config1: 256 x 256 (one stripe, four particles), KKS-stable dt, 1000 steps
 
+in ref_gpu_varmob.npz, the divergences of the reference's compiled (never
+launched) chemical_convolution_Cr/Nb kernels on two states (step2d.npz's
+grid, and the 256 x 256 workload after 1000 steps), given the fictitious
+compositions and mobility coefficients of the oracle's variable-mobility
+restatement (the reference's own mobility kernels are commented out);
+
 and, in ref_gpu_nucleation.npz, the event counts of the reference's own
 nucleation kernel (src/discretization.cu:1079-1177, clock-seeded curand) in
 four independent calls on a uniform enriched 512 x 512 grid whose nuclei
@@ -19,6 +25,8 @@ cover one cell each.
     python tests/golden/make_ref_gpu_golden.py [--cubin oracle/_ref/ref_step.cubin]
                                                [--out tests/golden/ref_gpu_step2d.npz]
                                                [--nuc-out tests/golden/ref_gpu_nucleation.npz]
+                                               [--varmob-out tests/golden/ref_gpu_varmob.npz]
+                                               [--only varmob]
 """
 import argparse
 import os
@@ -44,14 +52,34 @@ NUC_CALLS = 4
 
 def main():
     import oracle as O
-    from ref_gpu import CUBIN, Driver, run_reference, run_reference_nucleation
+    from ref_gpu import (CUBIN, Driver, run_reference, run_reference_chem_div,
+                         run_reference_nucleation)
     from pfa_gb300 import ic
     ap = argparse.ArgumentParser()
     ap.add_argument("--cubin", default=CUBIN)
     ap.add_argument("--out", default=os.path.join(HERE, "ref_gpu_step2d.npz"))
     ap.add_argument("--nuc-out", default=os.path.join(HERE, "ref_gpu_nucleation.npz"))
+    ap.add_argument("--varmob-out", default=os.path.join(HERE, "ref_gpu_varmob.npz"))
+    ap.add_argument("--only", default="", help="varmob: only that set")
     args = ap.parse_args()
     drv = Driver(args.cubin)
+    # variable-mobility divergences of the reference's chemical_convolution kernels
+    orc = O.Oracle()
+    vm = {}
+    states = [[np.load(os.path.join(HERE, "step2d.npz"))[f"ic_{n}"] for n in NAMES],
+              [np.load(os.path.join(HERE, "ref_gpu_step2d.npz"))[f"config1_s1000_{n}"]
+               for n in NAMES]]
+    dxy = (5e-9, 5e-9)
+    for k, st in enumerate(states):
+        fict, mob = orc.mobility2d(st)
+        div = run_reference_chem_div(drv, st, fict, mob, *dxy)
+        for j, n in enumerate(NAMES):
+            vm[f"s{k}_{n}"] = st[j]
+        vm[f"s{k}_div_cr"], vm[f"s{k}_div_nb"] = div
+    np.savez_compressed(args.varmob_out, dxy=np.array(dxy), **vm)
+    print("reference GPU variable-mobility divergences written to", args.varmob_out)
+    if args.only == "varmob":
+        return
     res = {}
     g = np.load(os.path.join(HERE, "step2d.npz"))
     f = [g[f"ic_{n}"] for n in NAMES]

@@ -176,3 +176,35 @@ def test_reference_nucleation_kernel_rate_matches_oracle_probability(orc):
         for k in list(counts[:, ph]) + [int(counts[:, ph].sum())]:
             m = n * P[ph] * (len(counts) if k == counts[:, ph].sum() else 1)
             assert abs(k - m) < 5 * np.sqrt(m * (1 - P[ph])), (ph, k, m)
+
+
+def test_variable_mobility_matches_reference(orc):
+    """The variable-mobility restatement (step2d_varmob: the reference's
+    disabled mobility and chemical_convolution kernels,
+    src/discretization.cu:175-358, 618-778) against the same semantics built
+    on the reference's compiled functions (tests/golden/step2d_varmob.npz):
+    chemical-potential derivatives and curvatures of all three phases, the
+    divergences, and 1, 10, 60 steps on two grids."""
+    g = golden("step2d_varmob.npz")
+    x, y = g["x"], g["y"]
+    for ph in range(3):
+        for c in range(2):
+            want = g[f"dg_{ph}_{c}"]
+            assert np.max(np.abs(orc.dg(ph, c, x, y) - want)) <= 1e-14 * np.max(np.abs(want))
+        for i in range(2):
+            for j in range(2):
+                assert orc.d2g(ph, i, j) == g[f"d2g_{ph}"][i, j]
+    p = O.model_params()
+    assert p.dt == g["params"][0] and p.dx == g["params"][1]
+    for k in range(2):
+        f0 = [g[f"g{k}_ic_{n}"] for n in ("cr", "nb", "pd", "pl")]
+        div = orc.chem_div2d(f0, p.dx, p.dy)
+        for a, n in zip(div, ("cr", "nb")):
+            want = g[f"g{k}_div_{n}"]
+            assert np.max(np.abs(a - want)) <= 1e-12 * np.max(np.abs(want)), (k, n)
+        done, f = 0, f0
+        for s in (1, 10, 60):
+            f = orc.run2d_varmob(f, p, s - done)
+            done = s
+            err = field_err(f, [g[f"g{k}_s{s}_{n}"] for n in ("cr", "nb", "pd", "pl")])
+            assert max(err) <= 1e-12, (k, s, err)
