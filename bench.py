@@ -363,6 +363,11 @@ def grid4096(c, quick_error=True):
     ms64 = g64.run_timed(STEPS_PER_BENCH_STEP)
     g64.close()
     fp64_value = cells * STEPS_PER_BENCH_STEP / (ms64 / 1e3)
+    # the variable-mobility form (FP64) on the same grid
+    gv = pl.Grid2D(fields, params, precision="fp64", mobility="variable")
+    gv.run(2)
+    msv = gv.run_timed(10) / 10
+    gv.close()
 
     err = None
     if quick_error:
@@ -452,7 +457,11 @@ def grid4096(c, quick_error=True):
         "fp64": {"value": fp64_value, "unit": "cell-updates/s",
                  "ms_per_step": ms64, "speedup_fp32_over_fp64": value / ws / fp64_value,
                  "fp64_flops_per_cell": profiled_value("step2d_f64_4096", "fp64_flops_per_cell"),
-                 "bound": "FP64 pipe"},
+                 "bound": "FP64 pipe",
+                 "variable_mobility": {"value": cells / (msv / 1e3), "unit": "cell-updates/s",
+                                       "ms_per_step": msv,
+                                       "what": "the reference's disabled variable-mobility "
+                                               "Cahn-Hilliard, FP64 (pfa_set_mobility)"}},
         "roofline": roof,
         "cpu_baseline": cpu,
         "reference_gpu": ref_gpu,
