@@ -42,7 +42,10 @@ enum {
 enum { PFA_MODE_FUSED = 0, PFA_MODE_COMPAT = 1 };
 /* PFA_FP32: FP32 arithmetic, every field Kahan-compensated with the
  * compensations packed as 16-bit counts (48 bytes per cell update);
- * PFA_FP32_KPHI: the same with FP32 compensations (64 bytes per cell). */
+ * PFA_FP32_KPHI: the same with FP32 compensations (64 bytes per cell).
+ * Both take the 5- or the 9-point mask of src/mesh.cpp:187-213 (any 3x3
+ * mask with equal corners, equal left / right and equal upper / lower
+ * weights; a step with another mask fails with PFA_EINVAL). */
 enum { PFA_FP64 = 0, PFA_FP32 = 1, PFA_FP32_KPHI = 2 };
 enum { PFA_NUC_REFERENCE_GEOMETRY = 0, PFA_NUC_FIXED_GEOMETRY = 1 };
 /* Cahn-Hilliard: the reference's constant diffusivity matrix (its loop's

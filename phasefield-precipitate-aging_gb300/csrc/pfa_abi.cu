@@ -72,6 +72,7 @@ struct State {
   int mode = PFA_MODE_FUSED, precision = PFA_FP64;
   double mask9[9] = {};
   bool five_point = true;
+  bool symmetric = true;  // corners, left / right and upper / lower weights equal (FP32 form)
   ModelConst m{};
   FastCoef fk{};
   cudaStream_t st = nullptr;
@@ -216,6 +217,15 @@ static Step2DArgs step_args(State* s, double alpha, double dt) {
   a.alpha2 = float(2.0 * alpha);
   a.idx2f[0] = float(s->m.idx2[0]);
   a.idx2f[1] = float(s->m.idx2[1]);
+  if (a.nine) {
+    double sum = 0.0;
+    for (double w : s->mask9) sum += w;
+    a.lap9[0] = float(s->mask9[3]);
+    a.lap9[1] = float(s->mask9[1]);
+    a.lap9[2] = float(s->mask9[0]);
+    a.lap9[3] = float(sum);
+    for (int k = 0; k < 2; k++) a.lap9xe[k] = float(sum * kXe[0][k]);
+  }
   return a;
 }
 
@@ -236,7 +246,8 @@ static int fused_step(CudaData* dev, State* s, double alpha, double dt) {
     CK(launch_step2d_f64(a, s->st));
     return 0;
   }
-  if (!s->five_point) return fail(PFA_EINVAL, "the FP32 form needs the 5-point mask");
+  if (!s->symmetric)
+    return fail(PFA_EINVAL, "the FP32 form needs a symmetric mask (equal corners, left / right, upper / lower)");
   if (int r = f32_import(dev, s)) return r;
   const int c = s->cur, n = 1 - c;
   a.in[0] = s->recA[c];
@@ -550,6 +561,8 @@ static int init_core(CudaData* dev, int nx, int ny, int nm, const double* mask,
   s->Ny = ny - 2;
   std::memcpy(s->mask9, mask, sizeof(s->mask9));
   s->five_point = mask[0] == 0.0 && mask[2] == 0.0 && mask[6] == 0.0 && mask[8] == 0.0;
+  s->symmetric = mask[0] == mask[2] && mask[0] == mask[6] && mask[0] == mask[8] &&
+                 mask[1] == mask[7] && mask[3] == mask[5];
   for (int i = 0; i < 2; i++) {
     s->m.D[0][i] = D_Cr[i];
     s->m.D[1][i] = D_Nb[i];

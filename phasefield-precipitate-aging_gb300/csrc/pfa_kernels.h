@@ -32,6 +32,9 @@ struct Step2DArgs {
   float alpha2;         // 2 alpha
   float kap[2];         // kappa
   float idx2f[2];       // 1/dx^2, 1/dy^2
+  float lap9[4];        // FP32 form, 9-point mask (symmetric): left / right weight,
+                        // upper / lower weight, corner weight, sum of the nine
+  float lap9xe[2];      // the sum of the nine weights times xe_gamma (Cr, Nb)
   int rows;             // FP32 form: rows per warp segment (set by the launcher)
 };
 

@@ -46,6 +46,17 @@ struct Nb {
   float u1, u2, pd, pl;
 };
 
+// With the 9-point mask a row also carries its x-difference sums
+// h = (v_w - v) + (v_e - v), formed once per row (two shuffles per field),
+// so the diagonal neighbours of the rows above and below cost no shuffles.
+struct Nb9 {
+  float u1, u2, pd, pl;
+  float h1, h2, hd, hl;
+};
+
+template <bool NINE>
+using NbT = typename std::conditional<NINE, Nb9, Nb>::type;
+
 // Compensation record: packed 16-bit counts or four FP32 values.
 template <bool PACK>
 using CompT = typename std::conditional<PACK, uint2, float4>::type;
@@ -97,7 +108,7 @@ __device__ __forceinline__ float2 comps_x(const CompT<PACK>& c) {
   }
 }
 
-template <bool PACK>
+template <bool PACK, bool NINE>
 struct Stream {
   const Step2DArgs& a;
   const float4* A;        // this lane's column, row 0
@@ -114,27 +125,47 @@ struct Stream {
   }
 
   // update row y from its window (up, c, dn); rc = raw centre record
-  __device__ __forceinline__ void update(int y, const Nb& up, const Nb& c, const Nb& dn,
-                                         const Raw<PACK>& rc) const {
-    Nb w, e;
-    w.u1 = __shfl_up_sync(0xffffffffu, c.u1, 1);
-    w.u2 = __shfl_up_sync(0xffffffffu, c.u2, 1);
-    w.pd = __shfl_up_sync(0xffffffffu, c.pd, 1);
-    w.pl = __shfl_up_sync(0xffffffffu, c.pl, 1);
-    e.u1 = __shfl_down_sync(0xffffffffu, c.u1, 1);
-    e.u2 = __shfl_down_sync(0xffffffffu, c.u2, 1);
-    e.pd = __shfl_down_sync(0xffffffffu, c.pd, 1);
-    e.pl = __shfl_down_sync(0xffffffffu, c.pl, 1);
-    const float idx2 = a.idx2f[0], idy2 = a.idx2f[1];
-    auto lap = [&](float vw, float ve, float vn, float vs, float vc) {
-      const float sx = (vw - vc) + (ve - vc);
-      const float sy = (vn - vc) + (vs - vc);
-      return fmaf(sx, idx2, sy * idy2);
-    };
-    const float lapCr = lap(w.u1, e.u1, up.u1, dn.u1, c.u1);
-    const float lapNb = lap(w.u2, e.u2, up.u2, dn.u2, c.u2);
-    const float lapD = lap(w.pd, e.pd, up.pd, dn.pd, c.pd);
-    const float lapL = lap(w.pl, e.pl, up.pl, dn.pl, c.pl);
+  __device__ __forceinline__ void update(int y, const NbT<NINE>& up, const NbT<NINE>& c,
+                                         const NbT<NINE>& dn, const Raw<PACK>& rc) const {
+    float lapCr, lapNb, lapD, lapL;
+    if constexpr (NINE) {
+      // sum over the eight neighbours of w (v - v_c): with sy = (v_up - v_c)
+      // + (v_dn - v_c) the corners add up to h_up + h_dn + 2 sy; then the
+      // sum of the nine weights times the centre value (zero for dx = dy up
+      // to rounding; k = that sum times xe_gamma for the deviations u)
+      const float ex = a.lap9[0], ey = a.lap9[1], cw = a.lap9[2], sw = a.lap9[3];
+      auto lap = [&](float hu, float hc, float hd, float vu, float vc, float vd, float k) {
+        const float sy = (vu - vc) + (vd - vc);
+        float t = fmaf(sw, vc, k);
+        t = fmaf(cw, fmaf(2.0f, sy, hu + hd), t);
+        t = fmaf(ey, sy, t);
+        return fmaf(ex, hc, t);
+      };
+      lapCr = lap(up.h1, c.h1, dn.h1, up.u1, c.u1, dn.u1, a.lap9xe[0]);
+      lapNb = lap(up.h2, c.h2, dn.h2, up.u2, c.u2, dn.u2, a.lap9xe[1]);
+      lapD = lap(up.hd, c.hd, dn.hd, up.pd, c.pd, dn.pd, 0.0f);
+      lapL = lap(up.hl, c.hl, dn.hl, up.pl, c.pl, dn.pl, 0.0f);
+    } else {
+      Nb w, e;
+      w.u1 = __shfl_up_sync(0xffffffffu, c.u1, 1);
+      w.u2 = __shfl_up_sync(0xffffffffu, c.u2, 1);
+      w.pd = __shfl_up_sync(0xffffffffu, c.pd, 1);
+      w.pl = __shfl_up_sync(0xffffffffu, c.pl, 1);
+      e.u1 = __shfl_down_sync(0xffffffffu, c.u1, 1);
+      e.u2 = __shfl_down_sync(0xffffffffu, c.u2, 1);
+      e.pd = __shfl_down_sync(0xffffffffu, c.pd, 1);
+      e.pl = __shfl_down_sync(0xffffffffu, c.pl, 1);
+      const float idx2 = a.idx2f[0], idy2 = a.idx2f[1];
+      auto lap = [&](float vw, float ve, float vn, float vs, float vc) {
+        const float sx = (vw - vc) + (ve - vc);
+        const float sy = (vn - vc) + (vs - vc);
+        return fmaf(sx, idx2, sy * idy2);
+      };
+      lapCr = lap(w.u1, e.u1, up.u1, dn.u1, c.u1);
+      lapNb = lap(w.u2, e.u2, up.u2, dn.u2, c.u2);
+      lapD = lap(w.pd, e.pd, up.pd, dn.pd, c.pd);
+      lapL = lap(w.pl, e.pl, up.pl, dn.pl, c.pl);
+    }
     const float4 cc = comps<PACK>(rc.c);
     // Cahn-Hilliard
     const float X = rc.a.x, Y = rc.a.y;
@@ -166,7 +197,7 @@ struct Stream {
 // directly (one row ahead, !STAGED) or through the warp's staging ring
 // (STAGED): the batched kernel's units are short, and the ring's deeper
 // prefetch hides the start-up latency each unit pays.
-template <bool PACK, bool STAGED>
+template <bool PACK, bool STAGED, bool NINE = false>
 __device__ __forceinline__ void stream_strip(const Step2DArgs& a, const float4* Ain,
                                              const CompT<PACK>* Bin, float4* Aout,
                                              CompT<PACK>* Bout, int Nx, int Ny, int P, int x0,
@@ -174,12 +205,13 @@ __device__ __forceinline__ void stream_strip(const Step2DArgs& a, const float4* 
   const int lane = threadIdx.x & 31;
   const int gx = x0 - 1 + lane;  // lanes 0 and 31 hold the neighbour columns
   const int cx = min(max(gx, 0), Nx - 1);
+  static_assert(!(STAGED && NINE), "the staged (batched) form has the 5-point mask only");
   const FastCoef& K = a.k;
-  const Stream<PACK> S{a, Ain + cx, Bin + cx, Aout + cx, Bout + cx,
-                       Ny, P, lane >= 1 && lane <= kCols && gx < Nx};
+  const Stream<PACK, NINE> S{a, Ain + cx, Bin + cx, Aout + cx, Bout + cx,
+                             Ny, P, lane >= 1 && lane <= kCols && gx < Nx};
   auto solve_raw = [&](const Raw<PACK>& r) {
     const float2 cxy = comps_x<PACK>(r.c);
-    Nb n;
+    NbT<NINE> n;
     n.pd = r.a.z;
     n.pl = r.a.w;
     // warp-uniform choice: a row of pure gamma needs no solve
@@ -187,12 +219,21 @@ __device__ __forceinline__ void stream_strip(const Step2DArgs& a, const float4* 
       gamma_bulk32(K, r.a.x, r.a.y, cxy.x, cxy.y, n.u1, n.u2);
     else
       gamma_u32(K, r.a.x, r.a.y, cxy.x, cxy.y, r.a.z, r.a.w, n.u1, n.u2);
+    if constexpr (NINE) {
+      auto hx = [](float v) {
+        return (__shfl_up_sync(0xffffffffu, v, 1) - v) + (__shfl_down_sync(0xffffffffu, v, 1) - v);
+      };
+      n.h1 = hx(n.u1);
+      n.h2 = hx(n.u2);
+      n.hd = hx(n.pd);
+      n.hl = hx(n.pl);
+    }
     return n;
   };
   if constexpr (!STAGED) {
     // window rows y-1, y, y+1 and raw records of rows y, y+1, y+2
     Raw<PACK> r0 = S.load(S.row(y0)), r1 = S.load(S.row(y0 + 1)), r2;
-    Nb n0 = solve_raw(S.load(S.row(y0 - 1))), n1 = solve_raw(r0), n2;
+    NbT<NINE> n0 = solve_raw(S.load(S.row(y0 - 1))), n1 = solve_raw(r0), n2;
     // three rows per iteration with rotated roles: no register moves
     int y = y0;
     for (; y + 2 < y1; y += 3) {
@@ -265,14 +306,15 @@ __device__ __forceinline__ void stream_strip(const Step2DArgs& a, const float4* 
 
 // The packed form fits 9 CTAs per SM (56 registers, no spills): the extra
 // warps cover load latency (4096^2: 0.1303 ms vs 0.1369 ms at 8); the FP32
-// compensation form is faster at 8.
-template <bool PACK>
-__global__ void __launch_bounds__(32 * kWarps, PACK ? 9 : 8) k_stream_f32(Step2DArgs a) {
+// compensation form is faster at 8.  NINE: the 9-point mask (a window of
+// eight values per row).
+template <bool PACK, bool NINE>
+__global__ void __launch_bounds__(32 * kWarps, PACK && !NINE ? 9 : 8) k_stream_f32(Step2DArgs a) {
   const int strip = blockIdx.x * kWarps + (threadIdx.x >> 5);
   const int x0 = strip * kCols;  // first output column of the strip
   if (x0 >= a.Nx) return;        // whole warp leaves together
   const int y0 = blockIdx.y * a.rows;
-  stream_strip<PACK, false>(a, static_cast<const float4*>(a.in[0]),
+  stream_strip<PACK, false, NINE>(a, static_cast<const float4*>(a.in[0]),
                             static_cast<const CompT<PACK>*>(a.in[1]),
                             static_cast<float4*>(a.out[0]), static_cast<CompT<PACK>*>(a.out[1]),
                             a.Nx, a.Ny, a.pitch, x0, y0, min(y0 + a.rows, a.Ny), nullptr);
@@ -378,7 +420,8 @@ int segment_rows(int Nx, int Ny, int resident) {
   return best;
 }
 
-int g_resident[3] = {0, 0, 0};  // resident CTAs: FP32 / packed variants, the batch kernel
+// resident CTAs: FP32 / packed variants, the batch kernel, the 9-point FP32 / packed variants
+int g_resident[5] = {0, 0, 0, 0, 0};
 
 template <typename K>
 cudaError_t query_resident(K kernel, int slot) {
@@ -391,27 +434,31 @@ cudaError_t query_resident(K kernel, int slot) {
   return e;
 }
 
-template <bool PACK>
+template <bool PACK, bool NINE>
 cudaError_t launch_stream(Step2DArgs a, cudaStream_t s) {
-  const int resident = g_resident[PACK] > 0 ? g_resident[PACK] : 152 * 8;
+  const int slot = NINE ? 3 + PACK : PACK;
+  const int resident = g_resident[slot] > 0 ? g_resident[slot] : 152 * 8;
   a.rows = segment_rows(a.Nx, a.Ny, resident);
   const int strips = (a.Nx + kCols - 1) / kCols;
   dim3 grid((strips + kWarps - 1) / kWarps, (a.Ny + a.rows - 1) / a.rows);
-  k_stream_f32<PACK><<<grid, 32 * kWarps, 0, s>>>(a);
+  k_stream_f32<PACK, NINE><<<grid, 32 * kWarps, 0, s>>>(a);
   return cudaGetLastError();
 }
 
 }  // namespace
 
 cudaError_t launch_step2d_f32(const Step2DArgs& a, cudaStream_t s) {
-  return a.full_comp ? launch_stream<false>(a, s) : launch_stream<true>(a, s);
+  if (a.nine) return a.full_comp ? launch_stream<false, true>(a, s) : launch_stream<true, true>(a, s);
+  return a.full_comp ? launch_stream<false, false>(a, s) : launch_stream<true, false>(a, s);
 }
 
 // occupancy of the FP32 kernels on the current device (outside any capture)
 cudaError_t prepare_step2d_f32() {
-  cudaError_t e = query_resident(k_stream_f32<false>, 0);
-  if (e == cudaSuccess) e = query_resident(k_stream_f32<true>, 1);
+  cudaError_t e = query_resident(k_stream_f32<false, false>, 0);
+  if (e == cudaSuccess) e = query_resident(k_stream_f32<true, false>, 1);
   if (e == cudaSuccess) e = query_resident(k_batch_f32, 2);
+  if (e == cudaSuccess) e = query_resident(k_stream_f32<false, true>, 3);
+  if (e == cudaSuccess) e = query_resident(k_stream_f32<true, true>, 4);
   return e;
 }
 

@@ -6,6 +6,8 @@ Tolerances: the plain FP64 step within 1e-12 of the reference (per field,
 max|a - b| / max|b| over the interior and the ghost edges); the FP32
 precision form within 1e-5 absolute of FP64 (fields are O(0.01 - 1)).
 """
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -190,6 +192,69 @@ def test_nine_point_mask_fused_matches_stages(pfa):
     assert max(field_err(a.read(), b.read())) <= FP64_TOL
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp32k"])
+def test_fp32_nine_point_mask_against_fp64(pfa, precision):
+    """The FP32 form with the reference's 9-point mask (src/mesh.cpp:198-213)
+    against the FP64 step with the same mask (itself equal to the
+    reference's stage-by-stage convolution, test above): the 256 x 256
+    workload after 1000 steps within the 5-point form's bound."""
+    from pfa_gb300 import ic
+    f = ic.config1()
+    p = _params(pfa)
+    m9 = pfa.nine_point_mask(p["dx"], p["dx"])
+    a = pfa.Grid2D(f, p, mask=m9, precision=precision)
+    b = pfa.Grid2D(f, p, mask=m9)
+    a.run(1000)
+    b.run(1000)
+    err = [float(np.max(np.abs(interior(x) - interior(y)))) for x, y in zip(a.read(), b.read())]
+    print(precision, "9-point max field error", err)
+    assert max(err) <= FP32_TOL_1000, err
+    # the 9-point mask acts: the 5-point FP64 run differs by far more
+    c = pfa.Grid2D(f, p)
+    c.run(1000)
+    d = max(float(np.max(np.abs(interior(x) - interior(y)))) for x, y in zip(c.read(), b.read()))
+    assert d > 100 * max(err), (d, err)
+    for g in (a, b, c):
+        g.close()
+
+
+@pytest.mark.parametrize("shape", [(3, 3), (5, 7), (31, 33), (40, 61)])
+def test_fp32_nine_point_mask_odd_sizes_and_spacing(pfa, shape):
+    """Odd sizes (strip and segment edges, the clamped corners) and unequal
+    spacing (dx != dy: the nine weights no longer sum to zero, which the
+    form carries as its own term), FP32 form against FP64."""
+    from pfa_gb300 import ic
+    ny, nx = shape
+    f = ic.grid2d(nx, ny, seed=nx * 7 + ny, stripe_width=max(1, nx // 3),
+                  n_particles=1 if min(nx, ny) > 12 else 0, radius=3.0)
+    for dy_over_dx in (1.0, 1.25):
+        p = _params(pfa)
+        p["dy"] = p["dx"] * dy_over_dx
+        m9 = pfa.nine_point_mask(p["dx"], p["dy"])
+        assert dy_over_dx == 1.0 or abs(m9.sum()) > 1e-3 * abs(m9[1, 1])
+        a = pfa.Grid2D(f, p, mask=m9, precision="fp32")
+        b = pfa.Grid2D(f, p, mask=m9)
+        a.run(100)
+        b.run(100)
+        err = [float(np.max(np.abs(interior(x) - interior(y)))) for x, y in zip(a.read(), b.read())]
+        assert max(err) <= 1e-7, (shape, dy_over_dx, err)
+        a.close()
+        b.close()
+
+
+def test_fp32_rejects_an_asymmetric_mask(pfa):
+    from pfa_gb300 import ic
+    f = ic.grid2d(20, 20, seed=1, stripe_width=5, n_particles=0)
+    p = _params(pfa)
+    m = pfa.nine_point_mask(p["dx"], p["dx"])
+    m[0, 0] *= 1.5
+    g = pfa.Grid2D(f, p, mask=m, precision="fp32")
+    assert g.L.pfa_run(g.ref, 1, ctypes.c_double(p["alpha"]), ctypes.c_double(p["dt"])) == 1
+    assert b"symmetric" in g.L.pfa_last_error_message()
+    g.L.pfa_clear_error()
+    g.close()
 
 
 def test_graph_run_equals_single_steps(pfa):
