@@ -157,12 +157,30 @@ def five_point_mask(dx, dy):
     return m
 
 
-def _setup(drv, fields, prm):
+def nine_point_mask(dx, dy):
+    """nine_point_Laplacian_stencil, src/mesh.cpp:198-213."""
+    m = np.zeros((3, 3))
+    m[0][0] = 1. / (6. * dx * dy)
+    m[0][1] = 4. / (6. * dy * dy)
+    m[0][2] = 1. / (6. * dx * dy)
+    m[1][0] = 4. / (6. * dx * dx)
+    m[1][1] = -10. * (dx * dx + dy * dy) / (6. * dx * dx * dy * dy)
+    m[1][2] = 4. / (6. * dx * dx)
+    m[2][0] = 1. / (6. * dx * dy)
+    m[2][1] = 4. / (6. * dy * dy)
+    m[2][2] = 1. / (6. * dx * dy)
+    return m
+
+
+def _setup(drv, fields, prm, mask=None):
     """init_cuda's constant uploads and the device arrays: [old, new] fields
-    and the six fictitious compositions (Cr / Nb of gamma, delta, laves)."""
+    and the six fictitious compositions (Cr / Nb of gamma, delta, laves).
+    mask: the 3 x 3 Laplacian mask (default: the 5-point mask of prm's
+    spacing, as src/main.cpp:237)."""
     ny, nx = fields[0].shape
     nb = nx * ny * 8
-    drv.set_constant(b"d_mask", five_point_mask(prm.dx, prm.dy))
+    drv.set_constant(b"d_mask", five_point_mask(prm.dx, prm.dy) if mask is None
+                     else np.ascontiguousarray(mask, dtype=np.float64))
     for name, v in ((b"d_DCr", prm.D_Cr), (b"d_DNb", prm.D_Nb), (b"d_Kapp", prm.kappa),
                     (b"d_Omeg", prm.omega), (b"d_Lmob", prm.Lmob)):
         drv.set_constant(name, list(v))
@@ -200,10 +218,11 @@ def _step(drv, state, fict, nx, ny, prm):
     state.reverse()
 
 
-def run_reference(drv, fields, prm, steps):
-    """Snapshots of the reference's update loop after each count in `steps`."""
+def run_reference(drv, fields, prm, steps, mask=None):
+    """Snapshots of the reference's update loop after each count in `steps`
+    (mask: the Laplacian mask, default 5-point)."""
     ny, nx = fields[0].shape
-    state, fict = _setup(drv, fields, prm)
+    state, fict = _setup(drv, fields, prm, mask)
     out = {}
     done = 0
     for target in steps:

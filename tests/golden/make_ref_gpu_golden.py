@@ -17,6 +17,16 @@ grid, and the 256 x 256 workload after 1000 steps), given the fictitious
 compositions and mobility coefficients of the oracle's variable-mobility
 restatement (the reference's own mobility kernels are commented out);
 
+in ref_gpu_nine.npz, the reference's step with its 9-point mask
+(nine_point_Laplacian_stencil, src/mesh.cpp:198-213) on a 260 x 260 grid
+with stripes and particles: snapshots after 1, 10, 100 and 500 steps at
+dx = dy, and after 100 steps at dy = 1.25 dx (the nine weights then do not
+sum to zero).  With that mask the Laplacian reads the ghost ring's corners,
+which the reference's boundary_kernel writes from threads that race unless
+each corner's writer and reader share a warp of its 13 x 13 blocks: they do
+when the interior side is a multiple of 13 (260), and the script checks
+that two runs agree bit for bit;
+
 and, in ref_gpu_nucleation.npz, the event counts of the reference's own
 nucleation kernel (src/discretization.cu:1079-1177, clock-seeded curand) in
 four independent calls on a uniform enriched 512 x 512 grid whose nuclei
@@ -26,7 +36,8 @@ cover one cell each.
                                                [--out tests/golden/ref_gpu_step2d.npz]
                                                [--nuc-out tests/golden/ref_gpu_nucleation.npz]
                                                [--varmob-out tests/golden/ref_gpu_varmob.npz]
-                                               [--only varmob]
+                                               [--nine-out tests/golden/ref_gpu_nine.npz]
+                                               [--only varmob|step|nine|nucleation]
 """
 import argparse
 import os
@@ -48,22 +59,40 @@ NUC_UNIT_A = 0.352e-9
 NUC_D = (2e-9, 2e-9, 1e-3)
 NUC_DT = 1e7
 NUC_CALLS = 4
+# 9-point case: interior side a multiple of the reference's 13-row tiles
+NINE_SIDE = 260
+NINE_STEPS = (1, 10, 100, 500)
+NINE_ANISO_STEPS = 100
 
 
 def main():
     import oracle as O
-    from ref_gpu import (CUBIN, Driver, run_reference, run_reference_chem_div,
-                         run_reference_nucleation)
+    from ref_gpu import CUBIN, Driver
     from pfa_gb300 import ic
     ap = argparse.ArgumentParser()
     ap.add_argument("--cubin", default=CUBIN)
     ap.add_argument("--out", default=os.path.join(HERE, "ref_gpu_step2d.npz"))
     ap.add_argument("--nuc-out", default=os.path.join(HERE, "ref_gpu_nucleation.npz"))
     ap.add_argument("--varmob-out", default=os.path.join(HERE, "ref_gpu_varmob.npz"))
-    ap.add_argument("--only", default="", help="varmob: only that set")
+    ap.add_argument("--nine-out", default=os.path.join(HERE, "ref_gpu_nine.npz"))
+    ap.add_argument("--only", default="", choices=["", "varmob", "step", "nine", "nucleation"],
+                    help="write only that set")
     args = ap.parse_args()
     drv = Driver(args.cubin)
-    # variable-mobility divergences of the reference's chemical_convolution kernels
+    want = lambda k: args.only in ("", k)
+    if want("varmob"):
+        varmob(drv, O, args)
+    if want("step"):
+        steps(drv, O, ic, args)
+    if want("nine"):
+        nine(drv, O, ic, args)
+    if want("nucleation"):
+        nucleation(drv, ic, args)
+
+
+def varmob(drv, O, args):
+    """Divergences of the reference's chemical_convolution kernels."""
+    from ref_gpu import run_reference_chem_div
     orc = O.Oracle()
     vm = {}
     states = [[np.load(os.path.join(HERE, "step2d.npz"))[f"ic_{n}"] for n in NAMES],
@@ -78,8 +107,11 @@ def main():
         vm[f"s{k}_div_cr"], vm[f"s{k}_div_nb"] = div
     np.savez_compressed(args.varmob_out, dxy=np.array(dxy), **vm)
     print("reference GPU variable-mobility divergences written to", args.varmob_out)
-    if args.only == "varmob":
-        return
+
+
+def steps(drv, O, ic, args):
+    """The reference's step with the 5-point mask."""
+    from ref_gpu import run_reference
     res = {}
     g = np.load(os.path.join(HERE, "step2d.npz"))
     f = [g[f"ic_{n}"] for n in NAMES]
@@ -98,6 +130,33 @@ def main():
             res[f"config1_s{k}_{n}"] = snap[j]
     np.savez_compressed(args.out, **res)
     print("reference GPU steps written to", args.out)
+
+
+def nine(drv, O, ic, args):
+    """The reference's step with its 9-point mask, two spacings."""
+    from ref_gpu import nine_point_mask, run_reference
+    f = ic.grid2d(NINE_SIDE, NINE_SIDE, seed=13, stripes=[60, 190], stripe_width=24,
+                  n_particles=6, radius=6.0)
+    res = {f"ic_{n}": f[j] for j, n in enumerate(NAMES)}
+    prm = O.model_params()
+    cases = (("iso", prm.dx, prm.dx, NINE_STEPS), ("aniso", prm.dx, 1.25 * prm.dx, (NINE_ANISO_STEPS,)))
+    for tag, dx, dy, counts in cases:
+        mask = nine_point_mask(dx, dy)
+        runs = [run_reference(drv, f, prm, counts, mask=mask) for _ in range(2)]
+        for k in counts:
+            for j, n in enumerate(NAMES):
+                a, b = runs[0][k][j], runs[1][k][j]
+                if not np.array_equal(a, b):
+                    raise SystemExit(f"the reference's 9-point step is not reproducible ({tag}, {k}, {n})")
+                res[f"{tag}_s{k}_{n}"] = a
+        res[f"{tag}_dxy"] = np.array([dx, dy])
+    np.savez_compressed(args.nine_out, dt=np.array([prm.dt]), **res)
+    print("reference GPU 9-point steps written to", args.nine_out)
+
+
+def nucleation(drv, ic, args):
+    """Event counts of the reference's nucleation kernel."""
+    from ref_gpu import run_reference_nucleation
     # nucleation: event counts of the reference's own kernel on a uniform
     # enriched grid, single-cell nuclei (critical radius and scan radius
     # below one cell), independent calls

@@ -194,6 +194,41 @@ def test_nine_point_mask_fused_matches_stages(pfa):
     b.close()
 
 
+def test_nine_point_mask_matches_reference_cuda_kernels(pfa):
+    """The 9-point mask against the reference's own CUDA step run with it on
+    a GB300 (tests/golden/ref_gpu_nine.npz, 260 x 260 interior, the side on
+    which the reference's corner fill is deterministic): the fused FP64 step
+    and the stage calls after 1, 10, 100, 500 steps at dx = dy and 100 steps
+    at dy = 1.25 dx, within 1e-12; the FP32 form within its 1000-step bound."""
+    r = golden("ref_gpu_nine.npz")
+    f = fields_of(r, "ic")
+    p = _params(pfa)
+    assert p["dt"] == r["dt"][0]
+    for tag in ("iso", "aniso"):
+        dx, dy = r[f"{tag}_dxy"]
+        m9 = pfa.nine_point_mask(dx, dy)
+        counts = sorted(int(k.split("_s")[1].split("_")[0]) for k in r.files
+                        if k.startswith(f"{tag}_s") and k.endswith("_cr"))
+        grids = [pfa.Grid2D(f, p, mask=m9), pfa.Grid2D(f, p, mask=m9, mode="compat"),
+                 pfa.Grid2D(f, p, mask=m9, precision="fp32")]
+        done = 0
+        for k in counts:
+            grids[0].run(k - done)
+            for _ in range(k - done):
+                grids[1].step_stages()
+            grids[2].run(k - done)
+            done = k
+            want = fields_of(r, f"{tag}_s{k}")
+            for mode, g in zip(("fused", "compat"), grids[:2]):
+                err = field_err(g.read(), want)
+                assert max(err) <= FP64_TOL, (tag, k, mode, err)
+            err32 = [float(np.max(np.abs(interior(a) - interior(b))))
+                     for a, b in zip(grids[2].read(), want)]
+            assert max(err32) <= FP32_TOL_1000, (tag, k, err32)
+        for g in grids:
+            g.close()
+
+
 @pytest.mark.parametrize("precision", ["fp32", "fp32k"])
 def test_fp32_nine_point_mask_against_fp64(pfa, precision):
     """The FP32 form with the reference's 9-point mask (src/mesh.cpp:198-213)
