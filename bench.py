@@ -442,6 +442,12 @@ def grid4096(c, quick_error=True):
                "cores": os.cpu_count(), "kind": "port", "cpu": cpu_model(),
                "sample": f"{sample_steps} FP64 time steps of the {N_SIDE}^2 grid, "
                          f"OpenMP, reference host flags"}
+        # the 256^2 workload at its full 1000 steps
+        f1 = ic.config1()
+        t1 = cpu_baseline(f1, pl.model_params(), 1000)
+        cpu["c1"] = {"value": (f1[0].shape[0] - 2) * (f1[0].shape[1] - 2) * 1000 / t1,
+                     "unit": "cell-updates/s", "seconds": t1,
+                     "sample": "the 256^2 grid (one stripe, four particles), 1000 FP64 steps"}
     ref_gpu = reference_gpu_baseline(fields)
     if "value" in ref_gpu:
         ref_gpu["speedup_fp32_over_reference_gpu"] = value / ws / ref_gpu["value"]
@@ -807,6 +813,25 @@ def serve(c, count=SERVE_COUNT, recipes=True, compare_host_fields=False):
                           "request, service = set-up + steps x step time, queueing computed "
                           "(running the loop would take hours)",
                    "step_ms": {f"{d}d{s}": 1e3 * v[1] for (d, s), v in per_size.items()}}
+    # the model against whole requests run for real: the first request of
+    # each of the two smallest sizes in the trace, FP64, all its steps,
+    # from upload to read-back
+    checks = []
+    for key in sorted(per_size, key=lambda k: k[1] ** k[0])[:2]:
+        t_ = next(t for t in trace if (t["dim"], t["side"]) == key)
+        f = ic.serve_fields(t_)
+        t0 = time.perf_counter()
+        g = (pl.Grid2D(f, p2, precision="fp64") if t_["dim"] == 2
+             else pl.Grid3D(f, p3, precision="fp64"))
+        g.run(t_["steps"])
+        g.read()
+        g.close()
+        measured = time.perf_counter() - t0
+        modelled = per_size[key][0] + per_size[key][1] * t_["steps"]
+        checks.append({"request": f"{key[0]}d{key[1]}, {t_['steps']} steps",
+                       "measured_s": measured, "modelled_s": modelled,
+                       "ratio": measured / modelled})
+    out["fp64"]["check"] = checks
     return out
 
 
