@@ -73,6 +73,7 @@ struct State {
   double mask9[9] = {};
   bool five_point = true;
   bool symmetric = true;  // corners, left / right and upper / lower weights equal (FP32 form)
+  bool zero_sum = true;   // the nine weights sum to zero (up to rounding)
   ModelConst m{};
   FastCoef fk{};
   cudaStream_t st = nullptr;
@@ -217,15 +218,14 @@ static Step2DArgs step_args(State* s, double alpha, double dt) {
   a.alpha2 = float(2.0 * alpha);
   a.idx2f[0] = float(s->m.idx2[0]);
   a.idx2f[1] = float(s->m.idx2[1]);
-  if (a.nine) {
-    double sum = 0.0;
-    for (double w : s->mask9) sum += w;
-    a.lap9[0] = float(s->mask9[3]);
-    a.lap9[1] = float(s->mask9[1]);
-    a.lap9[2] = float(s->mask9[0]);
-    a.lap9[3] = float(sum);
-    for (int k = 0; k < 2; k++) a.lap9xe[k] = float(sum * kXe[0][k]);
-  }
+  // the FP32 form's general (9-point) Laplacian weights
+  double sum = 0.0;
+  for (double w : s->mask9) sum += w;
+  a.lap9[0] = float(s->mask9[3]);
+  a.lap9[1] = float(s->mask9[1]);
+  a.lap9[2] = float(s->mask9[0]);
+  a.lap9[3] = float(sum);
+  for (int k = 0; k < 2; k++) a.lap9xe[k] = float(sum * kXe[0][k]);
   return a;
 }
 
@@ -256,6 +256,9 @@ static int fused_step(CudaData* dev, State* s, double alpha, double dt) {
   a.out[1] = s->recB[n];
   a.pitch = s->pitch32;
   a.full_comp = s->precision == PFA_FP32_KPHI;
+  // the 5-point FP32 kernel takes the centre weight as -2 (left + upper);
+  // a mask whose weights do not sum to zero goes through the general form
+  a.nine = !s->five_point || !s->zero_sum;
   CK(launch_step2d_f32(a, s->st));
   s->cur = n;
   return 0;
@@ -563,6 +566,11 @@ static int init_core(CudaData* dev, int nx, int ny, int nm, const double* mask,
   s->five_point = mask[0] == 0.0 && mask[2] == 0.0 && mask[6] == 0.0 && mask[8] == 0.0;
   s->symmetric = mask[0] == mask[2] && mask[0] == mask[6] && mask[0] == mask[8] &&
                  mask[1] == mask[7] && mask[3] == mask[5];
+  {
+    double sum = 0.0;
+    for (int k = 0; k < 9; k++) sum += mask[k];
+    s->zero_sum = std::fabs(sum) <= 1e-12 * std::fabs(mask[4]);
+  }
   for (int i = 0; i < 2; i++) {
     s->m.D[0][i] = D_Cr[i];
     s->m.D[1][i] = D_Nb[i];

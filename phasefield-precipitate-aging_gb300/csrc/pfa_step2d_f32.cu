@@ -10,10 +10,11 @@
 // economy:
 //  * each warp owns a strip of 30 output columns (lanes 1..30; lanes 0 and
 //    31 carry the neighbour columns) and streams down a segment of rows; the
-//    three rows a 5-point Laplacian needs live in registers, rotated by a
-//    3x-unrolled loop, so each cell's gamma solve runs once and nothing goes
-//    through shared memory;
-//  * left / right neighbours come from __shfl_up / __shfl_down;
+//    three rows a 5- or 9-point Laplacian needs live in registers, rotated by
+//    a 3x-unrolled loop, so each cell's gamma solve runs once and nothing
+//    goes through shared memory;
+//  * left / right neighbours come from __shfl_up / __shfl_down (with the
+//    9-point mask each row carries its x-difference sums, formed once);
 //  * the state is stored as two records per cell -- A = {x_Cr, x_Nb, phi_del,
 //    phi_lav} (16 bytes) and B = the four compensations, packed into 16-bit
 //    counts (8 bytes, PACK) or as FP32 (16 bytes) -- so a row costs one

@@ -279,6 +279,30 @@ def test_fp32_nine_point_mask_odd_sizes_and_spacing(pfa, shape):
         b.close()
 
 
+def test_fp32_mask_whose_weights_do_not_sum_to_zero(pfa):
+    """A 5-point mask with its centre weight off by 0.1 %: the FP32 form
+    carries the weights' sum as its own term (the general-mask kernel), so
+    it follows the FP64 step, which convolves the mask as given."""
+    from pfa_gb300 import ic
+    f = ic.grid2d(45, 37, seed=12, stripe_width=9, n_particles=2, radius=4.0)
+    p = _params(pfa)
+    m = pfa.five_point_mask(p["dx"], p["dx"])
+    m[1, 1] *= 1.001
+    a = pfa.Grid2D(f, p, mask=m, precision="fp32")
+    b = pfa.Grid2D(f, p, mask=m)
+    c = pfa.Grid2D(f, p)
+    for g in (a, b, c):
+        g.run(50)
+    ra, rb, rc = a.read(), b.read(), c.read()
+    err = [float(np.max(np.abs(interior(x) - interior(y)))) for x, y in zip(ra, rb)]
+    assert max(err) <= 1e-7, err
+    # the altered centre acts: the reference mask's run differs by far more
+    d = max(float(np.max(np.abs(interior(x) - interior(y)))) for x, y in zip(rb, rc))
+    assert d > 100 * max(err), (d, err)
+    for g in (a, b, c):
+        g.close()
+
+
 def test_fp32_rejects_an_asymmetric_mask(pfa):
     from pfa_gb300 import ic
     f = ic.grid2d(20, 20, seed=1, stripe_width=5, n_particles=0)
