@@ -963,6 +963,8 @@ int pfa_set_precision(struct CudaData* dev, int precision) {
     return fail(PFA_EINVAL, "compat mode is FP64 only");
   if (precision != PFA_FP64 && s->varmob)
     return fail(PFA_EINVAL, "the variable mobility is an FP64 form");
+  if (precision != PFA_FP64 && !fp32_records_fit(s->Nx, s->Ny))
+    return fail(PFA_EINVAL, "grid above 2^31 records (the FP32 form's 32-bit index)");
   if (precision == s->precision) return 0;
   if (s->f32_live) {
     if (int r = f32_export(dev, s)) return r;

@@ -395,6 +395,8 @@ int pfa_batch_add(void* handle, int nx, int ny, const double* conc_Cr, const dou
   if (!conc_Cr || !conc_Nb || !phi_del || !phi_lav || !slot)
     return fail(PFA_EINVAL, "pfa_batch_add: null argument");
   if (nx < 3 || ny < 3) return fail(PFA_EINVAL, "pfa_batch_add: grid smaller than 3x3");
+  if (!fp32_records_fit(nx - 2, ny - 2))
+    return fail(PFA_EINVAL, "pfa_batch_add: grid above 2^31 records (the FP32 form's 32-bit index)");
   int id = -1;
   if (int r = place(b, nx, ny, &id)) return r;
   const size_t cells = size_t(nx) * ny;
@@ -416,6 +418,8 @@ int pfa_batch_add_ic(void* handle, const pfa_ic_recipe* r, int* slot) {
   if (r->nz > 1) return fail(PFA_EINVAL, "pfa_batch_add_ic: the batch holds 2D grids (nz <= 1)");
   const int nx = r->nx + 2, ny = r->ny + 2;
   if (nx < 3 || ny < 3) return fail(PFA_EINVAL, "pfa_batch_add_ic: grid smaller than 3x3");
+  if (!fp32_records_fit(nx - 2, ny - 2))
+    return fail(PFA_EINVAL, "pfa_batch_add_ic: grid above 2^31 records (the FP32 form's 32-bit index)");
   int id = -1;
   if (int e = place(b, nx, ny, &id)) return e;
   if (int e = ensure_stage(b, size_t(nx) * ny)) return e;

@@ -314,6 +314,8 @@ static int create3d(void** handle, int nx, int ny, int nz, const double* params,
   if (nx < 3 || ny < 3 || nz < 3) return err(PFA_EINVAL, "pfa3d_create: grid smaller than 3^3");
   if (precision != PFA_FP64 && precision != PFA_FP32)
     return err(PFA_EINVAL, "pfa3d_create: 3D grids run in PFA_FP64 or PFA_FP32");
+  if (precision == PFA_FP32 && !fp32_records_fit(nx - 2, ny - 2))
+    return err(PFA_EINVAL, "pfa3d_create: plane above 2^31 records (the FP32 form's 32-bit index)");
   Grid3D* g = new Grid3D();
   *handle = g;
   g->Nx = nx - 2;

@@ -51,6 +51,12 @@ struct FastCoef {
 
 void model_fast_coef(FastCoef* out);
 
+// The FP32 form's kernels index a grid's (2D) or a plane's (3D) records with
+// 32-bit integers: rows of ceil(Nx / 32) * 32 records, Ny rows, below 2^31.
+inline bool fp32_records_fit(int Nx, int Ny) {
+  return (long long)((Nx + 31) / 32) * 32 * Ny < (1LL << 31);
+}
+
 // Host model helpers (pfa_model.cpp)
 double model_D(int row, int col, double xcr, double xnb);
 double model_kks_diffusivity(const double Dcr[2], const double Dnb[2]);
