@@ -45,7 +45,10 @@ enum { PFA_MODE_FUSED = 0, PFA_MODE_COMPAT = 1 };
  * PFA_FP32_KPHI: the same with FP32 compensations (64 bytes per cell).
  * Both take the 5- or the 9-point mask of src/mesh.cpp:187-213 (any 3x3
  * mask with equal corners, equal left / right and equal upper / lower
- * weights; a step with another mask fails with PFA_EINVAL). */
+ * weights; a step with another mask fails with PFA_EINVAL).  Both index a
+ * grid's records (rows of ceil((nx - 2) / 32) * 32, ny - 2 rows; for 3D
+ * grids a plane's) with 32-bit integers: from 2^31 records on, switching to
+ * them, pfa_batch_add and pfa3d_create fail with PFA_EINVAL. */
 enum { PFA_FP64 = 0, PFA_FP32 = 1, PFA_FP32_KPHI = 2 };
 enum { PFA_NUC_REFERENCE_GEOMETRY = 0, PFA_NUC_FIXED_GEOMETRY = 1 };
 /* Cahn-Hilliard: the reference's constant diffusivity matrix (its loop's
