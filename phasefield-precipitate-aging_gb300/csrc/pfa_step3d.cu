@@ -203,8 +203,9 @@ __global__ void __launch_bounds__(32 * kW) k_stream3d_f64(Step3DArgs a) {
 // records and one of B records, from two columns left of the tile (so that
 // the box of 8-byte B records starts on a 16-byte boundary), both
 // completing on the plane slot's mbarrier; every thread reads its own
-// (clamped) record from the slot, at the same index in both boxes.  Records outside the grid arrive as zeros
-// and are never read (threads past an edge read the clamped record).  Each
+// (clamped) record from the slot, at the same index in both boxes.  Records
+// outside the grid arrive as zeros and are never read (threads past an edge
+// read the clamped record).  Each
 // iteration solves planes z+1 and z+2, publishes them and passes one barrier
 // for both updates; a plane's record is read from the ring once, for its
 // solve, and kept in registers until its update.
