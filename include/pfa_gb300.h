@@ -209,9 +209,15 @@ int pfa3d_test_skip_plane(void* handle, int plane);
  * doubles of pfa3d_create) and dxy = dx, dy.  Grids join (pfa_batch_add:
  * fields in the reference layout, ny x nx doubles with the ghost ring;
  * PFA_ENOMEM, not printed, when the arena has no room) and leave
- * (pfa_batch_remove) between runs; slot ids are reused.  pfa_batch_add reads
- * page-locked host arrays asynchronously: keep them unchanged until the next
- * pfa_batch_sync (or pfa_batch_read, which waits).  A member advances
+ * (pfa_batch_remove) between runs; slot ids are reused.  pfa_batch_add,
+ * pfa_batch_remove, pfa_batch_run and pfa_batch_read_async do not wait for
+ * the GPU: the fields pass through a staging ring in device memory on copy
+ * streams of their own, so one batch's transfers overlap another batch's
+ * steps.  pfa_batch_add reads page-locked host arrays asynchronously: keep
+ * them unchanged until the next pfa_batch_sync (or pfa_batch_read, which
+ * waits); pfa_batch_read_async writes the slot's fields at the state of the
+ * runs enqueued before it into page-locked host arrays (null: skipped), valid
+ * after the next pfa_batch_sync.  A member advances
  * bit-for-bit as it would alone.  pfa_batch_footprint gives the arena bytes a
  * grid takes.  pfa_batch_tune times the launch shapes (rows per segment,
  * persistent or one warp per unit) on the current members without advancing
@@ -223,6 +229,8 @@ int pfa_batch_add(void* handle, int nx, int ny, const double* conc_Cr, const dou
 int pfa_batch_remove(void* handle, int slot);
 int pfa_batch_read(void* handle, int slot, double* conc_Cr, double* conc_Nb, double* phi_del,
                    double* phi_lav);
+int pfa_batch_read_async(void* handle, int slot, double* conc_Cr, double* conc_Nb,
+                         double* phi_del, double* phi_lav);
 int pfa_batch_run(void* handle, int nsteps);
 int pfa_batch_run_timed(void* handle, int nsteps, float* ms);
 int pfa_batch_sync(void* handle);

@@ -14,9 +14,21 @@
 // Every cell's update reads only its own grid's records, and a unit's result
 // does not depend on how rows are split into segments, so a grid advances
 // bit-for-bit the same alone, in any batch, and as a single-grid handle.
+//
+// Host transfers do not wait for the GPU.  The FP64 fields of adds and reads
+// pass through a staging ring in device memory, copied on two copy streams
+// (host to device, device to host); the conversions to and from the FP32
+// records run on a high-priority stream of their own, ordered against the
+// step stream with events.  So one batch's copies run while another batch's
+// persistent step kernel holds the SMs, and its conversions are dispatched
+// ahead of the next step launch.  A stream that writes a ring region first
+// waits for the event of the region's last reader (a stream wait, not a host
+// wait); an import into an arena block waits for the steps enqueued before
+// the latest removal, which may still read a freed block.
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <deque>
 #include <map>
 #include <mutex>
 #include <vector>
@@ -35,6 +47,12 @@ struct Slot {
   bool live = false;
   int Nx = 0, Ny = 0, pitch = 0;
   size_t off = 0, bytes = 0;  // block in the arena
+};
+
+// a region of the staging ring and the event after its last use
+struct RingEntry {
+  size_t begin, end;
+  cudaEvent_t done;
 };
 
 struct BGraph {
@@ -63,8 +81,14 @@ struct Batch {
   int ctas = 0;          // CTAs of a persistent launch (0 = all resident)
   unsigned long long version = 1;  // bumps when the device tables move
   std::vector<BGraph> graphs;
-  double* stage[4] = {};
-  size_t stage_cells = 0;
+  cudaStream_t up = nullptr, down = nullptr;  // host -> device / device -> host copies
+  cudaStream_t cv = nullptr;                  // conversions (high priority)
+  cudaEvent_t removed = nullptr;              // the step stream at the latest removal
+  bool fence = false;                         // a removal since the last import
+  char* ring = nullptr;                       // FP64 staging of adds and reads
+  size_t ring_cap = 0, ring_head = 0;
+  std::deque<RingEntry> ring_q;               // regions in use, in allocation order
+  std::vector<cudaEvent_t> ev_pool;
   double* sum_partial = nullptr;
   double* sum_out = nullptr;
 };
@@ -182,8 +206,7 @@ int upload_tables(Batch* b, int rows) {
     CKB(cudaMalloc(reinterpret_cast<void**>(&b->d_unit), sizeof(BatchUnit) * b->unit_cap));
     b->version++;
   }
-  // the copies are stream-ordered after every launch already enqueued, and
-  // must finish before the host vectors go out of scope
+  // the copies are stream-ordered after every launch already enqueued
   if (!grids.empty())
     CKB(cudaMemcpyAsync(b->d_grid, grids.data(), sizeof(BatchGrid) * grids.size(),
                         cudaMemcpyHostToDevice, b->st));
@@ -193,7 +216,9 @@ int upload_tables(Batch* b, int rows) {
   b->units = int(units.size());
   const int counters[3] = {0, 0, b->units};
   CKB(cudaMemcpyAsync(b->d_counter, counters, sizeof(counters), cudaMemcpyHostToDevice, b->st));
-  CKB(cudaStreamSynchronize(b->st));
+  // no host wait: copies from pageable host memory are staged before
+  // cudaMemcpyAsync returns, and the launches that read the tables follow
+  // them on the stream
   return 0;
 }
 
@@ -268,23 +293,79 @@ int run(Batch* b, int nsteps) {
   return 0;
 }
 
-int ensure_stage(Batch* b, size_t cells) {
-  if (cells <= b->stage_cells) return 0;
-  CKB(cudaStreamSynchronize(b->st));
-  for (int k = 0; k < 4; k++) {
-    cudaFree(b->stage[k]);
-    b->stage[k] = nullptr;
+cudaError_t take_event(Batch* b, cudaEvent_t* ev) {
+  if (!b->ev_pool.empty()) {
+    *ev = b->ev_pool.back();
+    b->ev_pool.pop_back();
+    return cudaSuccess;
   }
-  for (int k = 0; k < 4; k++)
-    CKB(cudaMalloc(reinterpret_cast<void**>(&b->stage[k]), cells * sizeof(double)));
-  b->stage_cells = cells;
+  return cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+}
+
+// `waiter` waits (on the device) for everything enqueued so far on `from`
+int order_after(Batch* b, cudaStream_t waiter, cudaStream_t from) {
+  cudaEvent_t ev;
+  CKB(take_event(b, &ev));
+  CKB(cudaEventRecord(ev, from));
+  CKB(cudaStreamWaitEvent(waiter, ev, 0));
+  b->ev_pool.push_back(ev);  // the wait holds the state it was enqueued with
   return 0;
 }
 
-ConvArgs conv(Batch* b, const Slot& s) {
+// n bytes of the staging ring for a region that `writer` fills first: the
+// writer waits for the last readers of the bytes it overwrites
+int ring_take(Batch* b, size_t n, cudaStream_t writer, size_t* off) {
+  n = (n + kAlign - 1) / kAlign * kAlign;
+  while (!b->ring_q.empty() && cudaEventQuery(b->ring_q.front().done) == cudaSuccess) {
+    b->ev_pool.push_back(b->ring_q.front().done);
+    b->ring_q.pop_front();
+  }
+  (void)cudaGetLastError();  // cudaErrorNotReady from the queries is not an error
+  if (n > b->ring_cap) {     // grow: rare; drain every stream first
+    for (cudaStream_t x : {b->up, b->cv, b->st, b->down}) CKB(cudaStreamSynchronize(x));
+    for (auto& e : b->ring_q) b->ev_pool.push_back(e.done);
+    b->ring_q.clear();
+    cudaFree(b->ring);
+    b->ring = nullptr;
+    b->ring_cap = std::max(n, 2 * b->ring_cap);
+    CKB(cudaMalloc(reinterpret_cast<void**>(&b->ring), b->ring_cap));
+    b->ring_head = 0;
+  }
+  size_t at = b->ring_head;
+  if (at + n > b->ring_cap) at = 0;
+  for (auto it = b->ring_q.begin(); it != b->ring_q.end();) {
+    if (it->begin < at + n && at < it->end) {
+      CKB(cudaStreamWaitEvent(writer, it->done, 0));
+      b->ev_pool.push_back(it->done);
+      it = b->ring_q.erase(it);
+    } else {
+      ++it;
+    }
+  }
+  b->ring_head = at + n;
+  *off = at;
+  return 0;
+}
+
+// the region [off, off + n) is free once `last` has done what is enqueued on it
+int ring_release(Batch* b, size_t off, size_t n, cudaStream_t last) {
+  n = (n + kAlign - 1) / kAlign * kAlign;
+  cudaEvent_t ev;
+  CKB(take_event(b, &ev));
+  CKB(cudaEventRecord(ev, last));
+  b->ring_q.push_back({off, off + n, ev});
+  return 0;
+}
+
+// the four FP64 fields of an nx x ny grid in the ring region at off
+void ring_fields(const Batch* b, size_t off, size_t cells, double* f[4]) {
+  for (int k = 0; k < 4; k++) f[k] = reinterpret_cast<double*>(b->ring + off) + k * cells;
+}
+
+ConvArgs conv(Batch* b, const Slot& s, double* const f64[4]) {
   const BatchGrid g = grid_entry(b, s);
   ConvArgs c{};
-  for (int k = 0; k < 4; k++) c.f64[k] = b->stage[k];
+  for (int k = 0; k < 4; k++) c.f64[k] = f64[k];
   c.A = reinterpret_cast<float*>(g.A[b->cur]);
   c.B = g.B[b->cur];
   c.pack = 1;
@@ -293,6 +374,32 @@ ConvArgs conv(Batch* b, const Slot& s) {
   c.pitch64 = s.Nx + 2;
   c.pitch32 = s.pitch;
   return c;
+}
+
+// the conversion stream waits for the steps enqueued before the latest
+// removal (an arena block freed there may be handed to the grid imported next)
+int await_removals(Batch* b) {
+  if (!b->fence) return 0;
+  CKB(cudaStreamWaitEvent(b->cv, b->removed, 0));
+  b->fence = false;
+  return 0;
+}
+
+// the export of a live slot into the ring and its copies to host arrays
+// (null: skipped) on the device-to-host stream; no host wait
+int read_async(Batch* b, const Slot& s, double* const dst[4]) {
+  const size_t cells = size_t(s.Nx + 2) * (s.Ny + 2), n = 4 * cells * sizeof(double);
+  size_t off = 0;
+  if (int r = ring_take(b, n, b->cv, &off)) return r;
+  double* f[4];
+  ring_fields(b, off, cells, f);
+  if (int r = order_after(b, b->cv, b->st)) return r;  // after the runs enqueued so far
+  CKB(launch_export_f32(conv(b, s, f), b->cv));
+  if (int r = order_after(b, b->down, b->cv)) return r;
+  for (int k = 0; k < 4; k++)
+    if (dst[k])
+      CKB(cudaMemcpyAsync(dst[k], f[k], cells * sizeof(double), cudaMemcpyDeviceToHost, b->down));
+  return ring_release(b, off, n, b->down);
 }
 
 Batch* get(void* h) { return static_cast<Batch*>(h); }
@@ -378,6 +485,16 @@ int pfa_batch_create(void** handle, const double* params, const double* dxy, siz
   a.idx2f[1] = float(m.idx2[1]);
   b->cap = arena_bytes / kAlign * kAlign;
   CKB(cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking));
+  CKB(cudaStreamCreateWithFlags(&b->up, cudaStreamNonBlocking));
+  CKB(cudaStreamCreateWithFlags(&b->down, cudaStreamNonBlocking));
+  int lo = 0, hi = 0;
+  CKB(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+  CKB(cudaStreamCreateWithPriority(&b->cv, cudaStreamNonBlocking, hi));
+  CKB(cudaEventCreateWithFlags(&b->removed, cudaEventDisableTiming));
+  // staging ring: the arena's size within [16 MiB, 8 GiB]; it grows for a
+  // larger single grid
+  b->ring_cap = std::min<size_t>(std::max<size_t>(b->cap, size_t(16) << 20), size_t(8) << 30);
+  CKB(cudaMalloc(reinterpret_cast<void**>(&b->ring), b->ring_cap));
   CKB(cudaMalloc(reinterpret_cast<void**>(&b->arena), b->cap));
   b->free_[0] = b->cap;
   CKB(cudaMalloc(reinterpret_cast<void**>(&b->d_counter), 3 * sizeof(int)));
@@ -399,12 +516,19 @@ int pfa_batch_add(void* handle, int nx, int ny, const double* conc_Cr, const dou
     return fail(PFA_EINVAL, "pfa_batch_add: grid above 2^31 records (the FP32 form's 32-bit index)");
   int id = -1;
   if (int r = place(b, nx, ny, &id)) return r;
-  const size_t cells = size_t(nx) * ny;
-  if (int r = ensure_stage(b, cells)) return r;
+  const size_t cells = size_t(nx) * ny, n = 4 * cells * sizeof(double);
+  size_t off = 0;
+  if (int r = ring_take(b, n, b->up, &off)) return r;
+  double* f[4];
+  ring_fields(b, off, cells, f);
   const double* src[4] = {conc_Cr, conc_Nb, phi_del, phi_lav};
   for (int k = 0; k < 4; k++)
-    CKB(cudaMemcpyAsync(b->stage[k], src[k], cells * sizeof(double), cudaMemcpyHostToDevice, b->st));
-  CKB(launch_import_f32(conv(b, b->slots[id]), b->st));
+    CKB(cudaMemcpyAsync(f[k], src[k], cells * sizeof(double), cudaMemcpyHostToDevice, b->up));
+  if (int r = order_after(b, b->cv, b->up)) return r;
+  if (int r = await_removals(b)) return r;
+  CKB(launch_import_f32(conv(b, b->slots[id], f), b->cv));
+  if (int r = order_after(b, b->st, b->cv)) return r;  // the steps read the block
+  if (int r = ring_release(b, off, n, b->cv)) return r;
   b->dirty = true;
   *slot = id;
   return 0;
@@ -422,9 +546,16 @@ int pfa_batch_add_ic(void* handle, const pfa_ic_recipe* r, int* slot) {
     return fail(PFA_EINVAL, "pfa_batch_add_ic: grid above 2^31 records (the FP32 form's 32-bit index)");
   int id = -1;
   if (int e = place(b, nx, ny, &id)) return e;
-  if (int e = ensure_stage(b, size_t(nx) * ny)) return e;
-  CKB(launch_ic_fill(*r, b->stage, b->st));
-  CKB(launch_import_f32(conv(b, b->slots[id]), b->st));
+  const size_t cells = size_t(nx) * ny, n = 4 * cells * sizeof(double);
+  size_t off = 0;
+  if (int e = ring_take(b, n, b->cv, &off)) return e;
+  double* f[4];
+  ring_fields(b, off, cells, f);
+  if (int e = await_removals(b)) return e;
+  CKB(launch_ic_fill(*r, f, b->cv));
+  CKB(launch_import_f32(conv(b, b->slots[id], f), b->cv));
+  if (int e = order_after(b, b->st, b->cv)) return e;  // the steps read the block
+  if (int e = ring_release(b, off, n, b->cv)) return e;
   b->dirty = true;
   *slot = id;
   return 0;
@@ -434,8 +565,10 @@ int pfa_batch_remove(void* handle, int slot) {
   Batch* b = get(handle);
   const Slot* s = live_slot(b, slot);
   if (!s) return fail(PFA_EINVAL, "pfa_batch_remove: no such grid");
-  // launches already enqueued may still read the block: drain them first
-  CKB(cudaStreamSynchronize(b->st));
+  // launches already enqueued may still read the block: the next import
+  // (which may reuse it) waits for them
+  CKB(cudaEventRecord(b->removed, b->st));
+  b->fence = true;
   arena_free(b, s->off, s->bytes);
   b->slots[slot].live = false;
   b->dirty = true;
@@ -447,15 +580,19 @@ int pfa_batch_read(void* handle, int slot, double* conc_Cr, double* conc_Nb, dou
   Batch* b = get(handle);
   const Slot* s = live_slot(b, slot);
   if (!s) return fail(PFA_EINVAL, "pfa_batch_read: no such grid");
-  const size_t cells = size_t(s->Nx + 2) * (s->Ny + 2);
-  if (int r = ensure_stage(b, cells)) return r;
-  CKB(launch_export_f32(conv(b, *s), b->st));
-  double* dst[4] = {conc_Cr, conc_Nb, phi_del, phi_lav};
-  for (int k = 0; k < 4; k++)
-    if (dst[k])
-      CKB(cudaMemcpyAsync(dst[k], b->stage[k], cells * sizeof(double), cudaMemcpyDeviceToHost, b->st));
-  CKB(cudaStreamSynchronize(b->st));
+  double* const dst[4] = {conc_Cr, conc_Nb, phi_del, phi_lav};
+  if (int r = read_async(b, *s, dst)) return r;
+  CKB(cudaStreamSynchronize(b->down));
   return 0;
+}
+
+int pfa_batch_read_async(void* handle, int slot, double* conc_Cr, double* conc_Nb,
+                         double* phi_del, double* phi_lav) {
+  Batch* b = get(handle);
+  const Slot* s = live_slot(b, slot);
+  if (!s) return fail(PFA_EINVAL, "pfa_batch_read_async: no such grid");
+  double* const dst[4] = {conc_Cr, conc_Nb, phi_del, phi_lav};
+  return read_async(b, *s, dst);
 }
 
 int pfa_batch_run(void* handle, int nsteps) {
@@ -487,7 +624,7 @@ int pfa_batch_run_timed(void* handle, int nsteps, float* ms) {
 int pfa_batch_sync(void* handle) {
   Batch* b = get(handle);
   if (!b) return fail(PFA_ESTATE, "pfa_batch_sync: null handle");
-  CKB(cudaStreamSynchronize(b->st));
+  for (cudaStream_t x : {b->up, b->cv, b->st, b->down}) CKB(cudaStreamSynchronize(x));
   return 0;
 }
 
@@ -600,16 +737,21 @@ void* pfa_batch_stream(void* handle) {
 int pfa_batch_destroy(void* handle) {
   Batch* b = get(handle);
   if (!b) return 0;
-  if (b->st) cudaStreamSynchronize(b->st);
+  for (cudaStream_t x : {b->up, b->cv, b->st, b->down})
+    if (x) cudaStreamSynchronize(x);
+  if (b->removed) cudaEventDestroy(b->removed);
   for (auto& g : b->graphs) cudaGraphExecDestroy(g.exec);
+  for (auto& e : b->ring_q) cudaEventDestroy(e.done);
+  for (cudaEvent_t e : b->ev_pool) cudaEventDestroy(e);
+  cudaFree(b->ring);
   cudaFree(b->arena);
   cudaFree(b->d_grid);
   cudaFree(b->d_unit);
   cudaFree(b->d_counter);
-  for (int k = 0; k < 4; k++) cudaFree(b->stage[k]);
   cudaFree(b->sum_partial);
   cudaFree(b->sum_out);
-  if (b->st) cudaStreamDestroy(b->st);
+  for (cudaStream_t x : {b->up, b->cv, b->st, b->down})
+    if (x) cudaStreamDestroy(x);
   delete b;
   return 0;
 }

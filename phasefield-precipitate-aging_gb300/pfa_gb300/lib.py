@@ -174,6 +174,7 @@ def load():
                                ctypes.POINTER(_i)]),
         "pfa_batch_remove": (_i, [ctypes.c_void_p, _i]),
         "pfa_batch_read": (_i, [ctypes.c_void_p, _i, _dp, _dp, _dp, _dp]),
+        "pfa_batch_read_async": (_i, [ctypes.c_void_p, _i, _dp, _dp, _dp, _dp]),
         "pfa_batch_run": (_i, [ctypes.c_void_p, _i]),
         "pfa_batch_run_timed": (_i, [ctypes.c_void_p, _i, _fp]),
         "pfa_batch_sync": (_i, [ctypes.c_void_p]),
@@ -567,6 +568,13 @@ class Batch:
     def read(self, slot, out=None):
         out = out or [np.empty(self.shapes[slot]) for _ in range(4)]
         check(self.L.pfa_batch_read(self.h, slot, *[_ptr(a) for a in out]), "pfa_batch_read")
+        return out
+
+    def read_async(self, slot, out):
+        """The slot's fields into `out` (four arrays, page-locked for the copy
+        to be asynchronous) after the runs enqueued so far; valid after sync()."""
+        check(self.L.pfa_batch_read_async(self.h, slot, *[_ptr(a) for a in out]),
+              "pfa_batch_read_async")
         return out
 
     def run(self, nsteps):

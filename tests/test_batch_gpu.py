@@ -165,3 +165,88 @@ def test_batch_errors(pfa):
         b.summarize(0)
     b.run(5)  # an empty batch runs nothing
     b.close()
+
+
+def _pinned(shape):
+    import torch
+    return torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+
+
+def test_async_reads_equal_sync_reads(pfa):
+    """pfa_batch_read_async into page-locked arrays, no wait until one sync:
+    the same fields as pfa_batch_read and as each grid run alone."""
+    p = pfa.model_params()
+    grids = _grids(seed0=40)
+    b = pfa.Batch(p, GIB)
+    slots = [b.add(f) for f in grids]
+    b.run(25)
+    outs = [[_pinned(f[0].shape) for _ in range(4)] for f in grids]
+    for s, o in zip(slots, outs):
+        b.read_async(s, o)
+    b.run(10)  # enqueued behind the reads: the reads keep the 25-step state
+    b.sync()
+    for s, f, o in zip(slots, grids, outs):
+        want, _ = _alone(pfa, f, p, 25)
+        assert _eq(o, want), s
+        assert _eq(b.read(s), _alone(pfa, f, p, 35)[0]), s
+    b.close()
+
+
+def test_staging_ring_wraps_without_host_waits(pfa):
+    """Many add / run / read / remove cycles enqueued without a wait, through
+    a staging ring far smaller than their traffic (16 MiB for ~80 MiB): every
+    cycle's read-out equals the grid run alone."""
+    p = pfa.model_params()
+    f = ic.grid2d(178, 178, seed=7, stripe_width=40, n_particles=2, radius=5.0)  # 1 MiB FP64
+    want, _ = _alone(pfa, f, p, 6)
+    b = pfa.Batch(p, 8 * pfa.Batch.footprint(f[0].shape))
+    host = [_pinned(f[0].shape) for _ in range(4)]
+    for x, a in zip(host, f):
+        x[...] = a
+    outs = []
+    for cycle in range(40):
+        s1, s2 = b.add(host), b.add(host)
+        b.run(6)
+        o = [[_pinned(f[0].shape) for _ in range(4)] for _ in range(2)]
+        b.read_async(s1, o[0])
+        b.read_async(s2, o[1])
+        b.remove(s1)
+        b.remove(s2)
+        outs += o
+    b.sync()
+    for k, o in enumerate(outs):
+        assert _eq(o, want), k
+    b.close()
+
+
+def test_removed_block_reused_at_once(pfa):
+    """A grid removed while its steps are still enqueued and another added
+    into the freed block right away: the new grid's import waits for those
+    steps, and it advances as it would alone."""
+    p = pfa.model_params()
+    fa = ic.grid2d(200, 150, seed=8, stripe_width=40, n_particles=3, radius=5.0)
+    fb = ic.grid2d(200, 150, seed=9, stripe_width=30, n_particles=2, radius=4.0)
+    b = pfa.Batch(p, pfa.Batch.footprint(fa[0].shape))  # room for one grid only
+    sa = b.add(fa)
+    b.run(200)
+    b.remove(sa)
+    sb = b.add(fb)
+    assert sb is not None
+    b.run(30)
+    assert _eq(b.read(sb), _alone(pfa, fb, p, 30)[0])
+    b.close()
+
+
+def test_grid_larger_than_the_staging_ring(pfa):
+    """A member whose FP64 fields exceed the ring grows it: one interior row
+    of 200 000 cells holds 19.2 MB of FP64 fields (ghost ring included) but
+    only 9.6 MB of FP32 records, so the ring (the arena's size, at least
+    16 MiB) is too small for it."""
+    p = pfa.model_params()
+    f = ic.grid2d(200000, 1, seed=10, stripe_width=5000, n_particles=0)
+    assert 4 * f[0].size * 8 > (16 << 20) > pfa.Batch.footprint(f[0].shape)
+    b = pfa.Batch(p, pfa.Batch.footprint(f[0].shape))
+    s = b.add(f)
+    b.run(12)
+    assert _eq(b.read(s), _alone(pfa, f, p, 12)[0])
+    b.close()
