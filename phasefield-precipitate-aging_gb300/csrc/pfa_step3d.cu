@@ -17,6 +17,7 @@
 //        phi_del, phi_lav}, B = the four compensations as packed 16-bit
 //        counts (uint2); tiles of 32 x 13 output cells, records staged by
 //        TMA, described below.
+#include <algorithm>
 #include <cstddef>
 #include <cstdint>
 #include <type_traits>
@@ -431,34 +432,32 @@ __global__ void __launch_bounds__(32 * kW3, 2)
       if (last[k] >= z0 - 1) tma::bar_wait(bar0 + 8 * k, uint32_t((last[k] - z0 + 1) >> 2) & 1u);
 }
 
-// FP64 ghost-ring fields <-> FP32 records (3D)
+// FP64 ghost-ring fields <-> FP32 records (3D): a thread per cell, the
+// launch grid covering (x, y) with its blocks and z with gridDim.z (looping
+// when Nz exceeds it), so no index needs a division
 __global__ void k_import3d(Conv3DArgs a) {
-  const long long n = (long long)a.Nx * a.Ny * a.Nz;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
-       t += (long long)gridDim.x * blockDim.x) {
-    const int x = int(t % a.Nx), y = int((t / a.Nx) % a.Ny), z = int(t / ((long long)a.Nx * a.Ny));
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= a.Nx || y >= a.Ny) return;
+  for (int z = blockIdx.z; z < a.Nz; z += gridDim.z) {
     const long long i64 = ((long long)(z + 1) * (a.Ny + 2) + (y + 1)) * (a.Nx + 2) + (x + 1);
     const long long r = ((long long)z * a.Ny + y) * a.pitch32 + x;
     float hi[4], c[4];
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
-      split_f64(a.f64[k][i64], hi[k], c[k]);  // value = hi - c
-    }
+    for (int k = 0; k < 4; k++) split_f64(a.f64[k][i64], hi[k], c[k]);  // value = hi - c
     reinterpret_cast<float4*>(a.A)[r] = make_float4(hi[0], hi[1], hi[2], hi[3]);
     static_cast<uint2*>(a.B)[r] = cq_pack(c[0], c[1], c[2], c[3]);
   }
 }
 
 __global__ void k_export3d(Conv3DArgs a) {
-  const long long n = (long long)a.Nx * a.Ny * a.Nz;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= a.Nx || y >= a.Ny) return;
   Step3DArgs g{};
   g.Nx = a.Nx;
   g.Ny = a.Ny;
   g.Nz = a.Nz;
   g.pitch = a.Nx + 2;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
-       t += (long long)gridDim.x * blockDim.x) {
-    const int x = int(t % a.Nx), y = int((t / a.Nx) % a.Ny), z = int(t / ((long long)a.Nx * a.Ny));
+  for (int z = blockIdx.z; z < a.Nz; z += gridDim.z) {
     const long long r = ((long long)z * a.Ny + y) * a.pitch32 + x;
     const float4 v = reinterpret_cast<const float4*>(a.A)[r];
     const float4 c = cq_unpack(static_cast<const uint2*>(a.B)[r]);
@@ -571,13 +570,17 @@ cudaError_t launch_step3d(Step3DArgs a, bool f64, const Tma3* t, cudaStream_t s)
   return cudaGetLastError();
 }
 
+dim3 conv3d_grid(const Conv3DArgs& a) {
+  return dim3((a.Nx + 31) / 32, (a.Ny + 7) / 8, std::min(a.Nz, 65535));
+}
+
 cudaError_t launch_import3d(const Conv3DArgs& a, cudaStream_t s) {
-  k_import3d<<<1024, 256, 0, s>>>(a);
+  k_import3d<<<conv3d_grid(a), dim3(32, 8), 0, s>>>(a);
   return cudaGetLastError();
 }
 
 cudaError_t launch_export3d(const Conv3DArgs& a, cudaStream_t s) {
-  k_export3d<<<1024, 256, 0, s>>>(a);
+  k_export3d<<<conv3d_grid(a), dim3(32, 8), 0, s>>>(a);
   return cudaGetLastError();
 }
 
