@@ -316,12 +316,20 @@ int order_after(Batch* b, cudaStream_t waiter, cudaStream_t from) {
 // writer waits for the last readers of the bytes it overwrites
 int ring_take(Batch* b, size_t n, cudaStream_t writer, size_t* off) {
   n = (n + kAlign - 1) / kAlign * kAlign;
-  while (!b->ring_q.empty() && cudaEventQuery(b->ring_q.front().done) == cudaSuccess) {
+  // drop the regions whose last use has completed (oldest first)
+  while (!b->ring_q.empty()) {
+    const cudaError_t q = cudaEventQuery(b->ring_q.front().done);
+    if (q == cudaErrorNotReady) {
+      // not an error: clear it if the query left it as the thread's last
+      // error, and leave any other pending error for its own check
+      if (cudaPeekAtLastError() == cudaErrorNotReady) (void)cudaGetLastError();
+      break;
+    }
+    CKB(q);
     b->ev_pool.push_back(b->ring_q.front().done);
     b->ring_q.pop_front();
   }
-  (void)cudaGetLastError();  // cudaErrorNotReady from the queries is not an error
-  if (n > b->ring_cap) {     // grow: rare; drain every stream first
+  if (n > b->ring_cap) {  // grow: rare; drain every stream first
     for (cudaStream_t x : {b->up, b->cv, b->st, b->down}) CKB(cudaStreamSynchronize(x));
     for (auto& e : b->ring_q) b->ev_pool.push_back(e.done);
     b->ring_q.clear();
