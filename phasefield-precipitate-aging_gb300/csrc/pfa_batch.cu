@@ -418,7 +418,7 @@ const Slot* live_slot(Batch* b, int slot) {
 }
 
 // A slot for an nx x ny grid (ghost-ring sizes) in the arena; its records
-// are filled from the FP64 staging fields by the caller.
+// are filled by the caller (an import from FP64 fields in the staging ring).
 int place(Batch* b, int nx, int ny, int* id_out) {
   Slot s;
   s.Nx = nx - 2;
