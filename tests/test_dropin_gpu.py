@@ -105,16 +105,19 @@ def _ok(pfa, what):
     assert err == 0, f"{what}: {L.pfa_last_error_message().decode()}"
 
 
-def _drive(pfa, fields, params, steps, io, precision=0):
+def _drive(pfa, fields, params, steps, io, precision=0, mask=None):
     """src/main.cpp's loop through the mangled entry points; returns
-    {step: (dataviz arrays, read_out_result arrays)} at every output step."""
+    {step: (dataviz arrays, read_out_result arrays)} at every output step.
+    mask: the 3 x 3 Laplacian mask in host.mask_lap (default: the 5-point
+    mask of src/main.cpp:237)."""
     fn = _abi(pfa)
     L = pfa.load()
     L.pfa_clear_error()
     ny, nx = fields[0].shape
     nm, bx, by = 3, 13, 13
     host = Host(nx, ny, nm)
-    host.blocks["mask_lap"][:] = pfa.five_point_mask(params["dx"], params["dx"])
+    host.blocks["mask_lap"][:] = (pfa.five_point_mask(params["dx"], params["dx"]) if mask is None
+                                  else mask)
     for name, a in zip(("conc_Cr_old", "conc_Nb_old", "phi_del_old", "phi_lav_old"), fields):
         host.blocks[name][:] = a
     consts = [np.ascontiguousarray(params[k], dtype=np.float64)
@@ -223,6 +226,27 @@ def test_fp32_driver_loop_matches_reference_kernels(pfa, tmp_path, caller):
     for a, b in zip(g.read(), out[1000][1]):
         assert np.array_equal(interior(a), interior(b))
     g.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_driver_loop_with_nine_point_mask(pfa, precision):
+    """The reference's loop with its 9-point mask in host.mask_lap
+    (nine_point_Laplacian_stencil, src/mesh.cpp:198-213), FP64 and the FP32
+    form, against the reference's CUDA kernels run with the same mask
+    (tests/golden/ref_gpu_nine.npz) after 100 steps."""
+    r = golden("ref_gpu_nine.npz")
+    p = pfa.model_params()
+    dx, dy = r["iso_dxy"]
+    m9 = pfa.nine_point_mask(dx, dy)
+    out = _drive(pfa, fields_of(r, "ic"), p, 100, 100,
+                 precision=pfa.FP32 if precision == "fp32" else 0, mask=m9)
+    _check_dataviz(*out[100])
+    want = fields_of(r, "iso_s100")
+    if precision == "fp64":
+        assert max(field_err(out[100][1], want)) <= FP64_TOL
+    else:
+        err = [float(np.max(np.abs(interior(a) - interior(b)))) for a, b in zip(out[100][1], want)]
+        assert max(err) <= FP32_TOL_1000, err
 
 
 def test_driver_loop_with_nucleation_equals_library_loop(pfa, tmp_path):
