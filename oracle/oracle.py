@@ -24,13 +24,23 @@ class OrcParams(ctypes.Structure):
                 ("kappa", ctypes.c_double * 2), ("omega", ctypes.c_double * 2),
                 ("Lmob", ctypes.c_double * 2), ("alpha", ctypes.c_double),
                 ("dt", ctypes.c_double), ("dx", ctypes.c_double),
-                ("dy", ctypes.c_double), ("dz", ctypes.c_double)]
+                ("dy", ctypes.c_double), ("dz", ctypes.c_double),
+                ("mask3", ctypes.c_int), ("mask9", ctypes.c_double * 9)]
 
     def as_dict(self):
         return {"D_Cr": list(self.D_Cr), "D_Nb": list(self.D_Nb),
                 "kappa": list(self.kappa), "omega": list(self.omega),
                 "Lmob": list(self.Lmob), "alpha": self.alpha, "dt": self.dt,
                 "dx": self.dx, "dy": self.dy, "dz": self.dz}
+
+    def with_mask(self, mask):
+        """A copy whose 2D step convolves the 3 x 3 `mask` as given (the
+        reference's convolution_kernel) instead of the 5-point mask."""
+        p = OrcParams.from_buffer_copy(self)
+        p.mask3 = 1
+        for k, w in enumerate(np.asarray(mask, dtype=np.float64).ravel()):
+            p.mask9[k] = w
+        return p
 
     @classmethod
     def from_dict(cls, d):

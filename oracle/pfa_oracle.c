@@ -322,6 +322,8 @@ void orc_model_params_rule(double dx, double ifce_width, double xcr0, double xnb
 	}
 	o->dt = round_dt;
 	o->dx = o->dy = o->dz = dx;
+	o->mask3 = 0;
+	for (int k = 0; k < 9; k++) o->mask9[k] = 0.0;
 }
 
 void orc_model_params(double dx, double ifce_width, double xcr0, double xnb0,

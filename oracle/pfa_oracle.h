@@ -35,6 +35,10 @@ typedef struct {
 	double alpha;     /* three-phase penalty (Omega), J/m^3 */
 	double dt;        /* time step, s */
 	double dx, dy, dz;/* grid spacing, m (dz unused in 2D) */
+	int mask3;        /* 2D step: 0 = the 5-point mask of dx, dy (src/mesh.cpp:187-196);
+	                     1 = convolve mask9 as given, like the reference's
+	                     convolution_kernel (src/discretization.cu:550-603) */
+	double mask9[9];  /* 3 x 3 mask, rows y-1 .. y+1, columns x-1 .. x+1 */
 } orc_params;
 
 typedef struct {

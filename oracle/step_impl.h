@@ -156,6 +156,8 @@ void SFN(step2d)(double* old_f[4], double* new_f[4], int nx, int ny,
 	const double m_e = 1. / (dx * dx);
 	const double m_s = 1. / (dy * dy);
 	const double* src[4] = {gcr, gnb, old_f[2], old_f[3]};
+	const double* m9 = prm->mask9;
+	const int general = prm->mask3;
 	int y;
 	#pragma omp parallel for schedule(static)
 	for (y = 1; y < ny - 1; y++) {
@@ -165,11 +167,19 @@ void SFN(step2d)(double* old_f[4], double* new_f[4], int nx, int ny,
 			for (int x = 1; x < nx - 1; x++) {
 				const size_t i = (size_t)y * nx + x;
 				double v = 0.;
-				v += m_n * s[i - nx];
-				v += m_w * s[i - 1];
-				v += m_c * s[i];
-				v += m_e * s[i + 1];
-				v += m_s * s[i + nx];
+				if (general) {
+					/* the mask as given, in convolution_kernel's order
+					 * (src/discretization.cu:586-595): rows j, columns i */
+					for (int j = -1; j <= 1; j++)
+						for (int c = -1; c <= 1; c++)
+							v += m9[(j + 1) * 3 + (c + 1)] * s[i + (long)j * nx + c];
+				} else {
+					v += m_n * s[i - nx];
+					v += m_w * s[i - 1];
+					v += m_c * s[i];
+					v += m_e * s[i + 1];
+					v += m_s * s[i + nx];
+				}
 				d[i] = v;
 			}
 		}

@@ -127,6 +127,32 @@ def test_oracle_3d_reduces_to_2d(orc):
         assert np.max(np.abs(a[2, 1:-1, 1:-1] - b[1:-1, 1:-1])) <= 1e-12 * np.max(np.abs(b))
 
 
+def test_nine_point_step_matches_reference_cuda_kernels(orc):
+    """The oracle with the reference's 9-point mask (convolved as given, like
+    its convolution_kernel) against the reference's own CUDA step run with
+    that mask (tests/golden/ref_gpu_nine.npz): dx = dy after 1, 10, 100, 500
+    steps and dy = 1.25 dx after 100, whole arrays (the 260-cell side makes
+    the reference's ghost corners deterministic) within 1e-12 of each
+    field's magnitude; measured <= 2.4e-15."""
+    from ref_gpu import nine_point_mask
+    r = golden("ref_gpu_nine.npz")
+    prm = O.model_params()
+    assert prm.dt == r["dt"][0]
+    for tag in ("iso", "aniso"):
+        q = prm.with_mask(nine_point_mask(*r[f"{tag}_dxy"]))
+        cur, done = fields_of(r, "ic"), 0
+        counts = sorted(int(k.split("_s")[1].split("_")[0]) for k in r.files
+                        if k.startswith(f"{tag}_s") and k.endswith("_cr"))
+        for k in counts:
+            cur = orc.run2d(cur, q, k - done)
+            done = k
+            want = fields_of(r, f"{tag}_s{k}")
+            err = [float(np.max(np.abs(a - b)) / np.max(np.abs(b))) for a, b in zip(cur, want)]
+            assert max(err) <= 1e-12, (tag, k, err)
+    # the default (5-point) step is untouched by the mask fields
+    assert O.model_params().mask3 == 0
+
+
 def test_step_matches_reference_cuda_kernels(orc):
     """The oracle's step against the reference's own CUDA step kernels
     (src/discretization.cu, compiled here for sm_103a and run on a GB300 by
