@@ -194,6 +194,26 @@ def test_nine_point_mask_fused_matches_stages(pfa):
     b.close()
 
 
+@pytest.mark.parametrize("shape", [(1, 1), (5, 7), (17, 13), (33, 65), (100, 3)])
+@pytest.mark.parametrize("dy_over_dx", [1.0, 1.25])
+def test_nine_point_mask_odd_sizes_match_oracle(pfa, orc, shape, dy_over_dx):
+    """The fused FP64 step with the 9-point mask against the oracle convolving
+    the same mask (itself pinned to the reference's kernels run with it) on
+    odd sizes, both spacings, within 1e-12."""
+    from pfa_gb300 import ic
+    ny, nx = shape
+    f = ic.grid2d(nx, ny, seed=nx * 11 + ny, stripe_width=max(1, nx // 3),
+                  n_particles=1 if min(nx, ny) > 12 else 0, radius=3.0)
+    p = _params(pfa)
+    p["dy"] = p["dx"] * dy_over_dx
+    m9 = pfa.nine_point_mask(p["dx"], p["dy"])
+    want = orc.run2d(f, O.model_params().with_mask(m9), 60)
+    g = pfa.Grid2D(f, p, mask=m9)
+    g.run(60)
+    assert max(field_err(g.read(), want)) <= FP64_TOL
+    g.close()
+
+
 def test_nine_point_mask_matches_reference_cuda_kernels(pfa):
     """The 9-point mask against the reference's own CUDA step run with it on
     a GB300 (tests/golden/ref_gpu_nine.npz, 260 x 260 interior, the side on
