@@ -325,6 +325,25 @@ int pfa_summarize_fields_noalloc(const double* conc_Cr, const double* conc_Nb,
                                  const double* phi_del, const double* phi_lav, int nx, int ny,
                                  double* out, void* stream);
 
+/* ---- checkpoint / resume ----
+ * What a run continues from besides its fields (pfa_read_out_result, and
+ * pfa_init_cuda to start again): the step counter (the phase of the
+ * nucleation interval) and the nucleation call counter (the Philox counter of
+ * the next call); for the FP32 forms also their records, written back
+ * exactly, so that a resumed run is bit-identical to an uninterrupted one
+ * (FP64 fields alone would re-split every value, which can move a
+ * compensation that sits exactly at half an FP32 ulp).  The reference writes
+ * its checkpoints as MMSP grid files (src/main.cpp:408), a format this
+ * library does not read or write.  pfa_f32_state_bytes is 0 for an FP64
+ * handle; pfa_read_f32_state / pfa_write_f32_state take exactly that many
+ * bytes and wait for the copies.  pfa_set_counters after
+ * pfa_set_nucleation / pfa_set_nucleation_args, which reset them. */
+int pfa_get_counters(struct CudaData* dev, uint64_t* steps, uint64_t* nucleation_calls);
+int pfa_set_counters(struct CudaData* dev, uint64_t steps, uint64_t nucleation_calls);
+size_t pfa_f32_state_bytes(struct CudaData* dev);
+int pfa_read_f32_state(struct CudaData* dev, void* host, size_t bytes);
+int pfa_write_f32_state(struct CudaData* dev, const void* host, size_t bytes);
+
 /* ---- on-device FP64 free energy (summarize_energy, src/alloy625.cpp:865-919,
  * with gibbs :752-786 and maskedgradient :788-807) ----
  * *energy = sum over interior nodes of dV (g(x, phi) + sum_i kappa_i |grad phi_i|^2),

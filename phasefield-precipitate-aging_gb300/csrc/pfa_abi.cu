@@ -1151,6 +1151,68 @@ int pfa_run_timed(struct CudaData* dev, int nsteps, double alpha, double dt, flo
   return 0;
 }
 
+// ---- checkpoint / resume ----
+int pfa_get_counters(struct CudaData* dev, uint64_t* steps, uint64_t* nucleation_calls) {
+  State* s = lookup(dev);
+  if (!s) return fail(PFA_ESTATE, "pfa_get_counters: unknown CudaData");
+  if (steps) *steps = s->step_counter;
+  if (nucleation_calls) *nucleation_calls = s->calls;
+  return 0;
+}
+
+int pfa_set_counters(struct CudaData* dev, uint64_t steps, uint64_t nucleation_calls) {
+  State* s = lookup(dev);
+  if (!s) return fail(PFA_ESTATE, "pfa_set_counters: unknown CudaData");
+  const unsigned long long calls = nucleation_calls;
+  CK(cudaMemcpyAsync(s->call_dev, &calls, sizeof(calls), cudaMemcpyHostToDevice, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  s->step_counter = steps;
+  s->calls = nucleation_calls;
+  return 0;
+}
+
+// bytes of the FP32 form's records: A (16 B) then B (8 B packed, 16 B in
+// PFA_FP32_KPHI) for pitch32 x Ny records each
+static size_t f32_state_bytes(const State* s) {
+  if (s->precision == PFA_FP64) return 0;
+  const size_t recs = size_t((s->Nx + 31) / 32) * 32 * s->Ny;
+  return recs * 16 + recs * (s->precision == PFA_FP32_KPHI ? 16 : 8);
+}
+
+size_t pfa_f32_state_bytes(struct CudaData* dev) {
+  State* s = lookup(dev);
+  return s ? f32_state_bytes(s) : 0;
+}
+
+int pfa_read_f32_state(struct CudaData* dev, void* host, size_t bytes) {
+  State* s = lookup(dev);
+  if (!s) return fail(PFA_ESTATE, "pfa_read_f32_state: unknown CudaData");
+  if (s->precision == PFA_FP64) return fail(PFA_EINVAL, "pfa_read_f32_state: the handle is FP64");
+  if (!host || bytes != f32_state_bytes(s)) return fail(PFA_EINVAL, "pfa_read_f32_state: buffer size");
+  if (int r = f32_import(dev, s)) return r;  // the records, from the FP64 fields if not live yet
+  const size_t a = size_t(s->pitch32) * s->Ny * 16;
+  CK(cudaMemcpyAsync(host, s->recA[s->cur], a, cudaMemcpyDeviceToHost, s->st));
+  CK(cudaMemcpyAsync(static_cast<char*>(host) + a, s->recB[s->cur], bytes - a,
+                     cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  return 0;
+}
+
+int pfa_write_f32_state(struct CudaData* dev, const void* host, size_t bytes) {
+  State* s = lookup(dev);
+  if (!s) return fail(PFA_ESTATE, "pfa_write_f32_state: unknown CudaData");
+  if (s->precision == PFA_FP64) return fail(PFA_EINVAL, "pfa_write_f32_state: the handle is FP64");
+  if (!host || bytes != f32_state_bytes(s)) return fail(PFA_EINVAL, "pfa_write_f32_state: buffer size");
+  if (int r = ensure_f32(s)) return r;
+  const size_t a = size_t(s->pitch32) * s->Ny * 16;
+  CK(cudaMemcpyAsync(s->recA[s->cur], host, a, cudaMemcpyHostToDevice, s->st));
+  CK(cudaMemcpyAsync(s->recB[s->cur], static_cast<const char*>(host) + a, bytes - a,
+                     cudaMemcpyHostToDevice, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  s->f32_live = true;  // the records are the state now
+  return 0;
+}
+
 int pfa_sync(struct CudaData* dev) {
   State* s = lookup(dev);
   if (!s) return fail(PFA_ESTATE, "pfa_sync: unknown CudaData");

@@ -118,6 +118,11 @@ def load():
         "pfa_set_precision": (_i, [P, _i]),
         "pfa_set_nucleation": (_i, [P, ctypes.c_uint64, _i]),
         "pfa_set_mobility": (_i, [P, _i]),
+        "pfa_get_counters": (_i, [P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]),
+        "pfa_set_counters": (_i, [P, ctypes.c_uint64, ctypes.c_uint64]),
+        "pfa_f32_state_bytes": (ctypes.c_size_t, [P]),
+        "pfa_read_f32_state": (_i, [P, ctypes.c_void_p, ctypes.c_size_t]),
+        "pfa_write_f32_state": (_i, [P, ctypes.c_void_p, ctypes.c_size_t]),
         "pfa_device_mobilities": (_i, [P, _i, _i, _i, _i, _i]),
         "pfa_mobility_boundaries": (_i, [P, _i, _i, _i, _i, _i]),
         "pfa_set_nucleation_args": (_i, [P, _i, _d, _d, _d, _d, _d, _d, _d]),
@@ -275,6 +280,7 @@ class Grid2D:
                               *[_ptr(c) for c in self._consts], *[_ptr(a) for a in f]),
               "pfa_init_cuda")
         self._live = True
+        self.mode, self.mobility, self.nucleation = mode, mobility, None
         if mode == "compat":
             check(L.pfa_set_mode(ctypes.byref(self.dev), MODE_COMPAT), "pfa_set_mode")
         self.set_precision(precision)
@@ -297,6 +303,50 @@ class Grid2D:
         dt_nuc = dt_nuc if dt_nuc is not None else interval * self.params["dt"]
         check(self.L.pfa_set_nucleation_args(self.ref, interval, sigma[0], sigma[1], unit_a,
                                              d[0], d[1], d[2], dt_nuc), "pfa_set_nucleation_args")
+        self.nucleation = dict(seed=int(seed), geometry=int(geometry), interval=int(interval),
+                               sigma=[float(v) for v in sigma], unit_a=float(unit_a),
+                               d=[float(v) for v in d], dt_nuc=float(dt_nuc))
+
+    def checkpoint(self, path):
+        """Write everything the run continues from to one .npz file: the
+        fields (FP64, the reference layout, ghost ring included), the mask,
+        parameters and settings, the step and nucleation-call counters and,
+        for the FP32 forms, their records; Grid2D.resume(path) continues
+        bit-identically."""
+        import json
+        steps, calls = ctypes.c_uint64(), ctypes.c_uint64()
+        check(self.L.pfa_get_counters(self.ref, ctypes.byref(steps), ctypes.byref(calls)),
+              "pfa_get_counters")
+        fields = self.read()
+        extra = {}
+        nb = int(self.L.pfa_f32_state_bytes(self.ref))
+        if nb:
+            raw = np.empty(nb, dtype=np.uint8)
+            check(self.L.pfa_read_f32_state(self.ref, raw.ctypes.data, nb), "pfa_read_f32_state")
+            extra["f32_state"] = raw
+        meta = dict(params=self.params, precision=self.precision, mode=self.mode,
+                    mobility=self.mobility, nucleation=self.nucleation,
+                    steps=int(steps.value), nucleation_calls=int(calls.value))
+        np.savez(path, cr=fields[0], nb=fields[1], pd=fields[2], pl=fields[3], mask=self.mask,
+                 meta=np.array(json.dumps(meta)), **extra)
+
+    @classmethod
+    def resume(cls, path):
+        """A new handle in the state a checkpoint() file holds."""
+        import json
+        z = np.load(path)
+        meta = json.loads(str(z["meta"]))
+        g = cls([z[k] for k in ("cr", "nb", "pd", "pl")], meta["params"],
+                precision=meta["precision"], mode=meta["mode"], mask=z["mask"],
+                mobility=meta["mobility"])
+        if meta["nucleation"]:
+            g.set_nucleation(**meta["nucleation"])
+        check(g.L.pfa_set_counters(g.ref, meta["steps"], meta["nucleation_calls"]),
+              "pfa_set_counters")
+        if "f32_state" in z.files:
+            raw = np.ascontiguousarray(z["f32_state"])
+            check(g.L.pfa_write_f32_state(g.ref, raw.ctypes.data, raw.size), "pfa_write_f32_state")
+        return g
 
     def run(self, nsteps, dt=None, alpha=None):
         dt = self.params["dt"] if dt is None else dt
