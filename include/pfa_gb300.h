@@ -163,6 +163,15 @@ int pfa3d_create(void** handle, int nx, int ny, int nz, const double* params, co
                  const double* conc_Cr, const double* conc_Nb, const double* phi_del,
                  const double* phi_lav, int precision);
 int pfa3d_run(void* handle, int nsteps);
+/* checkpoint / resume of a 3D grid: as pfa_get_counters, pfa_set_counters,
+ * pfa_f32_state_bytes, pfa_read_f32_state and pfa_write_f32_state (FP32:
+ * A then packed B records, pitch32 x Ny x Nz of each); pfa3d_set_counters
+ * after pfa3d_set_nucleation, which resets them */
+int pfa3d_get_counters(void* handle, uint64_t* steps, uint64_t* nucleation_calls);
+int pfa3d_set_counters(void* handle, uint64_t steps, uint64_t nucleation_calls);
+size_t pfa3d_f32_state_bytes(void* handle);
+int pfa3d_read_f32_state(void* handle, void* host, size_t bytes);
+int pfa3d_write_f32_state(void* handle, const void* host, size_t bytes);
 int pfa3d_run_timed(void* handle, int nsteps, float* ms);
 int pfa3d_sync(void* handle);  /* wait for the handle's enqueued work */
 int pfa3d_read(void* handle, double* conc_Cr, double* conc_Nb, double* phi_del, double* phi_lav);

@@ -490,6 +490,66 @@ int pfa3d_test_skip_plane(void* handle, int plane) {
   return 0;
 }
 
+// ---- checkpoint / resume (as pfa_get_counters ... for CudaData) ----
+int pfa3d_get_counters(void* handle, uint64_t* steps, uint64_t* nucleation_calls) {
+  Grid3D* g = static_cast<Grid3D*>(handle);
+  if (!g) return err(PFA_ESTATE, "pfa3d_get_counters: null handle");
+  unsigned long long calls = 0;  // the call counter lives on the device
+  CK3(cudaMemcpyAsync(&calls, g->call_dev, sizeof(calls), cudaMemcpyDeviceToHost, g->st));
+  CK3(cudaStreamSynchronize(g->st));
+  if (steps) *steps = g->step_counter;
+  if (nucleation_calls) *nucleation_calls = calls;
+  return 0;
+}
+
+int pfa3d_set_counters(void* handle, uint64_t steps, uint64_t nucleation_calls) {
+  Grid3D* g = static_cast<Grid3D*>(handle);
+  if (!g) return err(PFA_ESTATE, "pfa3d_set_counters: null handle");
+  const unsigned long long calls = nucleation_calls;
+  CK3(cudaMemcpyAsync(g->call_dev, &calls, sizeof(calls), cudaMemcpyHostToDevice, g->st));
+  CK3(cudaStreamSynchronize(g->st));
+  g->step_counter = steps;
+  return 0;
+}
+
+// A (16 B) then packed B (8 B) records, pitch32 x Ny x Nz of each
+static size_t f32_state_bytes3(const Grid3D* g) {
+  if (g->precision == PFA_FP64) return 0;
+  return size_t(g->pitch32) * g->Ny * g->Nz * 24;
+}
+
+size_t pfa3d_f32_state_bytes(void* handle) {
+  Grid3D* g = static_cast<Grid3D*>(handle);
+  return g ? f32_state_bytes3(g) : 0;
+}
+
+int pfa3d_read_f32_state(void* handle, void* host, size_t bytes) {
+  Grid3D* g = static_cast<Grid3D*>(handle);
+  if (!g) return err(PFA_ESTATE, "pfa3d_read_f32_state: null handle");
+  if (g->precision == PFA_FP64) return err(PFA_EINVAL, "pfa3d_read_f32_state: the grid is FP64");
+  if (!host || bytes != f32_state_bytes3(g)) return err(PFA_EINVAL, "pfa3d_read_f32_state: buffer size");
+  if (int r = ensure_live(g)) return r;
+  const size_t a = size_t(g->pitch32) * g->Ny * g->Nz * 16;
+  CK3(cudaMemcpyAsync(host, g->A[g->cur], a, cudaMemcpyDeviceToHost, g->st));
+  CK3(cudaMemcpyAsync(static_cast<char*>(host) + a, g->B[g->cur], bytes - a,
+                      cudaMemcpyDeviceToHost, g->st));
+  return check_status(g);  // waits for the copies
+}
+
+int pfa3d_write_f32_state(void* handle, const void* host, size_t bytes) {
+  Grid3D* g = static_cast<Grid3D*>(handle);
+  if (!g) return err(PFA_ESTATE, "pfa3d_write_f32_state: null handle");
+  if (g->precision == PFA_FP64) return err(PFA_EINVAL, "pfa3d_write_f32_state: the grid is FP64");
+  if (!host || bytes != f32_state_bytes3(g)) return err(PFA_EINVAL, "pfa3d_write_f32_state: buffer size");
+  const size_t a = size_t(g->pitch32) * g->Ny * g->Nz * 16;
+  CK3(cudaMemcpyAsync(g->A[g->cur], host, a, cudaMemcpyHostToDevice, g->st));
+  CK3(cudaMemcpyAsync(g->B[g->cur], static_cast<const char*>(host) + a, bytes - a,
+                      cudaMemcpyHostToDevice, g->st));
+  CK3(cudaStreamSynchronize(g->st));
+  g->f32_live = true;  // the records are the state now
+  return 0;
+}
+
 int pfa3d_sync(void* handle) {
   Grid3D* g = static_cast<Grid3D*>(handle);
   if (!g) return err(PFA_ESTATE, "pfa3d_sync: null handle");

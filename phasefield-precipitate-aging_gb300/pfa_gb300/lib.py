@@ -158,6 +158,12 @@ def load():
         "pfa3d_create": (_i, [ctypes.POINTER(ctypes.c_void_p), _i, _i, _i, _dp, _dp, _dp, _dp,
                               _dp, _dp, _i]),
         "pfa3d_run": (_i, [ctypes.c_void_p, _i]),
+        "pfa3d_get_counters": (_i, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64),
+                                    ctypes.POINTER(ctypes.c_uint64)]),
+        "pfa3d_set_counters": (_i, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64]),
+        "pfa3d_f32_state_bytes": (ctypes.c_size_t, [ctypes.c_void_p]),
+        "pfa3d_read_f32_state": (_i, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]),
+        "pfa3d_write_f32_state": (_i, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]),
         "pfa3d_run_timed": (_i, [ctypes.c_void_p, _i, _fp]),
         "pfa3d_read": (_i, [ctypes.c_void_p, _dp, _dp, _dp, _dp]),
         "pfa3d_upload": (_i, [ctypes.c_void_p, _dp, _dp, _dp, _dp]),
@@ -486,6 +492,7 @@ class Grid3D:
             check(L.pfa3d_create(ctypes.byref(self.h), nx, ny, nz, _ptr(self._pv), _ptr(self._d),
                                  *[_ptr(a) for a in f], PRECISIONS[precision]), "pfa3d_create")
         self._live = True
+        self.precision, self.nucleation = precision, None
 
     @staticmethod
     def footprint(shape, precision="fp32"):
@@ -517,6 +524,45 @@ class Grid3D:
         dt_nuc = dt_nuc if dt_nuc is not None else max(interval, 1) * self.params["dt"]
         check(self.L.pfa3d_set_nucleation(self.h, seed, interval, sigma[0], sigma[1], unit_a,
                                           d[0], d[1], d[2], dt_nuc), "pfa3d_set_nucleation")
+        self.nucleation = dict(seed=int(seed), interval=int(interval),
+                               sigma=[float(v) for v in sigma], unit_a=float(unit_a),
+                               d=[float(v) for v in d], dt_nuc=float(dt_nuc))
+
+    def checkpoint(self, path):
+        """As Grid2D.checkpoint, for a 3D grid."""
+        import json
+        steps, calls = ctypes.c_uint64(), ctypes.c_uint64()
+        check(self.L.pfa3d_get_counters(self.h, ctypes.byref(steps), ctypes.byref(calls)),
+              "pfa3d_get_counters")
+        fields = self.read()
+        extra = {}
+        nb = int(self.L.pfa3d_f32_state_bytes(self.h))
+        if nb:
+            raw = np.empty(nb, dtype=np.uint8)
+            check(self.L.pfa3d_read_f32_state(self.h, raw.ctypes.data, nb), "pfa3d_read_f32_state")
+            extra["f32_state"] = raw
+        meta = dict(params=self.params, precision=self.precision, nucleation=self.nucleation,
+                    steps=int(steps.value), nucleation_calls=int(calls.value))
+        np.savez(path, cr=fields[0], nb=fields[1], pd=fields[2], pl=fields[3],
+                 meta=np.array(json.dumps(meta)), **extra)
+
+    @classmethod
+    def resume(cls, path):
+        """A new 3D handle in the state a checkpoint() file holds."""
+        import json
+        z = np.load(path)
+        meta = json.loads(str(z["meta"]))
+        g = cls([z[k] for k in ("cr", "nb", "pd", "pl")], meta["params"],
+                precision=meta["precision"])
+        if meta["nucleation"]:
+            g.set_nucleation(**meta["nucleation"])
+        check(g.L.pfa3d_set_counters(g.h, meta["steps"], meta["nucleation_calls"]),
+              "pfa3d_set_counters")
+        if "f32_state" in z.files:
+            raw = np.ascontiguousarray(z["f32_state"])
+            check(g.L.pfa3d_write_f32_state(g.h, raw.ctypes.data, raw.size),
+                  "pfa3d_write_f32_state")
+        return g
 
     def events(self, cap=1 << 16):
         cells = (ctypes.c_int64 * cap)()
