@@ -307,9 +307,11 @@ def grid4096(c, quick_error=True):
     """The headline workload; returns its JSON line (rank 0) or None."""
     args, ws, rank, pl, ic = c.args, c.ws, c.rank, c.pl, c.ic
     import torch
-    fields = ic.config2(seed=2 + rank, n=N_SIDE)
+    # --side resizes the grid of a value-only run (smaller profiler captures)
+    side = args.side if args.only == "value" and args.side else N_SIDE
+    fields = ic.config2(seed=2 + rank, n=side)
     params = pl.model_params()
-    cells = N_SIDE * N_SIDE
+    cells = side * side
     nuc_kw = dict(seed=42, geometry=pl.NUC_REFERENCE_GEOMETRY, interval=STEPS_PER_BENCH_STEP,
                   sigma=NUC["sigma"], unit_a=NUC["unit_a"], d=(params["dx"],) * 3,
                   dt_nuc=STEPS_PER_BENCH_STEP * params["dt"])
@@ -336,7 +338,8 @@ def grid4096(c, quick_error=True):
     if args.only == "value":
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": "cell-updates/s",
-                              "ms_per_step": 1e3 * t / args.steps, "partial": "value only"}))
+                              "ms_per_step": 1e3 * t / args.steps, "partial": "value only",
+                              "nx": side, "ny": side}))
         return None
 
     # the whole 10 000-step run of the workload from its initial condition
@@ -953,7 +956,8 @@ def main():
                     help="all: the headline line with every other workload inside it; "
                          "the others print one workload's own line")
     ap.add_argument("--side", type=int, default=0,
-                    help="grid3d512 / error: another cube side (smaller profiler captures)")
+                    help="grid3d512 / error: another cube side; grid4096 with --only value: "
+                         "another square side (smaller profiler captures)")
     ap.add_argument("--requests", type=int, default=SERVE_COUNT, help="serve: trace length")
     ap.add_argument("--error-steps", type=int, default=0,
                     help="error: 2D step count (default 10000; 3D and batch take min(n, 2000 / "

@@ -91,30 +91,42 @@ __global__ void __launch_bounds__(256) k_nuc_decide(NucArgs a) {
 }
 
 // The decisions of a call whose neighbourhood scan covers each cell alone
-// (R_scan <= 1 cell, as in the reference's geometry): one cell per thread,
-// one coalesced load of its values, the clear test and the first tier of the
-// screen inline (the rest of the screen, the FP64 path and the lists are
-// calls the few open lanes take), so the kernel stays small enough for high
-// occupancy, which hides the loads' latency.
+// (R_scan <= 1 cell, as in the reference's geometry): one coalesced load of
+// a cell's values, the clear test and the screen.  The pass is bound by
+// instruction issue (the screen), not by its 16 B per cell: each thread takes
+// kOwnRows cells 8 rows apart and issues their loads before any screen, so
+// that four CTAs per SM (64 registers, room for the inlined screen) keep
+// enough bytes in flight.
+constexpr int kOwnRows = 4;
+
 template <class T>
-__global__ void __launch_bounds__(256, 6) k_nuc_decide_own(NucArgs a) {
+__global__ void __launch_bounds__(256, 4) k_nuc_decide_own(NucArgs a) {
   const int gx = blockIdx.x * 32 + (threadIdx.x & 31);
-  const int gy = blockIdx.y * 8 + (threadIdx.x >> 5);
-  bool need = false;
-  long long idx = 0;
-  size_t s = 0;
-  uint4 w = make_uint4(0, 0, 0, 0);
-  if (gx < a.Nx && gy < a.Ny) {
-    const int x = gx + 1, y = gy + 1, z = a.is3d ? int(blockIdx.z) + 1 : 0;
-    idx = ((long long)z * (a.Ny + 2) + y) * (a.Nx + 2) + x;
-    s = stor(a, x, y, z);
-    float v[4];
-    own_values<T>(a, s, v);
-    int clear = clear_fp32(v[2], v[3]);
-    if (clear < 0) clear = clear_exact(ldval<T>(a, 2, s), ldval<T>(a, 3, s));
-    if (clear) need = nuc_screen(a, v[0], v[1], idx, w);
+  const int gy0 = blockIdx.y * (8 * kOwnRows) + (threadIdx.x >> 5);
+  const int z = a.is3d ? int(blockIdx.z) + 1 : 0;
+  float v[kOwnRows][4];
+#pragma unroll
+  for (int r = 0; r < kOwnRows; r++) {
+    const int gy = gy0 + 8 * r;
+    if (gx < a.Nx && gy < a.Ny) own_values<T>(a, stor(a, gx + 1, gy + 1, z), v[r]);
   }
-  nuc_list_or_decide<T>(a, need, idx, s, w);
+#pragma unroll
+  for (int r = 0; r < kOwnRows; r++) {
+    const int gy = gy0 + 8 * r;
+    bool need = false;
+    long long idx = 0;
+    size_t s = 0;
+    uint4 w = make_uint4(0, 0, 0, 0);
+    if (gx < a.Nx && gy < a.Ny) {
+      const int x = gx + 1, y = gy + 1;
+      idx = ((long long)z * (a.Ny + 2) + y) * (a.Nx + 2) + x;
+      s = stor(a, x, y, z);
+      int clear = clear_fp32(v[r][2], v[r][3]);
+      if (clear < 0) clear = clear_exact(ldval<T>(a, 2, s), ldval<T>(a, 3, s));
+      if (clear) need = nuc_screen(a, v[r][0], v[r][1], idx, w);
+    }
+    nuc_list_or_decide<T>(a, need, idx, s, w);
+  }
 }
 
 // The FP64 decisions of the listed cells, 32 per warp.  Consecutive chunks
@@ -308,16 +320,18 @@ cudaError_t launch_nucleation(const NucArgs& a, cudaStream_t s) {
   const bool own = a.scan_lo == 0 && a.scan_hi == 1;  // the scan covers each cell alone
   // grid-stride over the FP64 list (its length is on the device): a CTA per SM
   const int fp64_blocks = 152;
+  // k_nuc_decide_own: 32 x (8 kOwnRows) cells per CTA
+  const dim3 grid_own(grid.x, (a.Ny + 8 * kOwnRows - 1) / (8 * kOwnRows), grid.z);
   if (a.is_f32) {
     if (own)
-      k_nuc_decide_own<float><<<grid, 256, 0, s>>>(a);
+      k_nuc_decide_own<float><<<grid_own, 256, 0, s>>>(a);
     else
       k_nuc_decide<float><<<grid, 256, 0, s>>>(a);
     k_nuc_fp64<float><<<fp64_blocks, 256, 0, s>>>(a);
     k_nuc_apply<float><<<1, 1024, 0, s>>>(a);
   } else {
     if (own)
-      k_nuc_decide_own<double><<<grid, 256, 0, s>>>(a);
+      k_nuc_decide_own<double><<<grid_own, 256, 0, s>>>(a);
     else
       k_nuc_decide<double><<<grid, 256, 0, s>>>(a);
     k_nuc_fp64<double><<<fp64_blocks, 256, 0, s>>>(a);

@@ -180,11 +180,16 @@ __device__ __forceinline__ void ln_z_tier1(const ZPre& p, const NucArgs& a, floa
 // tier 2 (p.ok): lnz[] holds tier 1's bounds on entry; the smaller is kept
 __device__ __forceinline__ void ln_z_tier2(float X, float Y, const ZPre& p, const NucArgs& a,
                                            float lnz[2]) {
-  // the diffusivities of thermo/parabola625.c:1860-1894 in FP32
+  // the diffusivities of thermo/parabola625.c:1860-1894 in FP32.  The fast
+  // exponential and logarithm suffice: __expf is within 2 + 1.17 |x| ulp
+  // (6e-6 relative at |x| = 44), far inside the 1e-3 relative slack added to
+  // each sum below, and __logf within 2^-21 absolute, far inside the 0.25 and
+  // kNucMargin nats the bounds carry; exponents below -87 flush to 0 where
+  // expf would give a subnormal, which the 1e-30 floor of each sum covers.
   const float xni = 1.0f - X - Y;
-  const float mNb = float(kMobPreNb) * expf(p.eNb);
-  const float mCr = float(kMobPreCr) * expf(p.eCr);
-  const float mNi = float(kMobPreNi) * expf(p.eNi);
+  const float mNb = float(kMobPreNb) * __expf(p.eNb);
+  const float mCr = float(kMobPreCr) * __expf(p.eCr);
+  const float mNi = float(kMobPreNi) * __expf(p.eNi);
   const float s0 = -float(kHCrCr) * X - float(kHCrNb) * Y;
   const float s1 = -float(kHCrNb) * X - float(kHNbNb) * Y;
   const float t0 = -mNb * X * Y * (s0 + float(kHCrNbAddA));
@@ -201,7 +206,7 @@ __device__ __forceinline__ void ln_z_tier2(float X, float Y, const ZPre& p, cons
   }
   // ln of |D_kk| x_k: the positive part's upper bound, or the magnitude's
   // lower bound where the upper bound is negative
-  const float lDX = logf(fabsf(dcc_up) * X), lDY = logf(fabsf(dnn_up) * Y);
+  const float lDX = __logf(fabsf(dcc_up) * X), lDY = __logf(fabsf(dnn_up) * Y);
   const float rCr = __fdividef(1.0f, p.dcCr), rNb = __fdividef(1.0f, p.dcNb);
 #pragma unroll
   for (int ph = 0; ph < 2; ph++) {
@@ -314,10 +319,11 @@ __device__ __forceinline__ void append_events(const NucArgs& a, bool ev, const N
 //    every draw -- no event, no draw needed;
 //  * else draw (w), and leave the cell to the FP64 decision unless u >= hi32
 //    2^-32 (rounded toward zero) >= P_up >= P_nuc for both phases.
-// Returns true when the FP64 decision is needed.  The first tier runs inline;
-// the rest (second tier, draw) is a call taken only by the lanes the first
-// tier leaves open, so its registers do not weigh on every thread.
-__device__ __noinline__ bool nuc_screen_rest(const NucArgs& a, float X, float Y, long long idx,
+// Returns true when the FP64 decision is needed.  The first tier settles
+// about 70 % of the warps of the enriched-stripe workloads; the second tier
+// and the draw are inlined for the rest (a call passed its arguments through
+// the stack, which cost more than the registers inlining adds).
+__device__ __forceinline__ bool nuc_screen_rest(const NucArgs& a, float X, float Y, long long idx,
                                              const ZPre p, float lnz0, float lnz1, uint4* wout) {
   float lnz[2] = {lnz0, lnz1};
   if (p.ok) ln_z_tier2(X, Y, p, a, lnz);
