@@ -254,6 +254,34 @@ def nine_point_mask(dx, dy):
     return m
 
 
+# checkpoint files: one .npz with the FP64 fields (cr, nb, pd, pl), the mask
+# (2D), a JSON `meta` record and, for the FP32 forms, the raw records
+CHECKPOINT_FORMAT = "pfa-gb300-checkpoint-1"
+
+
+def _load_checkpoint(path, dim):
+    """(meta, fields, mask or None, FP32 record bytes or None) of a checkpoint
+    file written by Grid2D / Grid3D .checkpoint for a grid of `dim`
+    dimensions; ValueError for anything else."""
+    import json
+    with np.load(path) as z:
+        if "meta" not in z.files:
+            raise ValueError(f"{path}: not a checkpoint file (no meta record)")
+        meta = json.loads(str(z["meta"]))
+        if meta.get("format") != CHECKPOINT_FORMAT:
+            raise ValueError(f"{path}: checkpoint format {meta.get('format')!r}, "
+                             f"expected {CHECKPOINT_FORMAT!r}")
+        if meta.get("dim") != dim:
+            raise ValueError(f"{path}: a {meta.get('dim')}D checkpoint, not {dim}D")
+        fields = [z[k] for k in ("cr", "nb", "pd", "pl")]
+        shape = fields[0].shape
+        if len(shape) != dim or any(f.shape != shape for f in fields):
+            raise ValueError(f"{path}: field arrays of shapes {[f.shape for f in fields]}")
+        mask = z["mask"] if "mask" in z.files else None
+        raw = np.ascontiguousarray(z["f32_state"]) if "f32_state" in z.files else None
+    return meta, fields, mask, raw
+
+
 def model_params(dx=5e-9, ifce_width=10e-9, xcr0=0.30, xnb0=0.02, meshres=None, dim=2,
                  dt_rule=1):
     """Model parameters from the library (src/main.cpp:252-268; see pfa_gb300.h)."""
@@ -330,28 +358,31 @@ class Grid2D:
             raw = np.empty(nb, dtype=np.uint8)
             check(self.L.pfa_read_f32_state(self.ref, raw.ctypes.data, nb), "pfa_read_f32_state")
             extra["f32_state"] = raw
-        meta = dict(params=self.params, precision=self.precision, mode=self.mode,
-                    mobility=self.mobility, nucleation=self.nucleation,
-                    steps=int(steps.value), nucleation_calls=int(calls.value))
+        meta = dict(format=CHECKPOINT_FORMAT, dim=2, params=self.params,
+                    precision=self.precision, mode=self.mode, mobility=self.mobility,
+                    nucleation=self.nucleation, steps=int(steps.value),
+                    nucleation_calls=int(calls.value))
         np.savez(path, cr=fields[0], nb=fields[1], pd=fields[2], pl=fields[3], mask=self.mask,
                  meta=np.array(json.dumps(meta)), **extra)
 
     @classmethod
     def resume(cls, path):
-        """A new handle in the state a checkpoint() file holds."""
-        import json
-        z = np.load(path)
-        meta = json.loads(str(z["meta"]))
-        g = cls([z[k] for k in ("cr", "nb", "pd", "pl")], meta["params"],
-                precision=meta["precision"], mode=meta["mode"], mask=z["mask"],
-                mobility=meta["mobility"])
-        if meta["nucleation"]:
-            g.set_nucleation(**meta["nucleation"])
-        check(g.L.pfa_set_counters(g.ref, meta["steps"], meta["nucleation_calls"]),
-              "pfa_set_counters")
-        if "f32_state" in z.files:
-            raw = np.ascontiguousarray(z["f32_state"])
-            check(g.L.pfa_write_f32_state(g.ref, raw.ctypes.data, raw.size), "pfa_write_f32_state")
+        """A new handle in the state a checkpoint() file holds (ValueError,
+        before any device work, for a file of another format or a 3D grid)."""
+        meta, fields, mask, raw = _load_checkpoint(path, dim=2)
+        g = cls(fields, meta["params"], precision=meta["precision"], mode=meta["mode"],
+                mask=mask, mobility=meta["mobility"])
+        try:
+            if meta["nucleation"]:
+                g.set_nucleation(**meta["nucleation"])
+            check(g.L.pfa_set_counters(g.ref, meta["steps"], meta["nucleation_calls"]),
+                  "pfa_set_counters")
+            if raw is not None:
+                check(g.L.pfa_write_f32_state(g.ref, raw.ctypes.data, raw.size),
+                      "pfa_write_f32_state")
+        except BaseException:
+            g.close()
+            raise
         return g
 
     def run(self, nsteps, dt=None, alpha=None):
@@ -541,27 +572,29 @@ class Grid3D:
             raw = np.empty(nb, dtype=np.uint8)
             check(self.L.pfa3d_read_f32_state(self.h, raw.ctypes.data, nb), "pfa3d_read_f32_state")
             extra["f32_state"] = raw
-        meta = dict(params=self.params, precision=self.precision, nucleation=self.nucleation,
+        meta = dict(format=CHECKPOINT_FORMAT, dim=3, params=self.params,
+                    precision=self.precision, nucleation=self.nucleation,
                     steps=int(steps.value), nucleation_calls=int(calls.value))
         np.savez(path, cr=fields[0], nb=fields[1], pd=fields[2], pl=fields[3],
                  meta=np.array(json.dumps(meta)), **extra)
 
     @classmethod
     def resume(cls, path):
-        """A new 3D handle in the state a checkpoint() file holds."""
-        import json
-        z = np.load(path)
-        meta = json.loads(str(z["meta"]))
-        g = cls([z[k] for k in ("cr", "nb", "pd", "pl")], meta["params"],
-                precision=meta["precision"])
-        if meta["nucleation"]:
-            g.set_nucleation(**meta["nucleation"])
-        check(g.L.pfa3d_set_counters(g.h, meta["steps"], meta["nucleation_calls"]),
-              "pfa3d_set_counters")
-        if "f32_state" in z.files:
-            raw = np.ascontiguousarray(z["f32_state"])
-            check(g.L.pfa3d_write_f32_state(g.h, raw.ctypes.data, raw.size),
-                  "pfa3d_write_f32_state")
+        """A new 3D handle in the state a checkpoint() file holds (ValueError,
+        before any device work, for a file of another format or a 2D grid)."""
+        meta, fields, _, raw = _load_checkpoint(path, dim=3)
+        g = cls(fields, meta["params"], precision=meta["precision"])
+        try:
+            if meta["nucleation"]:
+                g.set_nucleation(**meta["nucleation"])
+            check(g.L.pfa3d_set_counters(g.h, meta["steps"], meta["nucleation_calls"]),
+                  "pfa3d_set_counters")
+            if raw is not None:
+                check(g.L.pfa3d_write_f32_state(g.h, raw.ctypes.data, raw.size),
+                      "pfa3d_write_f32_state")
+        except BaseException:
+            g.close()
+            raise
         return g
 
     def events(self, cap=1 << 16):
