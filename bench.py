@@ -390,6 +390,11 @@ def grid4096(c, quick_error=True):
     gv.run(2)
     msv = gv.run_timed(10) / 10
     gv.close()
+    # and its FP32 form (the flux as div (D(X, Y) grad x^gamma), Kahan-compensated)
+    gw = pl.Grid2D(fields, params, precision=args.precision, mobility="variable")
+    gw.run(3)
+    msw = gw.run_timed(STEPS_PER_BENCH_STEP) / STEPS_PER_BENCH_STEP
+    gw.close()
 
     err = None
     if quick_error:
@@ -490,6 +495,12 @@ def grid4096(c, quick_error=True):
                                        "ms_per_step": msv,
                                        "what": "the reference's disabled variable-mobility "
                                                "Cahn-Hilliard, FP64 (pfa_set_mobility)"}},
+        "variable_mobility_fp32": {"value": cells / (msw / 1e3), "unit": "cell-updates/s",
+                                   "ms_per_step": msw, "speedup_over_fp64": msv / msw,
+                                   "bytes_per_cell": 48,
+                                   "hbm_frac": 48 * cells / (msw / 1e3) / 1e9 / roof["peak"],
+                                   "what": "the variable-mobility step in the FP32 form "
+                                           f"({args.precision}), no nucleation"},
         "roofline": roof,
         "cpu_baseline": cpu,
         "reference_gpu": ref_gpu,

@@ -226,6 +226,13 @@ static Step2DArgs step_args(State* s, double alpha, double dt) {
   a.lap9[2] = float(s->mask9[0]);
   a.lap9[3] = float(sum);
   for (int k = 0; k < 2; k++) a.lap9xe[k] = float(sum * kXe[0][k]);
+  // the FP32 form's variable-mobility step takes the diffusivity matrix
+  // already scaled by dt / (2 dx^2) (the x faces' weight of the divergence)
+  const double r2x = 0.5 * dt * s->m.idx2[0];
+  a.vm_pre[0] = float(kMobPreNb * r2x);
+  a.vm_pre[1] = float(kMobPreCr * r2x);
+  a.vm_pre[2] = float(kMobPreNi * r2x);
+  a.vm_qy = s->m.idx2[0] > 0.0 ? float(s->m.idx2[1] / s->m.idx2[0]) : 0.0f;
   return a;
 }
 
@@ -961,8 +968,8 @@ int pfa_set_precision(struct CudaData* dev, int precision) {
   if (precision < PFA_FP64 || precision > PFA_FP32_KPHI) return fail(PFA_EINVAL, "pfa_set_precision");
   if (precision != PFA_FP64 && s->mode == PFA_MODE_COMPAT)
     return fail(PFA_EINVAL, "compat mode is FP64 only");
-  if (precision != PFA_FP64 && s->varmob)
-    return fail(PFA_EINVAL, "the variable mobility is an FP64 form");
+  if (precision != PFA_FP64 && s->varmob && (!s->five_point || !s->zero_sum))
+    return fail(PFA_EINVAL, "the FP32 variable-mobility step needs the 5-point mask");
   if (precision != PFA_FP64 && !fp32_records_fit(s->Nx, s->Ny))
     return fail(PFA_EINVAL, "grid above 2^31 records (the FP32 form's 32-bit index)");
   if (precision == s->precision) return 0;
@@ -981,8 +988,8 @@ int pfa_set_mobility(struct CudaData* dev, int model) {
   if (model != PFA_MOBILITY_CONSTANT && model != PFA_MOBILITY_VARIABLE)
     return fail(PFA_EINVAL, "pfa_set_mobility: model");
   if (model == PFA_MOBILITY_VARIABLE) {
-    if (s->precision != PFA_FP64)
-      return fail(PFA_EINVAL, "the variable mobility is an FP64 form (pfa_set_precision PFA_FP64)");
+    if (s->precision != PFA_FP64 && (!s->five_point || !s->zero_sum))
+      return fail(PFA_EINVAL, "the FP32 variable-mobility step needs the 5-point mask");
     if (s->mode == PFA_MODE_FUSED && !s->five_point)
       return fail(PFA_EINVAL, "the fused variable-mobility step needs the 5-point mask");
   }

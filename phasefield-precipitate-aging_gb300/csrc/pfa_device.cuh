@@ -177,6 +177,29 @@ __device__ __forceinline__ float pp32(float x) {
   return 30.0f * (x * x) * (y * y);
 }
 
+// The diffusivity matrix D(X, Y) of dmatrix64 (thermo/parabola625.c:1860-1894)
+// in FP32, with the mobility prefactors (Nb, Cr, Ni) passed in `pre` already
+// multiplied by a scale the caller chooses (dt / (2 dx^2) in the FP32
+// variable-mobility step, which keeps the entries near 1e-4 .. 1e-1).  The
+// mobility exponents are at most 14.5 on the composition simplex, so no
+// exponential overflows; a term whose exponential underflows is negligible.
+__device__ __forceinline__ void dmat32(const float pre[3], float X, float Y, float& d00,
+                                       float& d01, float& d10, float& d11) {
+  const float xni = 1.0f - X - Y;
+  const float eNb = pre[0] * expf(fmaf(-34.982563536715503f * Y, xni, 14.437947842988088f * Y));
+  const float eCr = pre[1] * expf(fmaf(-7.1543718172640256f * X, xni, 3.3541967644499233f * X));
+  const float eNi = pre[2] * expf(fmaf(-8.5221193705645018f * X, xni, 4.0036674816806448f * X) -
+                                  fmaf(442.62877981749585f * Y, xni, 0.82164267100913768f * Y));
+  const float s0 = -float(kHCrCr) * X - float(kHCrNb) * Y;  // curvature row of the Cr column
+  const float s1 = -float(kHCrNb) * X - float(kHNbNb) * Y;  // of the Nb column
+  const float xy = X * Y, xx = X * (1.0f - X), yy = Y * (1.0f - Y);
+  const float niX = eNi * X * xni, niY = eNi * Y * xni;
+  d00 = -eNb * xy * (s0 + float(kHCrNbAddA)) + eCr * xx * (s0 + float(kHCrCrAdd)) - niX * s0;
+  d01 = -eNb * xy * (s1 + float(kHNbNbAdd)) + eCr * xx * (s1 + float(kHCrNbAddB)) - niX * s1;
+  d10 = -eCr * xy * (s0 + float(kHCrCrAdd)) + eNb * yy * (s0 + float(kHCrNbAddA)) - niY * s0;
+  d11 = -eCr * xy * (s1 + float(kHCrNbAddB)) + eNb * yy * (s1 + float(kHNbNbAdd)) - niY * s1;
+}
+
 // c0 + a (c1 + c11 a + c12 b) + b (c2 + c22 b), coefficients in the order
 // c0 c1 c2 c11 c12 c22
 __device__ __forceinline__ float quad2(const float* c, float a, float b) {

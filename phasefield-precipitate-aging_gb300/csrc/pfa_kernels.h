@@ -35,6 +35,9 @@ struct Step2DArgs {
   float lap9[4];        // FP32 form, 9-point mask (symmetric): left / right weight,
                         // upper / lower weight, corner weight, sum of the nine
   float lap9xe[2];      // the sum of the nine weights times xe_gamma (Cr, Nb)
+  float vm_pre[3];      // FP32 form, variable mobility: the mobility prefactors
+                        // (Nb, Cr, Ni) times dt / (2 dx^2)
+  float vm_qy;          // and the weight of the y faces, (1/dy^2) / (1/dx^2)
   int rows;             // FP32 form: rows per warp segment (set by the launcher)
 };
 

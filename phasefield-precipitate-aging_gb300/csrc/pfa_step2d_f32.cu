@@ -55,8 +55,17 @@ struct Nb9 {
   float h1, h2, hd, hl;
 };
 
-template <bool NINE>
-using NbT = typename std::conditional<NINE, Nb9, Nb>::type;
+// With the variable mobility a row also carries each cell's diffusivity
+// matrix D(X, Y), scaled by dt / (2 dx^2) (dev::dmat32), for the face sums of
+// the divergence.
+struct NbV {
+  float u1, u2, pd, pl;
+  float d00, d01, d10, d11;
+};
+
+template <bool NINE, bool VM = false>
+using NbT = typename std::conditional<NINE, Nb9,
+                                      typename std::conditional<VM, NbV, Nb>::type>::type;
 
 // Compensation record: packed 16-bit counts or four FP32 values.
 template <bool PACK>
@@ -109,7 +118,7 @@ __device__ __forceinline__ float2 comps_x(const CompT<PACK>& c) {
   }
 }
 
-template <bool PACK, bool NINE>
+template <bool PACK, bool NINE, bool VM = false>
 struct Stream {
   const Step2DArgs& a;
   const float4* A;        // this lane's column, row 0
@@ -126,10 +135,42 @@ struct Stream {
   }
 
   // update row y from its window (up, c, dn); rc = raw centre record
-  __device__ __forceinline__ void update(int y, const NbT<NINE>& up, const NbT<NINE>& c,
-                                         const NbT<NINE>& dn, const Raw<PACK>& rc) const {
+  __device__ __forceinline__ void update(int y, const NbT<NINE, VM>& up, const NbT<NINE, VM>& c,
+                                         const NbT<NINE, VM>& dn, const Raw<PACK>& rc) const {
     float lapCr, lapNb, lapD, lapL;
-    if constexpr (NINE) {
+    if constexpr (VM) {
+      // variable mobility: lapCr, lapNb hold dt times the divergence of
+      // D grad u over the four faces, ((D_n + D_c)(u_n - u_c) summed), the
+      // matrices already scaled by dt / (2 dx^2), y faces weighted by qy
+      NbV w, e;
+      auto sh = [](float v, float& wv, float& ev) {
+        wv = __shfl_up_sync(0xffffffffu, v, 1);
+        ev = __shfl_down_sync(0xffffffffu, v, 1);
+      };
+      sh(c.u1, w.u1, e.u1);
+      sh(c.u2, w.u2, e.u2);
+      sh(c.pd, w.pd, e.pd);
+      sh(c.pl, w.pl, e.pl);
+      sh(c.d00, w.d00, e.d00);
+      sh(c.d01, w.d01, e.d01);
+      sh(c.d10, w.d10, e.d10);
+      sh(c.d11, w.d11, e.d11);
+      // flux of component row (r0, r1) of D into the centre from neighbour n
+      auto in = [&](const NbV& n, float n0, float n1, float c0, float c1) {
+        return fmaf(n0 + c0, n.u1 - c.u1, (n1 + c1) * (n.u2 - c.u2));
+      };
+      const float qy = a.vm_qy;
+      lapCr = (in(w, w.d00, w.d01, c.d00, c.d01) + in(e, e.d00, e.d01, c.d00, c.d01)) +
+              qy * (in(up, up.d00, up.d01, c.d00, c.d01) + in(dn, dn.d00, dn.d01, c.d00, c.d01));
+      lapNb = (in(w, w.d10, w.d11, c.d10, c.d11) + in(e, e.d10, e.d11, c.d10, c.d11)) +
+              qy * (in(up, up.d10, up.d11, c.d10, c.d11) + in(dn, dn.d10, dn.d11, c.d10, c.d11));
+      const float idx2 = a.idx2f[0], idy2 = a.idx2f[1];
+      auto lap = [&](float vw, float ve, float vn, float vs, float vc) {
+        return fmaf((vw - vc) + (ve - vc), idx2, ((vn - vc) + (vs - vc)) * idy2);
+      };
+      lapD = lap(w.pd, e.pd, up.pd, dn.pd, c.pd);
+      lapL = lap(w.pl, e.pl, up.pl, dn.pl, c.pl);
+    } else if constexpr (NINE) {
       // sum over the eight neighbours of w (v - v_c): with sy = (v_up - v_c)
       // + (v_dn - v_c) the corners add up to h_up + h_dn + 2 sy; then the
       // sum of the nine weights times the centre value (zero for dx = dy up
@@ -170,8 +211,15 @@ struct Stream {
     const float4 cc = comps<PACK>(rc.c);
     // Cahn-Hilliard
     const float X = rc.a.x, Y = rc.a.y;
-    const float ycr = fmaf(a.dtD[0][0], lapCr, a.dtD[0][1] * lapNb) - cc.x, tcr = X + ycr;
-    const float ynb = fmaf(a.dtD[1][0], lapCr, a.dtD[1][1] * lapNb) - cc.y, tnb = Y + ynb;
+    float ycr, ynb;
+    if constexpr (VM) {
+      ycr = lapCr - cc.x;
+      ynb = lapNb - cc.y;
+    } else {
+      ycr = fmaf(a.dtD[0][0], lapCr, a.dtD[0][1] * lapNb) - cc.x;
+      ynb = fmaf(a.dtD[1][0], lapCr, a.dtD[1][1] * lapNb) - cc.y;
+    }
+    const float tcr = X + ycr, tnb = Y + ynb;
     // Allen-Cahn
     const FastCoef& K = a.k;
     const float phd = c.pd, phl = c.pl;
@@ -198,7 +246,7 @@ struct Stream {
 // directly (one row ahead, !STAGED) or through the warp's staging ring
 // (STAGED): the batched kernel's units are short, and the ring's deeper
 // prefetch hides the start-up latency each unit pays.
-template <bool PACK, bool STAGED, bool NINE = false>
+template <bool PACK, bool STAGED, bool NINE = false, bool VM = false>
 __device__ __forceinline__ void stream_strip(const Step2DArgs& a, const float4* Ain,
                                              const CompT<PACK>* Bin, float4* Aout,
                                              CompT<PACK>* Bout, int Nx, int Ny, int P, int x0,
@@ -207,12 +255,14 @@ __device__ __forceinline__ void stream_strip(const Step2DArgs& a, const float4* 
   const int gx = x0 - 1 + lane;  // lanes 0 and 31 hold the neighbour columns
   const int cx = min(max(gx, 0), Nx - 1);
   static_assert(!(STAGED && NINE), "the staged (batched) form has the 5-point mask only");
+  static_assert(!(STAGED && VM), "the staged (batched) form has the constant mobility only");
+  static_assert(!(NINE && VM), "the variable-mobility form has the 5-point mask only");
   const FastCoef& K = a.k;
-  const Stream<PACK, NINE> S{a, Ain + cx, Bin + cx, Aout + cx, Bout + cx,
+  const Stream<PACK, NINE, VM> S{a, Ain + cx, Bin + cx, Aout + cx, Bout + cx,
                              Ny, P, lane >= 1 && lane <= kCols && gx < Nx};
   auto solve_raw = [&](const Raw<PACK>& r) {
     const float2 cxy = comps_x<PACK>(r.c);
-    NbT<NINE> n;
+    NbT<NINE, VM> n;
     n.pd = r.a.z;
     n.pl = r.a.w;
     // warp-uniform choice: a row of pure gamma needs no solve
@@ -220,6 +270,7 @@ __device__ __forceinline__ void stream_strip(const Step2DArgs& a, const float4* 
       gamma_bulk32(K, r.a.x, r.a.y, cxy.x, cxy.y, n.u1, n.u2);
     else
       gamma_u32(K, r.a.x, r.a.y, cxy.x, cxy.y, r.a.z, r.a.w, n.u1, n.u2);
+    if constexpr (VM) dmat32(a.vm_pre, r.a.x, r.a.y, n.d00, n.d01, n.d10, n.d11);
     if constexpr (NINE) {
       auto hx = [](float v) {
         return (__shfl_up_sync(0xffffffffu, v, 1) - v) + (__shfl_down_sync(0xffffffffu, v, 1) - v);
@@ -234,7 +285,7 @@ __device__ __forceinline__ void stream_strip(const Step2DArgs& a, const float4* 
   if constexpr (!STAGED) {
     // window rows y-1, y, y+1 and raw records of rows y, y+1, y+2
     Raw<PACK> r0 = S.load(S.row(y0)), r1 = S.load(S.row(y0 + 1)), r2;
-    NbT<NINE> n0 = solve_raw(S.load(S.row(y0 - 1))), n1 = solve_raw(r0), n2;
+    NbT<NINE, VM> n0 = solve_raw(S.load(S.row(y0 - 1))), n1 = solve_raw(r0), n2;
     // three rows per iteration with rotated roles: no register moves
     int y = y0;
     for (; y + 2 < y1; y += 3) {
@@ -309,13 +360,14 @@ __device__ __forceinline__ void stream_strip(const Step2DArgs& a, const float4* 
 // warps cover load latency (4096^2: 0.1303 ms vs 0.1369 ms at 8); the FP32
 // compensation form is faster at 8.  NINE: the 9-point mask (a window of
 // eight values per row).
-template <bool PACK, bool NINE>
-__global__ void __launch_bounds__(32 * kWarps, PACK && !NINE ? 9 : 8) k_stream_f32(Step2DArgs a) {
+template <bool PACK, bool NINE, bool VM = false>
+__global__ void __launch_bounds__(32 * kWarps, VM ? 6 : (PACK && !NINE ? 9 : 8))
+    k_stream_f32(Step2DArgs a) {
   const int strip = blockIdx.x * kWarps + (threadIdx.x >> 5);
   const int x0 = strip * kCols;  // first output column of the strip
   if (x0 >= a.Nx) return;        // whole warp leaves together
   const int y0 = blockIdx.y * a.rows;
-  stream_strip<PACK, false, NINE>(a, static_cast<const float4*>(a.in[0]),
+  stream_strip<PACK, false, NINE, VM>(a, static_cast<const float4*>(a.in[0]),
                             static_cast<const CompT<PACK>*>(a.in[1]),
                             static_cast<float4*>(a.out[0]), static_cast<CompT<PACK>*>(a.out[1]),
                             a.Nx, a.Ny, a.pitch, x0, y0, min(y0 + a.rows, a.Ny), nullptr);
@@ -421,8 +473,9 @@ int segment_rows(int Nx, int Ny, int resident) {
   return best;
 }
 
-// resident CTAs: FP32 / packed variants, the batch kernel, the 9-point FP32 / packed variants
-int g_resident[5] = {0, 0, 0, 0, 0};
+// resident CTAs: FP32 / packed variants, the batch kernel, the 9-point FP32 / packed
+// variants, the variable-mobility FP32 / packed variants
+int g_resident[7] = {0, 0, 0, 0, 0, 0, 0};
 
 template <typename K>
 cudaError_t query_resident(K kernel, int slot) {
@@ -435,20 +488,25 @@ cudaError_t query_resident(K kernel, int slot) {
   return e;
 }
 
-template <bool PACK, bool NINE>
+template <bool PACK, bool NINE, bool VM = false>
 cudaError_t launch_stream(Step2DArgs a, cudaStream_t s) {
-  const int slot = NINE ? 3 + PACK : PACK;
+  const int slot = VM ? 5 + PACK : (NINE ? 3 + PACK : PACK);
   const int resident = g_resident[slot] > 0 ? g_resident[slot] : 152 * 8;
   a.rows = segment_rows(a.Nx, a.Ny, resident);
   const int strips = (a.Nx + kCols - 1) / kCols;
   dim3 grid((strips + kWarps - 1) / kWarps, (a.Ny + a.rows - 1) / a.rows);
-  k_stream_f32<PACK, NINE><<<grid, 32 * kWarps, 0, s>>>(a);
+  k_stream_f32<PACK, NINE, VM><<<grid, 32 * kWarps, 0, s>>>(a);
   return cudaGetLastError();
 }
 
 }  // namespace
 
 cudaError_t launch_step2d_f32(const Step2DArgs& a, cudaStream_t s) {
+  if (a.varmob) {
+    if (a.nine) return cudaErrorInvalidValue;  // refused by the host before
+    return a.full_comp ? launch_stream<false, false, true>(a, s)
+                       : launch_stream<true, false, true>(a, s);
+  }
   if (a.nine) return a.full_comp ? launch_stream<false, true>(a, s) : launch_stream<true, true>(a, s);
   return a.full_comp ? launch_stream<false, false>(a, s) : launch_stream<true, false>(a, s);
 }
@@ -460,6 +518,8 @@ cudaError_t prepare_step2d_f32() {
   if (e == cudaSuccess) e = query_resident(k_batch_f32, 2);
   if (e == cudaSuccess) e = query_resident(k_stream_f32<false, true>, 3);
   if (e == cudaSuccess) e = query_resident(k_stream_f32<true, true>, 4);
+  if (e == cudaSuccess) e = query_resident(k_stream_f32<false, false, true>, 5);
+  if (e == cudaSuccess) e = query_resident(k_stream_f32<true, false, true>, 6);
   return e;
 }
 

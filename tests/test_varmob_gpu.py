@@ -111,14 +111,77 @@ def test_variable_mobility_is_not_the_constant_form(pfa):
         x.close()
 
 
-def test_variable_mobility_rejects_the_fp32_forms(pfa):
+def test_fp32_variable_mobility_needs_the_five_point_mask(pfa):
+    """The FP32 forms take the variable mobility with the 5-point mask, in
+    either order of the two settings, and refuse it with the 9-point mask."""
     g = golden("step2d_varmob.npz")
-    grid = pfa.Grid2D(fields_of(g, "g0_ic"), pfa.model_params(), precision="fp32")
+    f = fields_of(g, "g0_ic")
+    p = pfa.model_params()
     L = pfa.load()
+    grid = pfa.Grid2D(f, p, precision="fp32")
+    pfa.check(L.pfa_set_mobility(grid.ref, pfa.MOBILITY_VARIABLE), "pfa_set_mobility")
+    grid.close()
+    grid = pfa.Grid2D(f, p, mobility="variable")
+    pfa.check(L.pfa_set_precision(grid.ref, pfa.FP32), "pfa_set_precision")
+    grid.close()
+    m9 = pfa.nine_point_mask(p["dx"], p["dx"])
+    grid = pfa.Grid2D(f, p, mask=m9, precision="fp32")
     assert L.pfa_set_mobility(grid.ref, pfa.MOBILITY_VARIABLE) == 1  # PFA_EINVAL
     L.pfa_clear_error()
-    grid.set_precision("fp64")
-    pfa.check(L.pfa_set_mobility(grid.ref, pfa.MOBILITY_VARIABLE), "pfa_set_mobility")
-    assert L.pfa_set_precision(grid.ref, pfa.FP32) == 1
+    grid.close()
+    grid = pfa.Grid2D(f, p, mask=m9, mode="compat", mobility="variable")
+    assert L.pfa_set_precision(grid.ref, pfa.FP32) == 1  # compat mode is FP64 only
     L.pfa_clear_error()
     grid.close()
+
+
+# The FP32 variable-mobility step against the FP64 one (itself pinned above).
+# The FP32 form evaluates the flux as div (D(X, Y) grad x^gamma): with
+# paraboloid energies the fictitious compositions share their diffusion
+# potentials, so x^phase = T_phase x^gamma + const with T_phase = H_phase^-1
+# H_gamma, each phase's coefficients compose to p_phase D, and the phase
+# gradient terms vanish -- the same discrete face sums as the 16-coefficient
+# FP64 form, up to rounding.  Tolerance: max |FP32 - FP64| per field over the
+# interior, 1e-7 after one step, 1e-5 after the 1000 steps of C1.
+FP32_VM_ONE_STEP = 1e-7
+FP32_VM_TOL = 1e-5
+
+
+def _vm_err(pfa, f, steps, precision):
+    p = pfa.model_params()
+    a = pfa.Grid2D(f, p, mobility="variable")
+    b = pfa.Grid2D(f, p, mobility="variable", precision=precision)
+    a.run(steps)
+    b.run(steps)
+    ra, rb = a.read(), b.read()
+    a.close()
+    b.close()
+    return [float(np.max(np.abs(x[1:-1, 1:-1] - y[1:-1, 1:-1]))) for x, y in zip(ra, rb)], ra, rb
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp32k"])
+def test_fp32_variable_mobility_matches_fp64(pfa, precision):
+    from pfa_gb300 import ic
+    f = ic.config1()
+    err, _, _ = _vm_err(pfa, f, 1, precision)
+    assert max(err) <= FP32_VM_ONE_STEP, err
+    err, ra, rb = _vm_err(pfa, f, 1000, precision)
+    assert max(err) <= FP32_VM_TOL, err
+    # the divergence acts: the constant-mobility FP32 step ends elsewhere
+    c = pfa.Grid2D(f, pfa.model_params(), precision=precision)
+    c.run(1000)
+    rc = c.read()
+    c.close()
+    assert max(float(np.max(np.abs(x - y))) for x, y in zip(rb[:2], rc[:2])) > 100 * FP32_VM_TOL
+
+
+@pytest.mark.parametrize("shape", [(1, 1), (5, 7), (17, 13), (33, 65), (100, 3), (31, 61)])
+def test_fp32_variable_mobility_on_odd_sizes(pfa, shape):
+    """Ragged strips (widths that are not multiples of 30) and short row
+    segments, 60 steps, against the FP64 variable-mobility step."""
+    from pfa_gb300 import ic
+    ny, nx = shape
+    f = ic.grid2d(nx, ny, seed=nx * 7 + ny, stripe_width=max(1, nx // 3),
+                  n_particles=1 if min(nx, ny) > 12 else 0, radius=3.0)
+    err, _, _ = _vm_err(pfa, f, 60, "fp32")
+    assert max(err) <= 1e-6, (shape, err)
