@@ -141,29 +141,34 @@ struct Stream {
     if constexpr (VM) {
       // variable mobility: lapCr, lapNb hold dt times the divergence of
       // D grad u over the four faces, ((D_n + D_c)(u_n - u_c) summed), the
-      // matrices already scaled by dt / (2 dx^2), y faces weighted by qy
-      NbV w, e;
-      auto sh = [](float v, float& wv, float& ev) {
-        wv = __shfl_up_sync(0xffffffffu, v, 1);
-        ev = __shfl_down_sync(0xffffffffu, v, 1);
-      };
-      sh(c.u1, w.u1, e.u1);
-      sh(c.u2, w.u2, e.u2);
-      sh(c.pd, w.pd, e.pd);
-      sh(c.pl, w.pl, e.pl);
-      sh(c.d00, w.d00, e.d00);
-      sh(c.d01, w.d01, e.d01);
-      sh(c.d10, w.d10, e.d10);
-      sh(c.d11, w.d11, e.d11);
-      // flux of component row (r0, r1) of D into the centre from neighbour n
+      // matrices already scaled by dt / (2 dx^2), y faces weighted by qy.
+      // Each lane forms the flux through its east face; its west face's is
+      // the east flux of the lane to its left (so both cells of a face use
+      // the same number, and the x fluxes conserve each component exactly).
+      auto dn1 = [](float v) { return __shfl_down_sync(0xffffffffu, v, 1); };
+      auto up1 = [](float v) { return __shfl_up_sync(0xffffffffu, v, 1); };
+      NbV e;
+      e.u1 = dn1(c.u1);
+      e.u2 = dn1(c.u2);
+      e.d00 = dn1(c.d00);
+      e.d01 = dn1(c.d01);
+      e.d10 = dn1(c.d10);
+      e.d11 = dn1(c.d11);
+      // flux of component row (n0 + c0, n1 + c1) into the centre from neighbour n
       auto in = [&](const NbV& n, float n0, float n1, float c0, float c1) {
         return fmaf(n0 + c0, n.u1 - c.u1, (n1 + c1) * (n.u2 - c.u2));
       };
+      const float fCr = in(e, e.d00, e.d01, c.d00, c.d01), fNb = in(e, e.d10, e.d11, c.d10, c.d11);
       const float qy = a.vm_qy;
-      lapCr = (in(w, w.d00, w.d01, c.d00, c.d01) + in(e, e.d00, e.d01, c.d00, c.d01)) +
+      lapCr = (fCr - up1(fCr)) +
               qy * (in(up, up.d00, up.d01, c.d00, c.d01) + in(dn, dn.d00, dn.d01, c.d00, c.d01));
-      lapNb = (in(w, w.d10, w.d11, c.d10, c.d11) + in(e, e.d10, e.d11, c.d10, c.d11)) +
+      lapNb = (fNb - up1(fNb)) +
               qy * (in(up, up.d10, up.d11, c.d10, c.d11) + in(dn, dn.d10, dn.d11, c.d10, c.d11));
+      Nb w;
+      w.pd = up1(c.pd);
+      w.pl = up1(c.pl);
+      e.pd = dn1(c.pd);
+      e.pl = dn1(c.pl);
       const float idx2 = a.idx2f[0], idy2 = a.idx2f[1];
       auto lap = [&](float vw, float ve, float vn, float vs, float vc) {
         return fmaf((vw - vc) + (ve - vc), idx2, ((vn - vc) + (vs - vc)) * idy2);
