@@ -234,3 +234,41 @@ def test_variable_mobility_matches_reference(orc):
             done = s
             err = field_err(f, [g[f"g{k}_s{s}_{n}"] for n in ("cr", "nb", "pd", "pl")])
             assert max(err) <= 1e-12, (k, s, err)
+
+
+def test_variable_mobility_flux_reduces_to_d_grad_gamma(orc):
+    """The identity the FP32 variable-mobility form rests on, on the oracle's
+    restatement: (1) the three phases' fictitious compositions share their
+    diffusion potentials (dg_phase(x^phase) = dg_gam(x^gam)); (2) hence the
+    16-coefficient divergence of the reference's mobility / chemical
+    convolution kernels equals the sum over the four faces of
+    (D_n + D_c)(x^gam_n - x^gam_c) / (2 d^2), D(X, Y) the diffusivity matrix
+    at each cell."""
+    from pfa_gb300 import ic
+    f = ic.grid2d(24, 20, seed=9, stripe_width=8, n_particles=2, radius=3.0)
+    fict, _ = orc.mobility2d(f)
+    gam, phases = fict[0:2], (fict[0:2], fict[2:4], fict[4:6])
+    for c in range(2):
+        mu = orc.dg(0, c, gam[0], gam[1])
+        for ph in (1, 2):
+            other = orc.dg(ph, c, phases[ph][0], phases[ph][1])
+            # rounding: a few ulps of the potential's terms (slopes up to
+            # 2e11 times compositions near 0.25), 1e-12 of the potential
+            assert np.max(np.abs(other - mu)) <= 1e-12 * np.max(np.abs(mu)), (ph, c)
+    dx = dy = 5e-9
+    want = orc.chem_div2d(f, dx, dy)
+    X, Y = f[0], f[1]
+    ny, nx = X.shape
+    D = [[orc.D(r, k, X.ravel(), Y.ravel()).reshape(ny, nx) for k in range(2)] for r in range(2)]
+    r2 = (0.5 / dx**2, 0.5 / dy**2)
+    for row in range(2):
+        got = np.zeros((ny - 2, nx - 2))
+        c = (slice(1, -1), slice(1, -1))
+        for (sy, sx), r in (((slice(1, -1), slice(2, None)), r2[0]),
+                            ((slice(1, -1), slice(0, -2)), r2[0]),
+                            ((slice(2, None), slice(1, -1)), r2[1]),
+                            ((slice(0, -2), slice(1, -1)), r2[1])):
+            for k in range(2):
+                got += r * (D[row][k][sy, sx] + D[row][k][c]) * (gam[k][sy, sx] - gam[k][c])
+        ref = want[row][1:-1, 1:-1]
+        assert np.max(np.abs(got - ref)) <= 1e-12 * np.max(np.abs(ref)), row  # 2e-14 seen
