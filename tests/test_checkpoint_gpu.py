@@ -101,3 +101,24 @@ def test_resumed_3d_run_is_bit_identical(pfa, tmp_path, precision):
     for x, y in zip(b.read(), want):
         assert np.array_equal(x, y), precision
     b.close()
+
+
+def test_resumed_fp32_variable_mobility_run_is_bit_identical(pfa, tmp_path):
+    """The FP32 variable-mobility step with nucleation, split at a checkpoint
+    (resume restores the precision, then the mobility, then the records)."""
+    p = pfa.model_params()
+    a = pfa.Grid2D(_grid(), p, precision="fp32", mobility="variable")
+    a.set_nucleation(geometry=pfa.NUC_FIXED_GEOMETRY, **NUC)
+    a.run(35)
+    path = str(tmp_path / "vm.npz")
+    a.checkpoint(path)
+    a.run(45)
+    want = a.read()
+    assert all(np.isfinite(x).all() for x in want)
+    a.close()
+    b = pfa.Grid2D.resume(path)
+    assert (b.precision, b.mobility) == ("fp32", "variable")
+    b.run(45)
+    for x, y in zip(b.read(), want):
+        assert np.array_equal(x, y)
+    b.close()
