@@ -64,6 +64,29 @@ def dist_env():
     return ws, rank, local
 
 
+def rank_sync(dist, device):
+    """The barrier and the max-over-ranks reduction that bracket every timed
+    region (dist None: one process).  device: where the reduction's tensor
+    lives ("cuda" under NCCL, where the barrier also waits for the device;
+    "cpu" under gloo)."""
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        if device == "cuda":
+            import torch
+            torch.cuda.synchronize()
+
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    return barrier, max_over_ranks
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -999,18 +1022,7 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
-    def barrier():
-        if dist is not None:
-            dist.barrier()
-        torch.cuda.synchronize()
-
-    def max_over_ranks(x):
-        if dist is None:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
-
+    barrier, max_over_ranks = rank_sync(dist, "cuda")
     c = Ctx(args, ws, rank, local, barrier, max_over_ranks, pl, ic)
     w = args.workload
     if w in ("all", "grid4096"):

@@ -1,7 +1,8 @@
 """bench.py's host side without a GPU: the reference arm (the CPU path timed
 on the host's cores) launched as two ranks over gloo prints exactly one
 JSON line, from rank 0, with the contract's keys; the other rank exits 0
-without work."""
+without work.  The GPU arm's barrier and max-over-ranks reduction
+(bench.rank_sync, NCCL on the GPU) run here as two gloo ranks."""
 import json
 import os
 import subprocess
@@ -29,3 +30,35 @@ def test_reference_arm_two_ranks_over_gloo(tmp_path):
         assert k in d, k
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["cpu_baseline"]["kind"] in ("port",
                                                                                   "reference")
+
+
+def _sync_rank(rank, port, out):
+    import torch.distributed as dist
+    sys.path.insert(0, ROOT)
+    import bench
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=2)
+    barrier, max_over_ranks = bench.rank_sync(dist, "cpu")
+    barrier()
+    got = max_over_ranks(1.5 + 2.0 * rank)  # rank 0: 1.5 s, rank 1: 3.5 s
+    barrier()
+    with open(os.path.join(out, f"r{rank}"), "w") as f:
+        f.write(repr(got))
+    dist.destroy_process_group()
+
+
+@pytest.mark.timeout(300)
+def test_rank_sync_over_gloo(tmp_path):
+    """The timed region's barrier and max-over-ranks reduction of the GPU arm
+    (bench.rank_sync), run as two gloo ranks: every rank gets the slowest
+    rank's time, which the whole-job rate divides by."""
+    import torch.multiprocessing as mp
+    mp.spawn(_sync_rank, args=(29541, str(tmp_path)), nprocs=2, join=True)
+    for r in range(2):
+        assert (tmp_path / f"r{r}").read_text() == "3.5"
+    if ROOT not in sys.path:
+        sys.path.insert(0, ROOT)
+    import bench
+    b, m = bench.rank_sync(None, "cpu")  # one process: identity, no barrier
+    b()
+    assert m(2.25) == 2.25
