@@ -114,6 +114,19 @@ def test_oracle_conserves_mass(orc):
     assert abs(s1[0] - s0[0]) < 1e-13 and abs(s1[1] - s0[1]) < 1e-13
 
 
+def test_oracle_variable_mobility_conserves_mass(orc):
+    """The variable-mobility Cahn-Hilliard is a divergence with zero flux
+    through the mirrored edges: the mean compositions stay put."""
+    from pfa_gb300 import ic
+    prm = O.model_params()
+    f = ic.grid2d(40, 30, seed=5, stripe_width=10, n_particles=3, radius=4.0)
+    s0 = orc.summarize(f)
+    out = orc.run2d_varmob(f, prm, 200)
+    s1 = orc.summarize(out)
+    assert abs(s1[0] - s0[0]) < 1e-13 and abs(s1[1] - s0[1]) < 1e-13
+    assert max(float(np.max(np.abs(a - b))) for a, b in zip(out[:2], f[:2])) > 1e-6  # it moved
+
+
 def test_oracle_3d_reduces_to_2d(orc):
     """A 3D grid uniform along z evolves like the 2D grid (7-point stencil with
     zero z-flux)."""
